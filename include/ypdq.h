@@ -1,0 +1,223 @@
+/*
+ * ypdq.h -- batched, device-resident C interface of the GB300 PDQ library.
+ *
+ * Plain pointers and sizes only. Device pointers are marked d_*; host pointers h_*.
+ * Every call takes a CUDA stream (ypdq_stream_t is layout-compatible with cudaStream_t;
+ * NULL means the legacy default stream). Calls are asynchronous on that stream unless
+ * their comment says otherwise. Every call returns a ypdq_status. The _host calls are
+ * the exceptions: they copy from and to host memory and block until the result is there.
+ *
+ * The reference (yume-pdq) has no batched or device API. Each entry point below replaces
+ * a per-image or per-batch reference item, cited beside it:
+ *
+ *   ypdq_hash_batch   Kernel::{jarosz_compress,dct2d,sum_of_gradients,quantize} driven by
+ *                     hash_get_threshold (src/lib.rs:427-455), plus visit_dihedrals
+ *                     (src/lib.rs:358-420), over n images per launch.
+ *   ypdq_dihedrals_batch  visit_dihedrals (src/lib.rs:358-420) on given PDQF matrices.
+ *   ypdq_scan         PDQMatcher::find of CpuMatcher (src/matching/mod.rs:336-362) and of
+ *                     VulkanMatcher (src/matching/vulkan.rs:408-472), returning every hit
+ *                     with its distance instead of a callback or the first hit.
+ *                     With capacity 0 it is PDQMatcher::scan (src/matching/mod.rs:94-102,
+ *                     232-257): the count alone says whether any row matched.
+ *   ypdq_db_*         VulkanVectorDatabase (src/matching/vulkan.rs:40-65).
+ *   ypdq_screen_host  the hash + 8-dihedral match loop of examples/end_to_end.rs:68-140,
+ *                     as one call from host buffers.
+ */
+#ifndef YPDQ_GB300_H
+#define YPDQ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *ypdq_stream_t;
+typedef struct ypdq_ctx ypdq_ctx;
+typedef struct ypdq_db ypdq_db;
+
+typedef enum {
+  YPDQ_OK = 0,
+  YPDQ_ERR_INVALID = 1,   /* bad argument: NULL where not allowed, size or enum out of range */
+  YPDQ_ERR_ALIGN = 2,     /* a pointer is not 16-byte aligned where the call requires it */
+  YPDQ_ERR_CUDA = 3,      /* a CUDA runtime call failed; ypdq_last_error() has the text */
+  YPDQ_ERR_NOMEM = 4,     /* device or pinned-host allocation failed */
+  YPDQ_ERR_OVERFLOW = 5,  /* more hits than capacity; the count holds the true total */
+  YPDQ_ERR_TIMEOUT = 6,   /* a device-side wait ran past its limit and the kernel gave up */
+  YPDQ_ERR_UNSUPPORTED = 7
+} ypdq_status;
+
+/* Input pixel format of 512x512 grayscale images, row-major, values 0..255. */
+typedef enum { YPDQ_INPUT_F32 = 0, YPDQ_INPUT_U8 = 1 } ypdq_input_kind;
+
+/* DCT arithmetic. FP32 reproduces yume-pdq's scalar f32 kernel bit for bit. */
+typedef enum {
+  YPDQ_DCT_FP32 = 0,      /* SIMT f32, no fused multiply-add, reference operation order */
+  YPDQ_DCT_TF32 = 1,      /* tensor cores, TF32 inputs, f32 accumulate */
+  YPDQ_DCT_BF16X3 = 2     /* tensor cores, split bf16 (hi*hi + hi*lo + lo*hi), f32 accumulate */
+} ypdq_dct_precision;
+
+/*
+ * Sign conventions of the dihedral derivation. yume-pdq's kernels disagree:
+ *   EXACT  = Avx512F32Kernel: negate rows 0,2,..,14 and columns 0,2,..,14, which is the
+ *            sign pattern of a real flip/flop of the image (src/kernel/x86.rs:989-1079).
+ *   AVX2   = Avx2F32Kernel: rows 0,2,..,14 but columns 0,2,4,6 only
+ *            (src/kernel/x86.rs:285-378).
+ *   SCALAR = trait default used by DefaultKernel / ReferenceKernel: rows 1,3,..,15,
+ *            columns 0,2,..,14 (src/kernel/mod.rs:345-406).
+ */
+typedef enum {
+  YPDQ_DIHEDRAL_EXACT = 0,
+  YPDQ_DIHEDRAL_AVX2 = 1,
+  YPDQ_DIHEDRAL_SCALAR = 2
+} ypdq_dihedral_semantics;
+
+/* The order of the 8 hashes per image in every batched output: slot 0 is the image,
+ * slots 1..7 the derived dihedrals in yume-pdq's visit order (src/lib.rs:391-419). */
+#define YPDQ_SLOT_NORMAL 0
+#define YPDQ_SLOT_FLOPPED 1
+#define YPDQ_SLOT_ROTATED_180 2
+#define YPDQ_SLOT_FLIPPED 3
+#define YPDQ_SLOT_ROTATED_90_FLOPPED 4
+#define YPDQ_SLOT_ROTATED_270 5
+#define YPDQ_SLOT_FLOPPED_ROTATED_270 6
+#define YPDQ_SLOT_ROTATED_90 7
+
+/* One match: database row, query number and Hamming distance. 16 bytes. */
+typedef struct {
+  uint64_t index;
+  uint32_t query;
+  uint32_t distance;
+} ypdq_hit;
+
+/* Scan algorithms (all exact, all return the same hit set). */
+typedef enum {
+  YPDQ_SCAN_AUTO = 0,   /* pick by query count */
+  YPDQ_SCAN_SIMT = 1,   /* XOR + popcount, one row per thread */
+  YPDQ_SCAN_B1MMA = 2   /* binary tensor-core MMA with XOR + popcount */
+} ypdq_scan_algo;
+
+/* ------------------------------------------------------------------ context */
+
+/* Create a context on CUDA device `device` (it becomes current on the calling thread). */
+ypdq_status ypdq_ctx_create(int device, ypdq_ctx **out);
+ypdq_status ypdq_ctx_destroy(ypdq_ctx *ctx);
+/* Text of the last error on this thread. */
+const char *ypdq_last_error(void);
+/* Sticky device-side error flags (timeouts) raised by kernels of this context; clears them.
+ * Blocks until the device is idle. */
+ypdq_status ypdq_check_device_errors(ypdq_ctx *ctx);
+/* Number of SMs and the hash kernel's resident CTAs per SM (for sizing batches). */
+ypdq_status ypdq_device_info(ypdq_ctx *ctx, int *num_sms, int *hash_ctas_per_sm);
+
+/* ------------------------------------------------------------------ hashing */
+
+/*
+ * Hash n images and derive their dihedrals.
+ *   d_images      n * 512 * 512 f32 or u8, 16-byte aligned.
+ *   d_hashes      n * 8 * 32 bytes (slot order above), or NULL.
+ *   d_quality     n * 8 f32, or NULL.
+ *   d_thresholds  n * 8 f32 (slot 0: the median; others as yume-pdq passes them), or NULL.
+ *   d_pdqf        n * pdqf_slots * 256 f32, or NULL. pdqf_slots is 1 (the image's PDQF)
+ *                 or 8 (every slot's matrix as the reference's buffer holds it).
+ *   d_buf1        n * 127 * 128 f32 compressed images (row stride 128), or NULL.
+ */
+ypdq_status ypdq_hash_batch(ypdq_ctx *ctx, const void *d_images, int64_t n, int input_kind,
+                            int dct_precision, int semantics, uint8_t *d_hashes,
+                            float *d_quality, float *d_thresholds, float *d_pdqf,
+                            int pdqf_slots, float *d_buf1, ypdq_stream_t stream);
+
+/*
+ * Dihedrals of n given PDQF matrices (n * 256 f32) with their thresholds (n f32, the
+ * value passed to visit_dihedrals). Outputs as in ypdq_hash_batch, 8 slots per matrix;
+ * slot 0 is the input quantized at the given threshold. With d_thresholds NULL, slot 0
+ * uses the exact median, which makes slot 0 the reference's Kernel::quantize
+ * (src/kernel/mod.rs:595-608).
+ */
+ypdq_status ypdq_dihedrals_batch(ypdq_ctx *ctx, const float *d_pdqf, const float *d_thresholds,
+                                 int64_t n, int semantics, uint8_t *d_hashes, float *d_quality,
+                                 float *d_thresholds_out, float *d_pdqf_out,
+                                 ypdq_stream_t stream);
+
+/* ----------------------------------------------------------------- matching */
+
+/*
+ * Exact linear scan: every (row, query) with popcount(row ^ query) <= threshold.
+ *   d_rows     n_rows * 32 bytes (four little-endian u64 per row), 16-byte aligned.
+ *   d_queries  n_queries * 32 bytes, 16-byte aligned.
+ *   d_hits     capacity entries; hits land in no particular order.
+ *   d_count    one u64, set (not added to) by the call: the total number of hits, which
+ *              can exceed capacity; then only `capacity` hits are stored.
+ * The call does not synchronise; read d_count after the stream completes.
+ */
+ypdq_status ypdq_scan(ypdq_ctx *ctx, const uint8_t *d_rows, uint64_t n_rows,
+                      const uint8_t *d_queries, uint32_t n_queries, uint32_t threshold,
+                      ypdq_hit *d_hits, uint64_t capacity, uint64_t *d_count, int algo,
+                      ypdq_stream_t stream);
+
+/* Sort n hits in place into the scalar matcher's visit order: index, then query. */
+ypdq_status ypdq_sort_hits(ypdq_ctx *ctx, ypdq_hit *d_hits, uint64_t n, ypdq_stream_t stream);
+
+/* ------------------------------------------------------------------ database */
+
+/* Copy n_rows * 32 bytes of host rows into a device-resident database owned by ctx. */
+ypdq_status ypdq_db_create(ypdq_ctx *ctx, const uint8_t *h_rows, uint64_t n_rows, ypdq_db **out);
+/* Wrap caller-owned device rows (not copied, not freed). */
+ypdq_status ypdq_db_wrap(ypdq_ctx *ctx, const uint8_t *d_rows, uint64_t n_rows, ypdq_db **out);
+ypdq_status ypdq_db_destroy(ypdq_db *db);
+ypdq_status ypdq_db_info(ypdq_db *db, const uint8_t **d_rows, uint64_t *n_rows);
+
+/*
+ * Screen n host images against db: hash, derive 8 dihedrals, scan all 8n hashes at
+ * `threshold`. Queries are numbered image * 8 + slot. Hits come back sorted by
+ * (index, query), as the scalar matcher reports them. Copies images in and results out
+ * inside the call and blocks until done.
+ *   h_images     n * 512 * 512 f32 or u8 (pinned memory is fastest; any host memory works).
+ *   h_hits       capacity entries; *n_hits gets the total (YPDQ_ERR_OVERFLOW if > capacity).
+ *   h_hashes     n * 8 * 32 bytes, or NULL.  h_quality  n * 8 f32, or NULL.
+ */
+ypdq_status ypdq_screen_host(ypdq_ctx *ctx, ypdq_db *db, const void *h_images, int64_t n,
+                             int input_kind, int dct_precision, int semantics,
+                             uint32_t threshold, ypdq_hit *h_hits, uint64_t capacity,
+                             uint64_t *n_hits, uint8_t *h_hashes, float *h_quality);
+
+/* --------------------------------------------------------- memory utilities */
+
+ypdq_status ypdq_malloc_device(ypdq_ctx *ctx, size_t bytes, void **d_ptr);
+ypdq_status ypdq_free_device(ypdq_ctx *ctx, void *d_ptr);
+ypdq_status ypdq_malloc_host(ypdq_ctx *ctx, size_t bytes, void **h_ptr); /* pinned */
+ypdq_status ypdq_free_host(ypdq_ctx *ctx, void *h_ptr);
+/* kind: 0 host->device, 1 device->host, 2 device->device. Asynchronous on stream. */
+ypdq_status ypdq_memcpy(ypdq_ctx *ctx, void *dst, const void *src, size_t bytes, int kind,
+                        ypdq_stream_t stream);
+ypdq_status ypdq_memset(ypdq_ctx *ctx, void *d_ptr, int value, size_t bytes, ypdq_stream_t stream);
+ypdq_status ypdq_stream_create(ypdq_ctx *ctx, ypdq_stream_t *out);
+ypdq_status ypdq_stream_destroy(ypdq_ctx *ctx, ypdq_stream_t stream);
+ypdq_status ypdq_stream_sync(ypdq_ctx *ctx, ypdq_stream_t stream);
+
+/* Events for timing on a stream (milliseconds between two recorded events). */
+typedef struct CUevent_st *ypdq_event_t;
+ypdq_status ypdq_event_create(ypdq_ctx *ctx, ypdq_event_t *out);
+ypdq_status ypdq_event_destroy(ypdq_ctx *ctx, ypdq_event_t ev);
+ypdq_status ypdq_event_record(ypdq_ctx *ctx, ypdq_event_t ev, ypdq_stream_t stream);
+ypdq_status ypdq_event_elapsed_ms(ypdq_ctx *ctx, ypdq_event_t start, ypdq_event_t end, float *ms);
+
+/* -------------------------------------------------------- synthetic workloads */
+
+/*
+ * Fill d_rows with n_rows pseudo-random 256-bit rows, each with exactly 128 set bits.
+ * Row r depends only on (seed, first_row + r). Workload generator for benchmarks and
+ * tests; it is not part of the hashing or matching path.
+ */
+ypdq_status ypdq_synth_rows(ypdq_ctx *ctx, uint8_t *d_rows, uint64_t n_rows, uint64_t first_row,
+                            uint64_t seed, ypdq_stream_t stream);
+
+/* The f32 DCT matrix (16 x 127) and tent weights (7 x 7) compiled into the library. */
+ypdq_status ypdq_constants(float *h_dct16x127, float *h_tent7x7);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YPDQ_GB300_H */

@@ -1,0 +1,554 @@
+/*
+ * ypdq_oracle.c -- CPU oracle for the yume-pdq hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. The tests and the CPU baseline of the benchmark load
+ * this code as the checker. The product library never calls, links or executes it.
+ *
+ * It is a plain-C restatement of yume-pdq's scalar path. Citations point into the
+ * yume-pdq sources:
+ *   - jarosz_compress   : DefaultKernel::jarosz_compress  src/kernel/mod.rs:644-666
+ *   - dct2d             : DefaultKernel::dct2d_impl       src/kernel/mod.rs:543-574
+ *   - sum_of_gradients  : DefaultKernel::sum_of_gradients src/kernel/mod.rs:617-642
+ *   - adjust_quality    : DefaultKernel::adjust_quality   src/kernel/mod.rs:611-615 (divisor :257)
+ *   - torben_median     : src/kernel/mod.rs:212-253
+ *   - quantize          : DefaultKernel::quantize         src/kernel/mod.rs:595-608
+ *   - threshold_2d_f32  : src/kernel/threshold.rs:37-119
+ *   - hash_get_threshold: src/lib.rs:427-455
+ *   - visit_dihedrals   : src/lib.rs:358-420; sign conventions src/kernel/mod.rs:345-427
+ *                         (trait default), src/kernel/x86.rs:285-378 (AVX2),
+ *                         src/kernel/x86.rs:989-1079 (AVX-512)
+ *   - dct2d f64 twin    : ReferenceKernel<f64>::dct2d     src/kernel/mod.rs:838-864
+ *   - scalar matcher    : CpuMatcher::find (u64 scalar)   src/matching/mod.rs:336-362
+ *
+ * The f32 arithmetic keeps the reference's operation order: a multiply and then an
+ * add, each rounded, with no fused multiply-add, because Rust does not contract a*b+c.
+ * Build this file with -ffp-contract=off.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "ypdq_constants.h"
+
+#define YPDQO_EXPORT __attribute__((visibility("default")))
+
+static float DCT32[16 * 127];
+static double DCT64[16 * 127];
+static float TENT[49];
+static int CONSTANTS_READY = 0;
+
+static void init_constants(void) {
+  if (CONSTANTS_READY) return;
+  for (int i = 0; i < 16 * 127; i++) {
+    uint32_t b = YPDQO_DCT_F32_BITS[i];
+    uint64_t d = YPDQO_DCT_F64_BITS[i];
+    memcpy(&DCT32[i], &b, 4);
+    memcpy(&DCT64[i], &d, 8);
+  }
+  for (int i = 0; i < 49; i++) {
+    uint32_t b = YPDQO_TENT_F32_BITS[i];
+    memcpy(&TENT[i], &b, 4);
+  }
+  CONSTANTS_READY = 1;
+}
+
+YPDQO_EXPORT void ypdqo_init(void) { init_constants(); }
+
+YPDQO_EXPORT void ypdqo_dct_matrix_f32(float* out) {
+  init_constants();
+  memcpy(out, DCT32, sizeof(DCT32));
+}
+YPDQO_EXPORT void ypdqo_dct_matrix_f64(double* out) {
+  init_constants();
+  memcpy(out, DCT64, sizeof(DCT64));
+}
+YPDQO_EXPORT void ypdqo_tent_weights(float* out) {
+  init_constants();
+  memcpy(out, TENT, sizeof(TENT));
+}
+
+/* 512x512 -> 127x127, all 7x7 taps in the reference order (di outer, dj inner). */
+YPDQO_EXPORT void ypdqo_compress(const float* img, float* out /* 127*127 */) {
+  init_constants();
+  for (int oi = 0; oi < 127; oi++) {
+    int in_i = YPDQO_CONV_OFFSET[oi] - YPDQO_TENT_OFFSET;
+    for (int oj = 0; oj < 127; oj++) {
+      int in_j = YPDQO_CONV_OFFSET[oj] - YPDQO_TENT_OFFSET;
+      float sum = 0.0f;
+      for (int di = 0; di < 7; di++)
+        for (int dj = 0; dj < 7; dj++) {
+          float p = TENT[di * 7 + dj] * img[(in_i + di) * 512 + (in_j + dj)];
+          sum = sum + p;
+        }
+      out[oi * 127 + oj] = sum;
+    }
+  }
+}
+
+/* 127x127 -> 16x16 with four interleaved partial sums, as dct2d_impl does. */
+YPDQO_EXPORT void ypdqo_dct2d(const float* buf /* 127*127 */, float* pdqf /* 256 */) {
+  init_constants();
+  float tmp[127];
+  for (int k = 0; k < 16; k++) {
+    for (int j = 0; j < 127; j++) {
+      float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int k2 = 0; k2 < 127; k2++) {
+        float p = DCT32[k * 127 + k2] * buf[k2 * 127 + j];
+        s[k2 & 3] = s[k2 & 3] + p;
+      }
+      tmp[j] = ((s[0] + s[1]) + s[2]) + s[3];
+    }
+    for (int j = 0; j < 16; j++) {
+      float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int m = 0; m < 127; m++) {
+        float p = tmp[m] * DCT32[j * 127 + m];
+        s[m & 3] = s[m & 3] + p;
+      }
+      pdqf[k * 16 + j] = ((s[0] + s[1]) + s[2]) + s[3];
+    }
+  }
+}
+
+/* FP64 DCT (straight sums) on the f32 compress output, for coefficient-error reports. */
+YPDQO_EXPORT void ypdqo_dct2d_f64(const float* buf /* 127*127 */, double* pdqf /* 256 */) {
+  init_constants();
+  double tmp[127];
+  for (int i = 0; i < 16; i++) {
+    for (int j = 0; j < 127; j++) {
+      double s = 0.0;
+      for (int k = 0; k < 127; k++) s += DCT64[i * 127 + k] * (double)buf[k * 127 + j];
+      tmp[j] = s;
+    }
+    for (int j = 0; j < 16; j++) {
+      double s = 0.0;
+      for (int k = 0; k < 127; k++) s += tmp[k] * DCT64[j * 127 + k];
+      pdqf[i * 16 + j] = s;
+    }
+  }
+}
+
+YPDQO_EXPORT float ypdqo_sum_of_gradients(const float* p) {
+  float g = 0.0f;
+  for (int i = 0; i < 15; i++)
+    for (int j = 0; j < 16; j++) {
+      float d = p[i * 16 + j] - p[(i + 1) * 16 + j];
+      g = g + fabsf(d);
+    }
+  for (int i = 0; i < 16; i++)
+    for (int j = 0; j < 15; j++) {
+      float d = p[i * 16 + j] - p[i * 16 + j + 1];
+      g = g + fabsf(d);
+    }
+  return g;
+}
+
+YPDQO_EXPORT float ypdqo_adjust_quality(float g) {
+  float scaled = g / 180.0f;
+  return scaled < 1.0f ? scaled : 1.0f;
+}
+
+/* Torben's median selection (returns the 128th smallest of 256 for finite inputs). */
+YPDQO_EXPORT float ypdqo_torben_median(const float* m) {
+  float mn = m[0], mx = m[0];
+  for (int i = 1; i < 256; i++) {
+    mn = fminf(mn, m[i]);
+    mx = fmaxf(mx, m[i]);
+  }
+  const int half = (256 + 1) / 2;
+  for (;;) {
+    float guess = (mn + mx) / 2.0f;
+    int less = 0, greater = 0, equal = 0;
+    float maxlt = mn, mingt = mx;
+    for (int i = 0; i < 256; i++) {
+      float v = m[i];
+      if (v < guess) {
+        less++;
+        if (v > maxlt) maxlt = v;
+      } else if (v > guess) {
+        greater++;
+        if (v < mingt) mingt = v;
+      } else {
+        equal++;
+      }
+    }
+    if (less <= half && greater <= half) {
+      if (less >= half) return maxlt;
+      if (less + equal >= half) return guess;
+      return mingt;
+    } else if (less > greater) {
+      mx = maxlt;
+    } else {
+      mn = mingt;
+    }
+  }
+}
+
+/* Element k = 16*i + j goes to byte 31 - k/8, bit k%8 (src/kernel/mod.rs:605-606). */
+YPDQO_EXPORT void ypdqo_threshold_2d(const float* p, uint8_t* out, float thr) {
+  memset(out, 0, 32);
+  for (int k = 0; k < 256; k++)
+    if (p[k] > thr) out[31 - k / 8] |= (uint8_t)(1u << (k % 8));
+}
+
+YPDQO_EXPORT void ypdqo_quantize(const float* p, float* thr, uint8_t* out) {
+  float med = ypdqo_torben_median(p);
+  *thr = med;
+  ypdqo_threshold_2d(p, out, med);
+}
+
+/* Whole single-image pipeline (src/lib.rs:427-455). buf127 and pdqf may be NULL. */
+YPDQO_EXPORT float ypdqo_hash_get_threshold(const float* img, float* thr, uint8_t* out,
+                                            float* buf127, float* pdqf) {
+  float b[127 * 127];
+  float p[256];
+  ypdqo_compress(img, b);
+  ypdqo_dct2d(b, p);
+  float q = ypdqo_adjust_quality(ypdqo_sum_of_gradients(p));
+  float t;
+  ypdqo_quantize(p, &t, out);
+  if (thr) *thr = t;
+  if (buf127) memcpy(buf127, b, sizeof(b));
+  if (pdqf) memcpy(pdqf, p, sizeof(p));
+  return q;
+}
+
+/*
+ * visit_dihedrals with parameterised sign conventions.
+ *
+ * row_mask bit i set: pdqf_negate_alt_rows::<true> negates row i.
+ * col_mask bit j set: pdqf_negate_alt_cols::<false> negates column j.
+ *   trait default (DefaultKernel, ReferenceKernel): rows 0xAAAA, cols 0x5555
+ *   Avx2F32Kernel                                 : rows 0x5555, cols 0x0055
+ *   Avx512F32Kernel (the true flip/flop pattern)  : rows 0x5555, cols 0x5555
+ *
+ * The seven variants come out in visit order: FLOPPED, ROTATED_180, FLIPPED,
+ * ROTATED_90_FLOPPED, ROTATED_270, FLOPPED_ROTATED_270, ROTATED_90.
+ * out_pdqf (may be NULL) receives each variant's matrix as the reference's buffer
+ * holds it at the callback.
+ */
+static void neg_rows(float* p, uint32_t mask) {
+  for (int i = 0; i < 16; i++)
+    if (mask >> i & 1)
+      for (int j = 0; j < 16; j++) p[i * 16 + j] = -p[i * 16 + j];
+}
+static void neg_cols(float* p, uint32_t mask) {
+  for (int i = 0; i < 16; i++)
+    for (int j = 0; j < 16; j++)
+      if (mask >> j & 1) p[i * 16 + j] = -p[i * 16 + j];
+}
+static void transpose16(float* p) {
+  for (int i = 0; i < 16; i++)
+    for (int j = i + 1; j < 16; j++) {
+      float t = p[i * 16 + j];
+      p[i * 16 + j] = p[j * 16 + i];
+      p[j * 16 + i] = t;
+    }
+}
+
+YPDQO_EXPORT void ypdqo_dihedrals(const float* pdqf_in, float threshold, uint32_t row_mask,
+                                  uint32_t col_mask, uint8_t* out_hashes /* 7*32 */,
+                                  float* out_thr /* 7 */, float* out_quality /* 7 */,
+                                  float* out_pdqf /* 7*256 or NULL */) {
+  float p[256];
+  memcpy(p, pdqf_in, sizeof(p));
+  float t_cols = threshold, t_rows = threshold, t_diag = threshold;
+  int v = 0;
+#define EMIT(thr)                                                   \
+  do {                                                              \
+    out_thr[v] = (thr);                                             \
+    out_quality[v] = ypdqo_adjust_quality(ypdqo_sum_of_gradients(p)); \
+    if (out_pdqf) memcpy(out_pdqf + v * 256, p, sizeof(p));          \
+    v++;                                                            \
+  } while (0)
+  neg_cols(p, col_mask);
+  ypdqo_quantize(p, &t_cols, out_hashes + v * 32);
+  EMIT(t_cols); /* FLOPPED */
+  neg_rows(p, row_mask);
+  ypdqo_quantize(p, &t_diag, out_hashes + v * 32);
+  EMIT(t_diag); /* ROTATED_180 */
+  neg_cols(p, col_mask);
+  ypdqo_quantize(p, &t_rows, out_hashes + v * 32);
+  EMIT(t_rows); /* FLIPPED */
+  neg_rows(p, row_mask);
+  transpose16(p);
+  ypdqo_threshold_2d(p, out_hashes + v * 32, threshold);
+  EMIT(threshold); /* ROTATED_90_FLOPPED */
+  neg_rows(p, row_mask);
+  ypdqo_threshold_2d(p, out_hashes + v * 32, t_cols);
+  EMIT(t_cols); /* ROTATED_270 */
+  neg_cols(p, col_mask);
+  ypdqo_threshold_2d(p, out_hashes + v * 32, t_diag);
+  EMIT(t_diag); /* FLOPPED_ROTATED_270 */
+  neg_rows(p, row_mask);
+  ypdqo_threshold_2d(p, out_hashes + v * 32, t_rows);
+  EMIT(t_rows); /* ROTATED_90 */
+#undef EMIT
+}
+
+/* ------------------------------------------------------------------ threads */
+
+typedef void (*range_fn)(void* ctx, int64_t begin, int64_t end);
+typedef struct {
+  range_fn fn;
+  void* ctx;
+  int64_t begin, end;
+} range_job;
+
+static void* range_thread(void* arg) {
+  range_job* j = (range_job*)arg;
+  j->fn(j->ctx, j->begin, j->end);
+  return NULL;
+}
+
+static void parallel_ranges(range_fn fn, void* ctx, int64_t n, int nthreads) {
+  if (nthreads <= 1 || n <= 1) {
+    fn(ctx, 0, n);
+    return;
+  }
+  if (nthreads > 256) nthreads = 256;
+  if ((int64_t)nthreads > n) nthreads = (int)n;
+  pthread_t th[256];
+  range_job jobs[256];
+  for (int t = 0; t < nthreads; t++) {
+    jobs[t].fn = fn;
+    jobs[t].ctx = ctx;
+    jobs[t].begin = n * t / nthreads;
+    jobs[t].end = n * (t + 1) / nthreads;
+  }
+  for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, range_thread, &jobs[t]);
+  range_thread(&jobs[0]);
+  for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+}
+
+/* ------------------------------------------------ batched hashing (baseline) */
+
+typedef struct {
+  const void* imgs;
+  int is_u8;
+  uint32_t row_mask, col_mask;
+  uint8_t* hashes;   /* n * 8 * 32 */
+  float* quality;    /* n * 8 */
+  float* thresholds; /* n * 8 */
+  float* pdqf;       /* n * 256 or NULL */
+} hash_batch_ctx;
+
+static void hash_batch_range(void* vctx, int64_t b, int64_t e) {
+  hash_batch_ctx* c = (hash_batch_ctx*)vctx;
+  float* img = NULL;
+  if (c->is_u8) img = (float*)malloc(512 * 512 * sizeof(float));
+  for (int64_t n = b; n < e; n++) {
+    const float* src;
+    if (c->is_u8) {
+      const uint8_t* u = (const uint8_t*)c->imgs + n * 512 * 512;
+      for (int i = 0; i < 512 * 512; i++) img[i] = (float)u[i];
+      src = img;
+    } else {
+      src = (const float*)c->imgs + n * 512 * 512;
+    }
+    float p[256], t;
+    float q = ypdqo_hash_get_threshold(src, &t, c->hashes + n * 256, NULL, p);
+    c->quality[n * 8] = q;
+    c->thresholds[n * 8] = t;
+    if (c->pdqf) memcpy(c->pdqf + n * 256, p, sizeof(p));
+    ypdqo_dihedrals(p, t, c->row_mask, c->col_mask, c->hashes + n * 256 + 32,
+                    c->thresholds + n * 8 + 1, c->quality + n * 8 + 1, NULL);
+  }
+  free(img);
+}
+
+/* Hash n images and derive the seven dihedrals of each (slot 0 = the image itself). */
+YPDQO_EXPORT void ypdqo_hash_batch(const void* imgs, int64_t n, int is_u8, uint32_t row_mask,
+                                   uint32_t col_mask, uint8_t* hashes, float* quality,
+                                   float* thresholds, float* pdqf, int nthreads) {
+  init_constants();
+  hash_batch_ctx c = {imgs, is_u8, row_mask, col_mask, hashes, quality, thresholds, pdqf};
+  parallel_ranges(hash_batch_range, &c, n, nthreads);
+}
+
+/* ------------------------------------------------------------ scalar matcher */
+
+typedef struct {
+  uint64_t index;
+  uint32_t query;
+  uint32_t distance;
+} ypdqo_hit;
+
+static inline uint32_t dist256(const uint64_t* a, const uint64_t* b) {
+  return (uint32_t)(__builtin_popcountll(a[0] ^ b[0]) + __builtin_popcountll(a[1] ^ b[1]) +
+                    __builtin_popcountll(a[2] ^ b[2]) + __builtin_popcountll(a[3] ^ b[3]));
+}
+
+typedef struct {
+  const uint64_t* db;
+  const uint64_t* needles;
+  int n_needles;
+  uint32_t threshold;
+  int nthreads;
+  int64_t n_rows;
+  ypdqo_hit** bufs;
+  int64_t* counts;
+  int64_t* caps;
+} find_ctx;
+
+static void find_range(void* vctx, int64_t b, int64_t e) {
+  find_ctx* c = (find_ctx*)vctx;
+  for (int64_t t = b; t < e; t++) {
+    int64_t r0 = c->n_rows * t / c->nthreads, r1 = c->n_rows * (t + 1) / c->nthreads;
+    int64_t cnt = 0, cap = 64;
+    ypdqo_hit* buf = (ypdqo_hit*)malloc(cap * sizeof(ypdqo_hit));
+    for (int64_t r = r0; r < r1; r++) {
+      const uint64_t* row = c->db + r * 4;
+      for (int q = 0; q < c->n_needles; q++) {
+        uint32_t d = dist256(row, c->needles + q * 4);
+        if (d <= c->threshold) {
+          if (cnt == cap) {
+            cap *= 2;
+            buf = (ypdqo_hit*)realloc(buf, cap * sizeof(ypdqo_hit));
+          }
+          buf[cnt].index = (uint64_t)r;
+          buf[cnt].query = (uint32_t)q;
+          buf[cnt].distance = d;
+          cnt++;
+        }
+      }
+    }
+    c->bufs[t] = buf;
+    c->counts[t] = cnt;
+  }
+}
+
+/*
+ * All (row, needle, distance) with popcount(row ^ needle) <= threshold, in the order
+ * the scalar CpuMatcher::find visits them: rows ascending, then needles ascending.
+ * Returns the total number of hits; writes at most cap of them.
+ */
+YPDQO_EXPORT int64_t ypdqo_find_all(const uint8_t* db, int64_t n_rows, const uint8_t* needles,
+                                    int n_needles, uint32_t threshold, ypdqo_hit* out,
+                                    int64_t cap, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  ypdqo_hit* bufs[256];
+  int64_t counts[256];
+  find_ctx c = {(const uint64_t*)db, (const uint64_t*)needles, n_needles, threshold,
+                nthreads, n_rows, bufs, counts, NULL};
+  parallel_ranges(find_range, &c, nthreads, nthreads);
+  int64_t total = 0;
+  for (int t = 0; t < nthreads; t++) {
+    for (int64_t k = 0; k < counts[t]; k++) {
+      if (total + k < cap) out[total + k] = bufs[t][k];
+    }
+    total += counts[t];
+    free(bufs[t]);
+  }
+  return total;
+}
+
+/* Number of hits only (no storage), for timing the matcher without a callback. */
+typedef struct {
+  const uint64_t* db;
+  const uint64_t* needles;
+  int n_needles;
+  uint32_t threshold;
+  int64_t n_rows;
+  int nthreads;
+  int64_t* counts;
+} count_ctx;
+
+static void count_range(void* vctx, int64_t b, int64_t e) {
+  count_ctx* c = (count_ctx*)vctx;
+  for (int64_t t = b; t < e; t++) {
+    int64_t r0 = c->n_rows * t / c->nthreads, r1 = c->n_rows * (t + 1) / c->nthreads;
+    int64_t cnt = 0;
+    for (int64_t r = r0; r < r1; r++) {
+      const uint64_t* row = c->db + r * 4;
+      for (int q = 0; q < c->n_needles; q++)
+        cnt += dist256(row, c->needles + q * 4) <= c->threshold;
+    }
+    c->counts[t] = cnt;
+  }
+}
+
+YPDQO_EXPORT int64_t ypdqo_count_all(const uint8_t* db, int64_t n_rows, const uint8_t* needles,
+                                     int n_needles, uint32_t threshold, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  int64_t counts[256];
+  count_ctx c = {(const uint64_t*)db, (const uint64_t*)needles, n_needles, threshold,
+                 n_rows, nthreads, counts};
+  parallel_ranges(count_range, &c, nthreads, nthreads);
+  int64_t total = 0;
+  for (int t = 0; t < nthreads; t++) total += counts[t];
+  return total;
+}
+
+/* README "API Usage" known-answer input: a horizontal FM sine, generated in f32 with the
+ * C library's sinf, in the same operation order as the README's Rust snippet
+ * (README.md:305-330). */
+YPDQO_EXPORT void ypdqo_fm_sine_image(float* out /* 512*512 */) {
+  const float pi = 3.14159265358979323846f;
+  float frequency = 4.0f;
+  const float modulation = frequency / 512.0f;
+  for (int i = 0; i < 512; i++)
+    for (int j = 0; j < 512; j++) {
+      frequency = frequency + modulation;
+      float a = (float)j * 2.0f;
+      a = a * pi;
+      a = a * frequency;
+      a = a / 512.0f;
+      float v = sinf(a);
+      float s = v * 127.0f;
+      out[i * 512 + j] = s + 128.0f;
+    }
+}
+
+/* ----------------------------------------------- synthetic rows (CPU twin) */
+
+/* Same construction as the library's workload generator: a splitmix64 stream per row
+ * (seeded by seed and row number), then bits cleared or set at uniformly drawn positions
+ * until exactly 128 remain. Used to give the CPU baseline the same database. */
+static inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+typedef struct {
+  uint64_t* out;
+  uint64_t first, seed;
+} synth_ctx;
+
+static void synth_range(void* vctx, int64_t b, int64_t e) {
+  synth_ctx* c = (synth_ctx*)vctx;
+  for (int64_t r = b; r < e; r++) {
+    uint64_t state = mix64(c->seed ^ mix64(c->first + (uint64_t)r + 0x9E3779B97F4A7C15ull));
+    uint64_t w[4];
+    for (int k = 0; k < 4; k++) {
+      state += 0x9E3779B97F4A7C15ull;
+      w[k] = mix64(state);
+    }
+    int pc = __builtin_popcountll(w[0]) + __builtin_popcountll(w[1]) +
+             __builtin_popcountll(w[2]) + __builtin_popcountll(w[3]);
+    while (pc != 128) {
+      state += 0x9E3779B97F4A7C15ull;
+      uint32_t pos = (uint32_t)(mix64(state) & 255u);
+      uint64_t bit = 1ull << (pos & 63);
+      uint64_t* word = &w[pos >> 6];
+      if (pc > 128 && (*word & bit)) {
+        *word &= ~bit;
+        pc--;
+      } else if (pc < 128 && !(*word & bit)) {
+        *word |= bit;
+        pc++;
+      }
+    }
+    memcpy(c->out + r * 4, w, 32);
+  }
+}
+
+YPDQO_EXPORT void ypdqo_synth_rows(uint8_t* out, int64_t n, uint64_t first, uint64_t seed,
+                                   int nthreads) {
+  synth_ctx c = {(uint64_t*)out, first, seed};
+  parallel_ranges(synth_range, &c, n, nthreads);
+}

@@ -1,0 +1,161 @@
+"""GPU parity of the exact Hamming scan against the oracle's scalar matcher.
+
+Hit sets must be identical (index, query, distance), in the scalar matcher's order once
+sorted. Every call goes through the C ABI.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ALGOS = [1, 2]  # YPDQ_SCAN_SIMT, YPDQ_SCAN_B1MMA
+
+
+def as_tuples(h):
+    return np.stack([h["index"].astype(np.int64), h["query"].astype(np.int64),
+                     h["distance"].astype(np.int64)], axis=1) if len(h) else np.zeros((0, 3), np.int64)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("n_rows,n_q", [(0, 8), (1, 1), (15, 3), (17, 8), (4099, 13), (20000, 64), (5000, 2049)])
+def test_scan_matches_oracle(ctx, yp, oracle, algo, n_rows, n_q):
+    rows = yp.synth.rows_128(n_rows, seed=n_rows + 1)
+    q = yp.synth.rows_128(n_q, seed=n_q + 1000)
+    if n_rows:
+        yp.synth.plant(rows, q, min(n_rows, 60), 0, 40, seed=7)
+    for t in (0, 16, 31, 48):
+        got = yp.scan(ctx, rows, q, t, algo=algo)
+        want = oracle.find_all(rows, q, t)
+        assert np.array_equal(as_tuples(got), as_tuples(want)), (t, len(got), len(want))
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_scan_thresholds_extremes(ctx, yp, oracle, algo):
+    rows = np.random.default_rng(1).integers(0, 256, (300, 32), dtype=np.uint8)
+    q = np.random.default_rng(2).integers(0, 256, (9, 32), dtype=np.uint8)
+    rows[5] = q[3]
+    for t in (0, 1, 100, 128, 255, 256):
+        got = yp.scan(ctx, rows, q, t, algo=algo, capacity=4096)
+        want = oracle.find_all(rows, q, t)
+        assert np.array_equal(as_tuples(got), as_tuples(want))
+    assert len(yp.scan(ctx, rows, q, 256, algo=algo)) == 300 * 9
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_planted_controls(ctx, yp, algo):
+    """src/matching/mod.rs:460-553 structure on the GPU: no false hits, every control found."""
+    rng = np.random.default_rng(0x79756D652D706471)
+    needles = rng.integers(0, 256, (8, 32), dtype=np.uint8)
+    rows = rng.integers(0, 256, (2048, 32), dtype=np.uint8)
+    assert len(yp.scan(ctx, rows, needles, 31, algo=algo)) == 0
+    for pos in range(0, 2048, 61):
+        k = int(rng.integers(0, 8))
+        planted = needles.copy()
+        planted[k] = rows[pos]
+        for _ in range(31):
+            b = int(rng.integers(0, 256))
+            planted[k, b // 8] ^= np.uint8(1 << (b % 8))
+        hits = yp.scan(ctx, rows, planted, 31, algo=algo)
+        assert len(hits) == 1 and hits[0]["index"] == pos and hits[0]["query"] == k
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_overflow_reports_total(ctx, yp, oracle, algo):
+    rows = yp.synth.rows_128(5000, seed=3)
+    q = yp.synth.rows_128(4, seed=4)
+    yp.synth.plant(rows, q, 400, 0, 10, seed=5)
+    d_rows, d_q = ctx.to_device(rows), ctx.to_device(q)
+    d_hits, d_cnt = ctx.alloc(100 * 16), ctx.alloc(8)
+    yp.core.scan_device(ctx, d_rows, 5000, d_q, 4, 31, d_hits, 100, d_cnt, algo)
+    ctx.sync()
+    total = int(d_cnt.download((1,), np.uint64)[0])
+    assert total == len(oracle.find_all(rows, q, 31))
+    stored = d_hits.download((100,), yp.HIT_DTYPE)
+    full = {tuple(x) for x in as_tuples(oracle.find_all(rows, q, 31))}
+    assert {tuple(x) for x in as_tuples(stored)} <= full
+
+
+def test_sort_hits(ctx, yp):
+    rng = np.random.default_rng(9)
+    for n in (2, 3, 100, 1025, 70000):
+        h = np.zeros(n, yp.HIT_DTYPE)
+        h["index"] = rng.integers(0, 1 << 40, n)
+        h["query"] = rng.integers(0, 5000, n)
+        h["index"][: n // 3] = h["index"][0]  # ties on index
+        d = ctx.to_device(h)
+        yp.core.sort_hits_device(ctx, d, n)
+        got = d.download((n,), yp.HIT_DTYPE)
+        order = np.lexsort((h["query"], h["index"]))
+        assert np.array_equal(got[["index", "query"]], h[order][["index", "query"]])
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_matcher_surface(ctx, yp, oracle, algo):
+    rows = yp.synth.rows_128(3000, seed=31)
+    q = yp.synth.rows_128(8, seed=32)
+    yp.synth.plant(rows, q, 30, 0, 31, seed=33)
+    db = yp.CudaVectorDatabase(ctx, rows)
+    m = yp.CudaMatcher(ctx, db, 31, algo=algo)
+    assert m.scan(q)
+    assert not m.scan(yp.synth.rows_128(8, seed=99))
+    want = oracle.find_all(rows, q, 31)
+    first = m.find(q, lambda i, j: (i, j))
+    assert first == (int(want[0]["index"]), int(want[0]["query"]))
+    seen = []
+    assert m.find(q, lambda i, j: seen.append((i, j))) is None
+    assert seen == [(int(w["index"]), int(w["query"])) for w in want]
+
+
+def test_full_size_10m_scan(ctx, yp, oracle):
+    """10M-row database (320 MB) with 10,000 planted rows at distances 0..31: both kernels
+    return the oracle's exact hit list for a batch of 8 and of 64 queries."""
+    n = 10_000_000
+    d_rows = ctx.alloc(n * 32)
+    ctx.lib.ypdq_synth_rows(ctx.handle, d_rows.ptr, n, 0, 1234, None)
+    ctx.sync()
+    rows = d_rows.download((n, 32), np.uint8)
+    assert np.all(yp.synth.popcount_rows(rows[:100000]) == 128)
+    q = yp.synth.rows_128(64, seed=77)
+    pos, qid, dist = yp.synth.plant(rows, q, 10_000, 0, 31, seed=78)
+    d_rows.upload(rows)
+    d_q = ctx.to_device(q)
+    d_cnt = ctx.alloc(8)
+    for nq in (8, 64):
+        want = oracle.find_all(rows, q[:nq], 31)
+        assert len(want) >= int(np.sum(qid < nq))
+        for algo in ALGOS:
+            d_hits = ctx.alloc(len(want) * 16 + 16)
+            yp.core.scan_device(ctx, d_rows, n, d_q, nq, 31, d_hits, len(want) + 1, d_cnt, algo)
+            ctx.sync()
+            total = int(d_cnt.download((1,), np.uint64)[0])
+            assert total == len(want)
+            yp.core.sort_hits_device(ctx, d_hits, total)
+            got = d_hits.download((total,), yp.HIT_DTYPE)
+            assert np.array_equal(as_tuples(got), as_tuples(want))
+
+
+def test_screen_host_end_to_end(ctx, yp, oracle):
+    """ypdq_screen_host: host images in, sorted (index, query, distance) hits out."""
+    imgs = yp.synth.blob_images(6, seed=41)
+    h, q, t, _ = oracle.hash_batch(imgs)
+    queries = h.reshape(-1, 32)
+    rows = yp.synth.rows_128(50000, seed=42)
+    yp.synth.plant(rows, queries, 500, 0, 40, seed=43)
+    db = yp.Database(ctx, rows)
+    hits, hashes = yp.screen_host(ctx, db, imgs, threshold=31, want_hashes=True)
+    assert np.array_equal(hashes, h)
+    want = oracle.find_all(rows, queries, 31)
+    assert np.array_equal(as_tuples(hits), as_tuples(want))
+    # capacity smaller than the hit count: the call grows and retries
+    hits2 = yp.screen_host(ctx, db, imgs, threshold=31, capacity=3)
+    assert np.array_equal(as_tuples(hits2), as_tuples(want))
+
+
+def test_synth_rows_match_cpu_twin(ctx, yp, oracle):
+    n = 20000
+    d = ctx.alloc(n * 32)
+    yp._lib.check(ctx.lib.ypdq_synth_rows(ctx.handle, d.ptr, n, 5, 42, None))
+    ctx.sync()
+    assert np.array_equal(d.download((n, 32), np.uint8), oracle.synth_rows(n, 42, first=5))

@@ -1,0 +1,278 @@
+"""Host-side objects over the C ABI: context, device buffers, batched hash and scan."""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, ptr, HIT_DTYPE
+
+
+class Context:
+    """A CUDA context of the library on one device (ypdq_ctx)."""
+
+    def __init__(self, device=0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self.lib.ypdq_ctx_create(device, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+        sms, ctas = ctypes.c_int(), ctypes.c_int()
+        check(self.lib.ypdq_device_info(h, ctypes.byref(sms), ctypes.byref(ctas)))
+        self.num_sms = sms.value
+        self.hash_ctas_per_sm = ctas.value
+
+    def close(self):
+        if self.handle:
+            self.lib.ypdq_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- memory
+    def alloc(self, nbytes):
+        return DeviceBuffer(self, nbytes)
+
+    def to_device(self, array, stream=None):
+        a = np.ascontiguousarray(array)
+        buf = DeviceBuffer(self, a.nbytes)
+        buf.upload(a, stream)
+        return buf
+
+    def sync(self, stream=None):
+        check(self.lib.ypdq_stream_sync(self.handle, stream))
+
+    def check_device_errors(self):
+        check(self.lib.ypdq_check_device_errors(self.handle))
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        check(self.lib.ypdq_stream_create(self.handle, ctypes.byref(s)))
+        return s
+
+    def event(self):
+        e = ctypes.c_void_p()
+        check(self.lib.ypdq_event_create(self.handle, ctypes.byref(e)))
+        return e
+
+    def record(self, event, stream=None):
+        check(self.lib.ypdq_event_record(self.handle, event, stream))
+
+    def elapsed_ms(self, start, end):
+        ms = ctypes.c_float()
+        check(self.lib.ypdq_event_elapsed_ms(self.handle, start, end, ctypes.byref(ms)))
+        return ms.value
+
+
+class DeviceBuffer:
+    """Device memory from ypdq_malloc_device; freed with the object."""
+
+    def __init__(self, ctx, nbytes):
+        self.ctx = ctx
+        self.nbytes = int(nbytes)
+        p = ctypes.c_void_p()
+        check(ctx.lib.ypdq_malloc_device(ctx.handle, max(self.nbytes, 1), ctypes.byref(p)))
+        self.ptr = p
+
+    @property
+    def address(self):
+        return self.ptr.value
+
+    def at(self, offset):
+        return ctypes.c_void_p(self.ptr.value + int(offset))
+
+    def upload(self, array, stream=None, offset=0):
+        a = np.ascontiguousarray(array)
+        assert a.nbytes + offset <= self.nbytes
+        check(self.ctx.lib.ypdq_memcpy(self.ctx.handle, self.at(offset), ptr(a), a.nbytes,
+                                       _lib.H2D, stream))
+        if stream is None:
+            self.ctx.sync(None)
+
+    def download(self, shape, dtype, stream=None, offset=0):
+        out = np.empty(shape, dtype)
+        assert out.nbytes + offset <= self.nbytes
+        check(self.ctx.lib.ypdq_memcpy(self.ctx.handle, ptr(out), self.at(offset), out.nbytes,
+                                       _lib.D2H, stream))
+        self.ctx.sync(stream)
+        return out
+
+    def zero(self, stream=None):
+        check(self.ctx.lib.ypdq_memset(self.ctx.handle, self.ptr, 0, self.nbytes, stream))
+
+    def free(self):
+        if self.ptr is not None and self.ptr.value:
+            self.ctx.lib.ypdq_free_device(self.ctx.handle, self.ptr)
+        self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _semantics(sem):
+    return _lib.SEMANTICS[sem] if isinstance(sem, str) else int(sem)
+
+
+def hash_batch_device(ctx, d_images, n, input_kind, d_hashes=None, d_quality=None,
+                      d_thresholds=None, d_pdqf=None, pdqf_slots=1, d_buf1=None,
+                      dct=_lib.DCT_FP32, semantics="exact", stream=None):
+    """Launch ypdq_hash_batch on device buffers (asynchronous)."""
+    def dp(b):
+        return None if b is None else (b.ptr if isinstance(b, DeviceBuffer) else b)
+    check(ctx.lib.ypdq_hash_batch(ctx.handle, dp(d_images), int(n), int(input_kind), int(dct),
+                                  _semantics(semantics), dp(d_hashes), dp(d_quality),
+                                  dp(d_thresholds), dp(d_pdqf), int(pdqf_slots), dp(d_buf1),
+                                  stream))
+
+
+def hash_batch(ctx, images, semantics="exact", dct=_lib.DCT_FP32, want_pdqf=False,
+               pdqf_slots=1, want_buf1=False):
+    """Hash host images [n, 512, 512] (f32 or u8) on the GPU.
+
+    Returns a dict with hashes [n, 8, 32] u8, quality [n, 8], thresholds [n, 8] and,
+    when asked, pdqf [n, slots, 16, 16] and buf1 [n, 127, 127].
+    """
+    imgs = np.ascontiguousarray(images)
+    if imgs.dtype == np.uint8:
+        kind = _lib.INPUT_U8
+    else:
+        imgs = imgs.astype(np.float32, copy=False)
+        kind = _lib.INPUT_F32
+    assert imgs.shape[1:] == (512, 512), imgs.shape
+    n = imgs.shape[0]
+    d_img = ctx.to_device(imgs)
+    d_h = ctx.alloc(n * 256)
+    d_q = ctx.alloc(n * 32)
+    d_t = ctx.alloc(n * 32)
+    d_p = ctx.alloc(n * pdqf_slots * 1024) if want_pdqf else None
+    d_b = ctx.alloc(n * 127 * 128 * 4) if want_buf1 else None
+    hash_batch_device(ctx, d_img, n, kind, d_h, d_q, d_t, d_p, pdqf_slots, d_b, dct, semantics)
+    ctx.sync()
+    out = {
+        "hashes": d_h.download((n, 8, 32), np.uint8),
+        "quality": d_q.download((n, 8), np.float32),
+        "thresholds": d_t.download((n, 8), np.float32),
+    }
+    if want_pdqf:
+        out["pdqf"] = d_p.download((n, pdqf_slots, 16, 16), np.float32)
+    if want_buf1:
+        out["buf1"] = d_b.download((n, 127, 128), np.float32)[:, :, :127]
+    return out
+
+
+def dihedrals_batch(ctx, pdqf, thresholds, semantics="exact"):
+    """Derived dihedrals of given PDQF matrices [n, 16, 16] at thresholds [n] (8 slots each)."""
+    p = np.ascontiguousarray(pdqf, np.float32).reshape(-1, 256)
+    t = np.ascontiguousarray(thresholds, np.float32).reshape(-1)
+    n = p.shape[0]
+    d_p, d_t = ctx.to_device(p), ctx.to_device(t)
+    d_h, d_q, d_to, d_po = ctx.alloc(n * 256), ctx.alloc(n * 32), ctx.alloc(n * 32), ctx.alloc(n * 8192)
+    check(ctx.lib.ypdq_dihedrals_batch(ctx.handle, d_p.ptr, d_t.ptr, n, _semantics(semantics),
+                                       d_h.ptr, d_q.ptr, d_to.ptr, d_po.ptr, None))
+    ctx.sync()
+    return {
+        "hashes": d_h.download((n, 8, 32), np.uint8),
+        "quality": d_q.download((n, 8), np.float32),
+        "thresholds": d_to.download((n, 8), np.float32),
+        "pdqf": d_po.download((n, 8, 16, 16), np.float32),
+    }
+
+
+def scan_device(ctx, d_rows, n_rows, d_queries, n_queries, threshold, d_hits, capacity, d_count,
+                algo=_lib.SCAN_AUTO, stream=None):
+    def dp(b):
+        return b.ptr if isinstance(b, DeviceBuffer) else b
+    check(ctx.lib.ypdq_scan(ctx.handle, dp(d_rows), int(n_rows), dp(d_queries), int(n_queries),
+                            int(threshold), dp(d_hits), int(capacity), dp(d_count), int(algo),
+                            stream))
+
+
+def sort_hits_device(ctx, d_hits, n, stream=None):
+    check(ctx.lib.ypdq_sort_hits(ctx.handle, d_hits.ptr if isinstance(d_hits, DeviceBuffer) else d_hits,
+                                 int(n), stream))
+
+
+def scan(ctx, db_rows, queries, threshold, algo=_lib.SCAN_AUTO, capacity=1 << 16, sort=True):
+    """Exact scan of host rows [n, 32] u8 against host queries [q, 32] u8. Returns hits."""
+    rows = np.ascontiguousarray(db_rows, np.uint8).reshape(-1, 32)
+    q = np.ascontiguousarray(queries, np.uint8).reshape(-1, 32)
+    d_rows = ctx.to_device(rows) if rows.shape[0] else ctx.alloc(32)
+    d_q = ctx.to_device(q) if q.shape[0] else ctx.alloc(32)
+    d_cnt = ctx.alloc(8)
+    while True:
+        d_hits = ctx.alloc(max(capacity, 1) * 16)
+        scan_device(ctx, d_rows, rows.shape[0], d_q, q.shape[0], threshold, d_hits, capacity,
+                    d_cnt, algo)
+        ctx.sync()
+        total = int(d_cnt.download((1,), np.uint64)[0])
+        if total <= capacity:
+            break
+        capacity = total
+    if sort and total > 1:
+        sort_hits_device(ctx, d_hits, total)
+        ctx.sync()
+    return d_hits.download((total,), HIT_DTYPE) if total else np.zeros(0, HIT_DTYPE)
+
+
+class Database:
+    """Device-resident database of 256-bit rows (ypdq_db)."""
+
+    def __init__(self, ctx, rows=None, device_buffer=None, n_rows=None):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        if device_buffer is not None:
+            self._keep = device_buffer
+            check(ctx.lib.ypdq_db_wrap(ctx.handle, device_buffer.ptr, int(n_rows), ctypes.byref(h)))
+            self.n_rows = int(n_rows)
+        else:
+            r = np.ascontiguousarray(rows, np.uint8).reshape(-1, 32)
+            check(ctx.lib.ypdq_db_create(ctx.handle, ptr(r), r.shape[0], ctypes.byref(h)))
+            self.n_rows = r.shape[0]
+        self.handle = h
+
+    def device_rows(self):
+        p = ctypes.c_void_p()
+        n = ctypes.c_uint64()
+        check(self.ctx.lib.ypdq_db_info(self.handle, ctypes.byref(p), ctypes.byref(n)))
+        return p, n.value
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.ypdq_db_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def screen_host(ctx, db, images, threshold=31, semantics="exact", dct=_lib.DCT_FP32,
+                capacity=1 << 16, want_hashes=False):
+    """ypdq_screen_host: hash + 8 dihedrals + scan, from host images to sorted host hits."""
+    imgs = np.ascontiguousarray(images)
+    kind = _lib.INPUT_U8 if imgs.dtype == np.uint8 else _lib.INPUT_F32
+    if kind == _lib.INPUT_F32:
+        imgs = imgs.astype(np.float32, copy=False)
+    n = imgs.shape[0]
+    while True:
+        hits = np.zeros(max(capacity, 1), HIT_DTYPE)
+        nh = ctypes.c_uint64()
+        hashes = np.zeros((n, 8, 32), np.uint8) if want_hashes else None
+        st = ctx.lib.ypdq_screen_host(ctx.handle, db.handle, ptr(imgs), n, kind, int(dct),
+                                      _semantics(semantics), int(threshold), ptr(hits), capacity,
+                                      ctypes.byref(nh), ptr(hashes), None)
+        if st == _lib.ERR_OVERFLOW:
+            capacity = int(nh.value)
+            continue
+        check(st)
+        break
+    out = hits[: nh.value]
+    return (out, hashes) if want_hashes else out

@@ -1,0 +1,650 @@
+// C ABI of libyumepdq_gb300: the batched device API (include/ypdq.h) and the drop-in
+// symbols of yume-pdq's C header (include/yume_pdq.h).
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "ypdq_internal.cuh"
+#include "ypdq_tables.h"
+#include "yume_pdq.h"
+
+using namespace ypdq;
+
+struct ypdq_ctx {
+  int device = 0;
+  int num_sms = 0;
+  int hash_ctas_f32 = 1;
+  int hash_ctas_u8 = 1;
+  int* d_err = nullptr;
+  cudaStream_t stream = nullptr;  // used by the blocking _host calls
+  std::mutex mu;                  // guards the scratch buffers below
+  void* scratch[8] = {};
+  size_t scratch_bytes[8] = {};
+};
+
+struct ypdq_db {
+  ypdq_ctx* ctx;
+  const uint8_t* d_rows;
+  uint64_t n_rows;
+  bool owned;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+ypdq_status fail(ypdq_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return st;
+}
+
+ypdq_status cuda_fail(cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation)
+    return fail(YPDQ_ERR_NOMEM, "%s: %s", what, cudaGetErrorString(e));
+  return fail(YPDQ_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                       \
+  do {                                       \
+    cudaError_t e_ = (call);                 \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+void semantics_masks(int sem, uint32_t* rm, uint32_t* cm) {
+  switch (sem) {
+    case YPDQ_DIHEDRAL_AVX2:
+      *rm = 0x5555u;
+      *cm = 0x0055u;
+      break;
+    case YPDQ_DIHEDRAL_SCALAR:
+      *rm = 0xAAAAu;
+      *cm = 0x5555u;
+      break;
+    default:
+      *rm = 0x5555u;
+      *cm = 0x5555u;
+      break;
+  }
+}
+
+// Grow-only scratch buffer `slot` of ctx to at least `bytes`. Caller holds ctx->mu.
+ypdq_status scratch(ypdq_ctx* ctx, int slot, size_t bytes, void** out) {
+  if (ctx->scratch_bytes[slot] < bytes) {
+    if (ctx->scratch[slot]) cudaFree(ctx->scratch[slot]);
+    ctx->scratch[slot] = nullptr;
+    ctx->scratch_bytes[slot] = 0;
+    size_t want = bytes < 4096 ? 4096 : bytes;
+    CK(cudaMalloc(&ctx->scratch[slot], want), "cudaMalloc(scratch)");
+    ctx->scratch_bytes[slot] = want;
+  }
+  *out = ctx->scratch[slot];
+  return YPDQ_OK;
+}
+
+ypdq_status check_ctx(ypdq_ctx* ctx) {
+  if (!ctx) return fail(YPDQ_ERR_INVALID, "ctx is NULL");
+  CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+  return YPDQ_OK;
+}
+
+ypdq_status read_device_errors(ypdq_ctx* ctx) {
+  int err = 0;
+  CK(cudaMemcpy(&err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read device errors");
+  if (err) {
+    CK(cudaMemset(ctx->d_err, 0, sizeof(int)), "clear device errors");
+    if (err & kDevErrTimeout)
+      return fail(YPDQ_ERR_TIMEOUT, "a kernel wait exceeded its time limit and gave up");
+    return fail(YPDQ_ERR_CUDA, "device error flags 0x%x", err);
+  }
+  return YPDQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ----------------------------------------------------------------- context
+
+const char* ypdq_last_error(void) { return g_last_error.c_str(); }
+
+ypdq_status ypdq_ctx_create(int device, ypdq_ctx** out) {
+  if (!out) return fail(YPDQ_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int count = 0;
+  CK(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+  if (device < 0 || device >= count)
+    return fail(YPDQ_ERR_INVALID, "device %d out of range (%d devices)", device, count);
+  CK(cudaSetDevice(device), "cudaSetDevice");
+  ypdq_ctx* ctx = new ypdq_ctx();
+  ctx->device = device;
+  cudaError_t e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = upload_constants();
+  if (e == cudaSuccess) e = scan_init();
+  if (e == cudaSuccess) e = hash_occupancy(0, &ctx->hash_ctas_f32);
+  if (e == cudaSuccess) e = hash_occupancy(1, &ctx->hash_ctas_u8);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    if (ctx->d_err) cudaFree(ctx->d_err);
+    delete ctx;
+    return cuda_fail(e, "ypdq_ctx_create");
+  }
+  if (ctx->hash_ctas_f32 < 1 || ctx->hash_ctas_u8 < 1) {
+    cudaFree(ctx->d_err);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return fail(YPDQ_ERR_UNSUPPORTED, "hash kernel does not fit on this device");
+  }
+  *out = ctx;
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_ctx_destroy(ypdq_ctx* ctx) {
+  if (!ctx) return YPDQ_OK;
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  for (int i = 0; i < 8; ++i)
+    if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_check_device_errors(ypdq_ctx* ctx) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+  return read_device_errors(ctx);
+}
+
+ypdq_status ypdq_device_info(ypdq_ctx* ctx, int* num_sms, int* hash_ctas_per_sm) {
+  if (!ctx) return fail(YPDQ_ERR_INVALID, "ctx is NULL");
+  if (num_sms) *num_sms = ctx->num_sms;
+  if (hash_ctas_per_sm) *hash_ctas_per_sm = ctx->hash_ctas_f32;
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_constants(float* h_dct, float* h_tent) {
+  if (h_dct) memcpy(h_dct, YPDQ_DCT_F32_BITS, sizeof(YPDQ_DCT_F32_BITS));
+  if (h_tent) memcpy(h_tent, YPDQ_TENT_F32_BITS, sizeof(YPDQ_TENT_F32_BITS));
+  return YPDQ_OK;
+}
+
+// ----------------------------------------------------------------- hashing
+
+ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int input_kind,
+                            int dct_precision, int semantics, uint8_t* d_hashes,
+                            float* d_quality, float* d_thresholds, float* d_pdqf,
+                            int pdqf_slots, float* d_buf1, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (n < 0) return fail(YPDQ_ERR_INVALID, "n < 0");
+  if (n > 0 && !d_images) return fail(YPDQ_ERR_INVALID, "d_images is NULL");
+  if (input_kind != YPDQ_INPUT_F32 && input_kind != YPDQ_INPUT_U8)
+    return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
+  if (semantics < YPDQ_DIHEDRAL_EXACT || semantics > YPDQ_DIHEDRAL_SCALAR)
+    return fail(YPDQ_ERR_INVALID, "semantics %d", semantics);
+  if (dct_precision != YPDQ_DCT_FP32) {
+    if (dct_precision == YPDQ_DCT_TF32 || dct_precision == YPDQ_DCT_BF16X3)
+      return fail(YPDQ_ERR_UNSUPPORTED, "dct_precision %d is not available in this build",
+                  dct_precision);
+    return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
+  }
+  if (d_pdqf && pdqf_slots != 1 && pdqf_slots != 8)
+    return fail(YPDQ_ERR_INVALID, "pdqf_slots must be 1 or 8");
+  if (!aligned16(d_images)) return fail(YPDQ_ERR_ALIGN, "d_images must be 16-byte aligned");
+  if (d_pdqf && !aligned16(d_pdqf)) return fail(YPDQ_ERR_ALIGN, "d_pdqf must be 16-byte aligned");
+  HashLaunch p{};
+  p.images = d_images;
+  p.n = n;
+  p.input_u8 = input_kind == YPDQ_INPUT_U8;
+  semantics_masks(semantics, &p.row_mask, &p.col_mask);
+  p.hashes = d_hashes;
+  p.quality = d_quality;
+  p.thresholds = d_thresholds;
+  p.pdqf = d_pdqf;
+  p.pdqf_slots = pdqf_slots;
+  p.buf1 = d_buf1;
+  p.dev_err = ctx->d_err;
+  CK(launch_hash(p, ctx->num_sms, p.input_u8 ? ctx->hash_ctas_u8 : ctx->hash_ctas_f32,
+                 reinterpret_cast<cudaStream_t>(stream)),
+     "hash kernel launch");
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_dihedrals_batch(ypdq_ctx* ctx, const float* d_pdqf, const float* d_thr,
+                                 int64_t n, int semantics, uint8_t* d_hashes, float* d_quality,
+                                 float* d_thr_out, float* d_pdqf_out, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (n < 0) return fail(YPDQ_ERR_INVALID, "n < 0");
+  if (n > 0 && !d_pdqf) return fail(YPDQ_ERR_INVALID, "d_pdqf is NULL");
+  if (semantics < YPDQ_DIHEDRAL_EXACT || semantics > YPDQ_DIHEDRAL_SCALAR)
+    return fail(YPDQ_ERR_INVALID, "semantics %d", semantics);
+  if (!aligned16(d_pdqf) || (d_pdqf_out && !aligned16(d_pdqf_out)))
+    return fail(YPDQ_ERR_ALIGN, "PDQF buffers must be 16-byte aligned");
+  DihedralLaunch p{};
+  p.pdqf = d_pdqf;
+  p.thr_in = d_thr;
+  p.n = n;
+  semantics_masks(semantics, &p.row_mask, &p.col_mask);
+  p.hashes = d_hashes;
+  p.quality = d_quality;
+  p.thresholds = d_thr_out;
+  p.pdqf_out = d_pdqf_out;
+  CK(launch_dihedrals(p, reinterpret_cast<cudaStream_t>(stream)), "dihedral kernel launch");
+  return YPDQ_OK;
+}
+
+// ----------------------------------------------------------------- matching
+
+ypdq_status ypdq_scan(ypdq_ctx* ctx, const uint8_t* d_rows, uint64_t n_rows,
+                      const uint8_t* d_queries, uint32_t n_queries, uint32_t threshold,
+                      ypdq_hit* d_hits, uint64_t capacity, uint64_t* d_count, int algo,
+                      ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (!d_count) return fail(YPDQ_ERR_INVALID, "d_count is NULL");
+  if (n_rows > 0 && !d_rows) return fail(YPDQ_ERR_INVALID, "d_rows is NULL");
+  if (n_queries > 0 && !d_queries) return fail(YPDQ_ERR_INVALID, "d_queries is NULL");
+  if (capacity > 0 && !d_hits) return fail(YPDQ_ERR_INVALID, "d_hits is NULL");
+  if (threshold > 256) return fail(YPDQ_ERR_INVALID, "threshold %u > 256", threshold);
+  if (algo < YPDQ_SCAN_AUTO || algo > YPDQ_SCAN_B1MMA)
+    return fail(YPDQ_ERR_INVALID, "algo %d", algo);
+  if (!aligned16(d_rows) || !aligned16(d_queries))
+    return fail(YPDQ_ERR_ALIGN, "rows and queries must be 16-byte aligned");
+  ScanLaunch p{};
+  p.rows = d_rows;
+  p.n_rows = n_rows;
+  p.queries = d_queries;
+  p.n_queries = n_queries;
+  p.threshold = threshold;
+  p.hits = d_hits;
+  p.capacity = capacity;
+  p.count = reinterpret_cast<unsigned long long*>(d_count);
+  CK(launch_scan(p, algo, ctx->num_sms, reinterpret_cast<cudaStream_t>(stream)), "scan launch");
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_sort_hits(ypdq_ctx* ctx, ypdq_hit* d_hits, uint64_t n, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (n > 0 && !d_hits) return fail(YPDQ_ERR_INVALID, "d_hits is NULL");
+  CK(launch_sort_hits(d_hits, n, reinterpret_cast<cudaStream_t>(stream)), "sort launch");
+  return YPDQ_OK;
+}
+
+// ----------------------------------------------------------------- database
+
+ypdq_status ypdq_db_create(ypdq_ctx* ctx, const uint8_t* h_rows, uint64_t n_rows, ypdq_db** out) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (!out || (n_rows > 0 && !h_rows)) return fail(YPDQ_ERR_INVALID, "NULL argument");
+  void* d = nullptr;
+  if (n_rows > 0) {
+    CK(cudaMalloc(&d, n_rows * 32), "cudaMalloc(db)");
+    cudaError_t e = cudaMemcpy(d, h_rows, n_rows * 32, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(d);
+      return cuda_fail(e, "db upload");
+    }
+  }
+  *out = new ypdq_db{ctx, static_cast<const uint8_t*>(d), n_rows, true};
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_db_wrap(ypdq_ctx* ctx, const uint8_t* d_rows, uint64_t n_rows, ypdq_db** out) {
+  if (!ctx || !out || (n_rows > 0 && !d_rows)) return fail(YPDQ_ERR_INVALID, "NULL argument");
+  if (!aligned16(d_rows)) return fail(YPDQ_ERR_ALIGN, "d_rows must be 16-byte aligned");
+  *out = new ypdq_db{ctx, d_rows, n_rows, false};
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_db_destroy(ypdq_db* db) {
+  if (!db) return YPDQ_OK;
+  if (db->owned && db->d_rows) {
+    cudaSetDevice(db->ctx->device);
+    cudaFree(const_cast<uint8_t*>(db->d_rows));
+  }
+  delete db;
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_db_info(ypdq_db* db, const uint8_t** d_rows, uint64_t* n_rows) {
+  if (!db) return fail(YPDQ_ERR_INVALID, "db is NULL");
+  if (d_rows) *d_rows = db->d_rows;
+  if (n_rows) *n_rows = db->n_rows;
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, int64_t n,
+                             int input_kind, int dct_precision, int semantics,
+                             uint32_t threshold, ypdq_hit* h_hits, uint64_t capacity,
+                             uint64_t* n_hits, uint8_t* h_hashes, float* h_quality) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (!db || !n_hits || (n > 0 && !h_images) || (capacity > 0 && !h_hits))
+    return fail(YPDQ_ERR_INVALID, "NULL argument");
+  if (n < 0 || n * 8 > 0xffffffffll) return fail(YPDQ_ERR_INVALID, "n out of range");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaStream_t s = ctx->stream;
+  const size_t img_bytes = (input_kind == YPDQ_INPUT_U8 ? 1u : 4u) * 512u * 512u;
+  void *d_img, *d_hash, *d_q, *d_hits, *d_cnt;
+  if ((st = scratch(ctx, 0, img_bytes * (n > 0 ? n : 1), &d_img))) return st;
+  if ((st = scratch(ctx, 1, 256 * (n > 0 ? n : 1), &d_hash))) return st;
+  if ((st = scratch(ctx, 2, 32 * (n > 0 ? n : 1), &d_q))) return st;
+  if ((st = scratch(ctx, 3, sizeof(ypdq_hit) * (capacity > 0 ? capacity : 1), &d_hits))) return st;
+  if ((st = scratch(ctx, 4, 64, &d_cnt))) return st;
+  if (n > 0) CK(cudaMemcpyAsync(d_img, h_images, img_bytes * n, cudaMemcpyHostToDevice, s), "H2D images");
+  if ((st = ypdq_hash_batch(ctx, d_img, n, input_kind, dct_precision, semantics,
+                            static_cast<uint8_t*>(d_hash), static_cast<float*>(d_q), nullptr,
+                            nullptr, 1, nullptr, reinterpret_cast<ypdq_stream_t>(s))))
+    return st;
+  if ((st = ypdq_scan(ctx, db->d_rows, db->n_rows, static_cast<uint8_t*>(d_hash),
+                      static_cast<uint32_t>(n * 8), threshold, static_cast<ypdq_hit*>(d_hits),
+                      capacity, static_cast<uint64_t*>(d_cnt), YPDQ_SCAN_AUTO,
+                      reinterpret_cast<ypdq_stream_t>(s))))
+    return st;
+  uint64_t total = 0;
+  CK(cudaMemcpyAsync(&total, d_cnt, sizeof(uint64_t), cudaMemcpyDeviceToHost, s), "D2H count");
+  CK(cudaStreamSynchronize(s), "screen sync");
+  const uint64_t m = total < capacity ? total : capacity;
+  CK(launch_sort_hits(static_cast<ypdq_hit*>(d_hits), m, s), "sort launch");
+  if (m > 0) CK(cudaMemcpyAsync(h_hits, d_hits, m * sizeof(ypdq_hit), cudaMemcpyDeviceToHost, s), "D2H hits");
+  if (h_hashes && n > 0) CK(cudaMemcpyAsync(h_hashes, d_hash, 256 * n, cudaMemcpyDeviceToHost, s), "D2H hashes");
+  if (h_quality && n > 0) CK(cudaMemcpyAsync(h_quality, d_q, 32 * n, cudaMemcpyDeviceToHost, s), "D2H quality");
+  CK(cudaStreamSynchronize(s), "screen sync");
+  if ((st = read_device_errors(ctx))) return st;
+  *n_hits = total;
+  if (total > capacity) return fail(YPDQ_ERR_OVERFLOW, "%llu hits > capacity %llu",
+                                    (unsigned long long)total, (unsigned long long)capacity);
+  return YPDQ_OK;
+}
+
+// --------------------------------------------------------- memory utilities
+
+ypdq_status ypdq_malloc_device(ypdq_ctx* ctx, size_t bytes, void** d_ptr) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (!d_ptr) return fail(YPDQ_ERR_INVALID, "d_ptr is NULL");
+  CK(cudaMalloc(d_ptr, bytes ? bytes : 1), "cudaMalloc");
+  return YPDQ_OK;
+}
+ypdq_status ypdq_free_device(ypdq_ctx* ctx, void* d_ptr) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  CK(cudaFree(d_ptr), "cudaFree");
+  return YPDQ_OK;
+}
+ypdq_status ypdq_malloc_host(ypdq_ctx* ctx, size_t bytes, void** h_ptr) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (!h_ptr) return fail(YPDQ_ERR_INVALID, "h_ptr is NULL");
+  CK(cudaMallocHost(h_ptr, bytes ? bytes : 1), "cudaMallocHost");
+  return YPDQ_OK;
+}
+ypdq_status ypdq_free_host(ypdq_ctx* ctx, void* h_ptr) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  CK(cudaFreeHost(h_ptr), "cudaFreeHost");
+  return YPDQ_OK;
+}
+ypdq_status ypdq_memcpy(ypdq_ctx* ctx, void* dst, const void* src, size_t bytes, int kind,
+                        ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  cudaMemcpyKind k = kind == 0   ? cudaMemcpyHostToDevice
+                     : kind == 1 ? cudaMemcpyDeviceToHost
+                     : kind == 2 ? cudaMemcpyDeviceToDevice
+                                 : cudaMemcpyDefault;
+  if (kind < 0 || kind > 2) return fail(YPDQ_ERR_INVALID, "memcpy kind %d", kind);
+  CK(cudaMemcpyAsync(dst, src, bytes, k, reinterpret_cast<cudaStream_t>(stream)), "cudaMemcpyAsync");
+  return YPDQ_OK;
+}
+ypdq_status ypdq_memset(ypdq_ctx* ctx, void* d_ptr, int value, size_t bytes, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  CK(cudaMemsetAsync(d_ptr, value, bytes, reinterpret_cast<cudaStream_t>(stream)), "cudaMemsetAsync");
+  return YPDQ_OK;
+}
+ypdq_status ypdq_stream_create(ypdq_ctx* ctx, ypdq_stream_t* out) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  cudaStream_t s;
+  CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+  *out = reinterpret_cast<ypdq_stream_t>(s);
+  return YPDQ_OK;
+}
+ypdq_status ypdq_stream_destroy(ypdq_ctx* ctx, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  CK(cudaStreamDestroy(reinterpret_cast<cudaStream_t>(stream)), "cudaStreamDestroy");
+  return YPDQ_OK;
+}
+ypdq_status ypdq_stream_sync(ypdq_ctx* ctx, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  CK(cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)), "cudaStreamSynchronize");
+  return read_device_errors(ctx);
+}
+ypdq_status ypdq_event_create(ypdq_ctx* ctx, ypdq_event_t* out) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  cudaEvent_t ev;
+  CK(cudaEventCreate(&ev), "cudaEventCreate");
+  *out = reinterpret_cast<ypdq_event_t>(ev);
+  return YPDQ_OK;
+}
+ypdq_status ypdq_event_destroy(ypdq_ctx* ctx, ypdq_event_t ev) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  CK(cudaEventDestroy(reinterpret_cast<cudaEvent_t>(ev)), "cudaEventDestroy");
+  return YPDQ_OK;
+}
+ypdq_status ypdq_event_record(ypdq_ctx* ctx, ypdq_event_t ev, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  CK(cudaEventRecord(reinterpret_cast<cudaEvent_t>(ev), reinterpret_cast<cudaStream_t>(stream)),
+     "cudaEventRecord");
+  return YPDQ_OK;
+}
+ypdq_status ypdq_event_elapsed_ms(ypdq_ctx* ctx, ypdq_event_t a, ypdq_event_t b, float* ms) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  CK(cudaEventSynchronize(reinterpret_cast<cudaEvent_t>(b)), "cudaEventSynchronize");
+  CK(cudaEventElapsedTime(ms, reinterpret_cast<cudaEvent_t>(a), reinterpret_cast<cudaEvent_t>(b)),
+     "cudaEventElapsedTime");
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_synth_rows(ypdq_ctx* ctx, uint8_t* d_rows, uint64_t n_rows, uint64_t first_row,
+                            uint64_t seed, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (n_rows > 0 && !d_rows) return fail(YPDQ_ERR_INVALID, "d_rows is NULL");
+  if (!aligned16(d_rows)) return fail(YPDQ_ERR_ALIGN, "d_rows must be 16-byte aligned");
+  CK(launch_synth_rows(d_rows, n_rows, first_row, seed, reinterpret_cast<cudaStream_t>(stream)),
+     "synth launch");
+  return YPDQ_OK;
+}
+
+// ------------------------------------------------------------ drop-in ABI
+
+__attribute__((visibility("default"))) const uint32_t YUME_PDQ_VERSION_MAJOR = 1;
+__attribute__((visibility("default"))) const uint32_t YUME_PDQ_VERSION_MINOR = 1;
+__attribute__((visibility("default"))) const uint32_t YUME_PDQ_VERSION_PATCH = 0;
+__attribute__((visibility("default"))) const char YUME_PDQ_VERSION_STRING[] = "1.1.0";
+
+// Dihedrals::from_tuples packs ((xx, xy), (yx, yy)) as big-endian i8 bytes (src/lib.rs:97-104).
+#define YPDQ_PACK(a, b, c, d)                                                             \
+  ((static_cast<uint32_t>(static_cast<uint8_t>(a)) << 24) |                               \
+   (static_cast<uint32_t>(static_cast<uint8_t>(b)) << 16) |                               \
+   (static_cast<uint32_t>(static_cast<uint8_t>(c)) << 8) | static_cast<uint32_t>(static_cast<uint8_t>(d)))
+__attribute__((visibility("default"))) const YumePDQ_Dihedrals YUME_PDQ_DIHEDRAL_NORMAL = {YPDQ_PACK(1, 0, 0, 1)};
+__attribute__((visibility("default"))) const YumePDQ_Dihedrals YUME_PDQ_DIHEDRAL_FLIPPED = {YPDQ_PACK(1, 0, 0, -1)};
+__attribute__((visibility("default"))) const YumePDQ_Dihedrals YUME_PDQ_DIHEDRAL_FLOPPED = {YPDQ_PACK(-1, 0, 0, 1)};
+__attribute__((visibility("default"))) const YumePDQ_Dihedrals YUME_PDQ_DIHEDRAL_ROTATED_180 = {YPDQ_PACK(-1, 0, 0, -1)};
+__attribute__((visibility("default"))) const YumePDQ_Dihedrals YUME_PDQ_DIHEDRAL_ROTATED_90 = {YPDQ_PACK(0, 1, -1, 0)};
+__attribute__((visibility("default"))) const YumePDQ_Dihedrals YUME_PDQ_DIHEDRAL_ROTATED_270 = {YPDQ_PACK(0, 1, 1, 0)};
+__attribute__((visibility("default"))) const YumePDQ_Dihedrals YUME_PDQ_DIHEDRAL_ROTATED_90_FLOPPED = {YPDQ_PACK(0, -1, -1, 0)};
+__attribute__((visibility("default"))) const YumePDQ_Dihedrals YUME_PDQ_DIHEDRAL_FLOPPED_ROTATED_270 = {YPDQ_PACK(0, -1, 1, 0)};
+
+}  // extern "C"
+
+namespace {
+
+std::once_flag g_dropin_once;
+ypdq_ctx* g_dropin_ctx = nullptr;
+int g_dropin_semantics = YPDQ_DIHEDRAL_EXACT;
+
+// The drop-in symbols use one library-owned context on device 0. The dihedral sign
+// convention comes from YUME_PDQ_DIHEDRAL_SEMANTICS = exact | avx2 | scalar (default exact).
+ypdq_ctx* dropin_ctx() {
+  std::call_once(g_dropin_once, [] {
+    const char* sem = getenv("YUME_PDQ_DIHEDRAL_SEMANTICS");
+    if (sem && !strcmp(sem, "avx2")) g_dropin_semantics = YPDQ_DIHEDRAL_AVX2;
+    if (sem && !strcmp(sem, "scalar")) g_dropin_semantics = YPDQ_DIHEDRAL_SCALAR;
+    ypdq_ctx* c = nullptr;
+    if (ypdq_ctx_create(0, &c) == YPDQ_OK) g_dropin_ctx = c;
+    else fprintf(stderr, "yume_pdq (gb300): %s\n", ypdq_last_error());
+  });
+  return g_dropin_ctx;
+}
+
+const uint32_t kSlotDihedral[8] = {
+    YPDQ_PACK(1, 0, 0, 1),   YPDQ_PACK(-1, 0, 0, 1), YPDQ_PACK(-1, 0, 0, -1), YPDQ_PACK(1, 0, 0, -1),
+    YPDQ_PACK(0, -1, -1, 0), YPDQ_PACK(0, 1, 1, 0),  YPDQ_PACK(0, -1, 1, 0),  YPDQ_PACK(0, 1, -1, 0)};
+
+ypdq_status dropin_hash(ypdq_ctx* ctx, const float* input, float* threshold, uint8_t* output,
+                        float* buf1, float* pdqf, float* quality) {
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  cudaStream_t s = ctx->stream;
+  void *d_img, *d_out, *d_buf1;
+  if ((st = scratch(ctx, 0, 512 * 512 * 4, &d_img))) return st;
+  if ((st = scratch(ctx, 5, 256 + 32 + 32 + 1024, &d_out))) return st;
+  if ((st = scratch(ctx, 6, 127 * 128 * 4, &d_buf1))) return st;
+  uint8_t* d_hash = static_cast<uint8_t*>(d_out);
+  float* d_q = reinterpret_cast<float*>(d_hash + 256);
+  float* d_t = d_q + 8;
+  float* d_p = d_t + 8;
+  CK(cudaMemcpyAsync(d_img, input, 512 * 512 * 4, cudaMemcpyHostToDevice, s), "H2D image");
+  HashLaunch p{};
+  p.images = d_img;
+  p.n = 1;
+  p.input_u8 = 0;
+  semantics_masks(g_dropin_semantics, &p.row_mask, &p.col_mask);
+  p.hashes = d_hash;
+  p.quality = d_q;
+  p.thresholds = d_t;
+  p.pdqf = d_p;
+  p.pdqf_slots = 1;
+  p.buf1 = buf1 ? static_cast<float*>(d_buf1) : nullptr;
+  p.dev_err = ctx->d_err;
+  CK(launch_hash(p, ctx->num_sms, ctx->hash_ctas_f32, s), "hash launch");
+  uint8_t out[256 + 32 + 32 + 1024];
+  CK(cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s), "D2H results");
+  if (buf1)
+    CK(cudaMemcpy2DAsync(buf1, 128 * 4, d_buf1, 128 * 4, 127 * 4, 127, cudaMemcpyDeviceToHost, s),
+       "D2H buf1");
+  CK(cudaStreamSynchronize(s), "sync");
+  if ((st = read_device_errors(ctx))) return st;
+  memcpy(output, out, 32);
+  float q, t;
+  memcpy(&q, out + 256, 4);
+  memcpy(&t, out + 256 + 32, 4);
+  if (threshold) *threshold = t;
+  if (pdqf) memcpy(pdqf, out + 256 + 64, 1024);
+  *quality = q;
+  return YPDQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+__attribute__((visibility("default"))) float yume_pdq_hash_smart_kernel(
+    const float* input, float* threshold, uint8_t* output, float* buf1, float* tmp, float* pdqf) {
+  (void)tmp;
+  ypdq_ctx* ctx = dropin_ctx();
+  if (!ctx || !input || !output) {
+    fprintf(stderr, "yume_pdq_hash_smart_kernel: %s\n",
+            ctx ? "NULL input/output" : "no CUDA context");
+    return -1.0f;
+  }
+  float q = -1.0f;
+  if (dropin_hash(ctx, input, threshold, output, buf1, pdqf, &q) != YPDQ_OK) {
+    fprintf(stderr, "yume_pdq_hash_smart_kernel: %s\n", ypdq_last_error());
+    return -1.0f;
+  }
+  return q;
+}
+
+__attribute__((visibility("default"))) bool yume_pdq_visit_dihedrals_smart_kernel(
+    void* cb_ctx, float threshold, uint8_t* output, float* pdqf, DihedralCallback callback) {
+  ypdq_ctx* ctx = dropin_ctx();
+  if (!ctx || !output || !pdqf || !callback) {
+    fprintf(stderr, "yume_pdq_visit_dihedrals_smart_kernel: %s\n",
+            ctx ? "NULL argument" : "no CUDA context");
+    return false;
+  }
+  uint8_t res[256 + 32 + 32 + 8 * 1024];
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (check_ctx(ctx) != YPDQ_OK) return false;
+    cudaStream_t s = ctx->stream;
+    void *d_in, *d_out;
+    ypdq_status st;
+    if ((st = scratch(ctx, 5, 1024 + 16, &d_in)) || (st = scratch(ctx, 7, sizeof(res), &d_out))) {
+      fprintf(stderr, "yume_pdq_visit_dihedrals_smart_kernel: %s\n", ypdq_last_error());
+      return false;
+    }
+    float* d_p = static_cast<float*>(d_in);
+    float* d_thr = d_p + 256;
+    uint8_t* d_hash = static_cast<uint8_t*>(d_out);
+    float* d_q = reinterpret_cast<float*>(d_hash + 256);
+    float* d_t = d_q + 8;
+    float* d_pv = d_t + 8;
+    cudaError_t e = cudaMemcpyAsync(d_p, pdqf, 1024, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_thr, &threshold, 4, cudaMemcpyHostToDevice, s);
+    DihedralLaunch p{};
+    p.pdqf = d_p;
+    p.thr_in = d_thr;
+    p.n = 1;
+    semantics_masks(g_dropin_semantics, &p.row_mask, &p.col_mask);
+    p.hashes = d_hash;
+    p.quality = d_q;
+    p.thresholds = d_t;
+    p.pdqf_out = d_pv;
+    if (e == cudaSuccess) e = launch_dihedrals(p, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(res, d_out, sizeof(res), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "yume_pdq_visit_dihedrals_smart_kernel: %s\n", cudaGetErrorString(e));
+      return false;
+    }
+  }
+  const float* q = reinterpret_cast<const float*>(res + 256);
+  const float* pv = reinterpret_cast<const float*>(res + 256 + 64);
+  for (int v = 1; v < 8; ++v) {
+    memcpy(output, res + v * 32, 32);
+    memcpy(pdqf, pv + v * 256, 1024);
+    if (!callback(cb_ctx, kSlotDihedral[v], threshold, q[v])) return false;
+  }
+  return true;
+}
+
+}  // extern "C"

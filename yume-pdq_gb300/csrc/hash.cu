@@ -1,0 +1,533 @@
+// Fused PDQ hash kernel: 512x512 image -> tent compress -> DCT -> quality -> exact median
+// quantize -> the 8 dihedral hashes, for a batch of images, one image per CTA at a time.
+//
+// Reference semantics (yume-pdq):
+//   compress  DefaultKernel::jarosz_compress   src/kernel/mod.rs:644-666
+//   DCT       DefaultKernel::dct2d_impl        src/kernel/mod.rs:543-574
+//   quality   sum_of_gradients / adjust_quality src/kernel/mod.rs:611-642
+//   median    torben_median                    src/kernel/mod.rs:212-253 (the 128th smallest)
+//   packing   quantize / threshold_2d_f32      src/kernel/mod.rs:595-608, threshold.rs:37-119
+//   dihedrals visit_dihedrals                  src/lib.rs:358-420
+//
+// The FP32 path reproduces the reference's f32 results bit for bit for finite inputs.
+// Every product and sum is a separately rounded __fmul_rn / __fadd_rn (the reference is
+// Rust, which never contracts a*b+c). Sums run in the reference's order: taps row by row;
+// the DCT in four interleaved partial sums combined as ((s0+s1)+s2)+s3. The tent table is
+// 7x7, but only 27 taps are nonzero: the 5x5 centre (k/81) and two subnormal residues in
+// row 0 that the reference's 128-bit constant generation leaves behind. A zero tap adds +0
+// to a finite partial sum, which changes nothing, so the kernel skips those taps.
+//
+// CTA layout (192 threads):
+//   warps 0-3  compute: thread j owns output column j (j < 127) of the compressed image,
+//              accumulates DCT stage 1 (16 x 127 x 127) as each compressed row appears,
+//              then computes the 16 x 16 stage 2 together.
+//   warp 4     producer: one lane streams the image into a shared-memory ring with 1-D
+//              bulk async copies (4 input rows = one stage), NSTAGE stages deep.
+//   warp 5     epilogue: quality, exact medians, bits and dihedrals of image k while the
+//              compute warps already work on image k+1 (double-buffered PDQF).
+#include <cstring>
+
+#include "ypdq_internal.cuh"
+#include "ypdq_tables.h"
+
+namespace ypdq {
+
+__device__ float g_dct[16 * 127];  // D[k][i] = sqrt(2/127) cos(pi (k+1) (2i+1) / 254), f32
+
+constexpr int kNumStages = 8;
+constexpr int kStagesPerImage = 128;  // stage s holds rows 4s+1 .. 4s+4 (stage 127: 509, 510)
+constexpr int kComputeThreads = 128;
+constexpr int kProducerWarp = 4;
+constexpr int kEpilogueWarp = 5;
+constexpr int kHashThreads = 192;
+constexpr int kComputeBarrier = 1;  // named barrier id used by the 128 compute threads
+
+template <int kStageBytes>
+struct HashSmem {
+  alignas(128) unsigned char ring[kNumStages][kStageBytes];
+  alignas(16) float dt[128][16];  // dt[i][k] = D[k][i]; row 127 is zero
+  float dr[16][129];              // D[k][m], padded against bank conflicts
+  float t[16][129];               // DCT stage 1 result T = D * B
+  alignas(16) float p[2][256];    // PDQF, double-buffered between compute and epilogue
+  uint64_t full[kNumStages];
+  uint64_t empty[kNumStages];
+  uint64_t pfull[2];
+  uint64_t pempty[2];
+  int abort_flag;
+};
+
+template <typename Tin>
+struct InputTraits;
+template <>
+struct InputTraits<float> {
+  static constexpr int kRowBytes = 512 * 4;
+};
+template <>
+struct InputTraits<uint8_t> {
+  static constexpr int kRowBytes = 512;
+};
+
+// Columns 4j .. 4j+7 of one input row held in shared memory.
+__device__ __forceinline__ void load_row8(const float* row, int j, float x[8]) {
+  const float4* r = reinterpret_cast<const float4*>(row);
+  float4 a = r[j], b = r[j + 1];
+  x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+  x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+}
+__device__ __forceinline__ void load_row8(const uint8_t* row, int j, float x[8]) {
+  const uint32_t* r = reinterpret_cast<const uint32_t*>(row);
+  uint32_t a = r[j], b = r[j + 1];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    x[e] = static_cast<float>((a >> (8 * e)) & 0xffu);
+    x[4 + e] = static_cast<float>((b >> (8 * e)) & 0xffu);
+  }
+}
+
+#define YPDQ_W(di, dj) __uint_as_float(YPDQ_TENT_BITS_##di##_##dj)
+#define YPDQ_TAP(acc, di, dj, x) acc = __fadd_rn(acc, __fmul_rn(YPDQ_W(di, dj), (x)))
+#define YPDQ_ROW_TAPS(acc, di, x)     \
+  YPDQ_TAP(acc, di, 1, x[2]);         \
+  YPDQ_TAP(acc, di, 2, x[3]);         \
+  YPDQ_TAP(acc, di, 3, x[4]);         \
+  YPDQ_TAP(acc, di, 4, x[5]);         \
+  YPDQ_TAP(acc, di, 5, x[6])
+
+// Compressed value (i, j): rows 4i+1 .. 4i+6 come from stage i (rows 0..3) and stage i+1
+// (rows 0..1); tap (di, dj) reads input column 4j+1+dj, which is x[1+dj].
+template <typename Tin>
+__device__ __forceinline__ float compress_at(const Tin* st0, const Tin* st1, int j) {
+  constexpr int kRow = 512;  // elements per row
+  float x[8];
+  float s = 0.0f;
+  load_row8(st0 + 0 * kRow, j, x);  // row 4i+1: only the two residue taps are nonzero
+  YPDQ_TAP(s, 0, 4, x[5]);
+  YPDQ_TAP(s, 0, 5, x[6]);
+  load_row8(st0 + 1 * kRow, j, x);
+  YPDQ_ROW_TAPS(s, 1, x);
+  load_row8(st0 + 2 * kRow, j, x);
+  YPDQ_ROW_TAPS(s, 2, x);
+  load_row8(st0 + 3 * kRow, j, x);
+  YPDQ_ROW_TAPS(s, 3, x);
+  load_row8(st1 + 0 * kRow, j, x);
+  YPDQ_ROW_TAPS(s, 4, x);
+  load_row8(st1 + 1 * kRow, j, x);
+  YPDQ_ROW_TAPS(s, 5, x);
+  return s;
+}
+
+// ---------------------------------------------------------------- epilogue
+
+__device__ __forceinline__ uint32_t f32_key(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_f32(uint32_t k) {
+  uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+  return __uint_as_float(u);
+}
+
+// Exact 128th-smallest (rank 127) of four 256-value sets held 8 per lane: MSB-first
+// radix selection on order-preserving keys, one warp reduction per bit and set.
+__device__ __forceinline__ void select_rank127_x4(const float (&v)[4][8], float (&out)[4]) {
+  uint32_t key[4][8];
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) key[s][e] = f32_key(v[s][e]);
+  uint32_t prefix[4] = {0u, 0u, 0u, 0u};
+  int rank[4] = {127, 127, 127, 127};
+  uint32_t decided = 0u;
+#pragma unroll 4
+  for (int bit = 31; bit >= 0; --bit) {
+    const uint32_t b = 1u << bit;
+    const uint32_t m = decided | b;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      uint32_t c = 0;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) c += ((key[s][e] & m) == prefix[s]) ? 1u : 0u;
+      const int tot = static_cast<int>(__reduce_add_sync(0xffffffffu, c));
+      if (rank[s] >= tot) {
+        rank[s] -= tot;
+        prefix[s] |= b;
+      }
+    }
+    decided = m;
+  }
+#pragma unroll
+  for (int s = 0; s < 4; ++s) out[s] = key_f32(prefix[s]);
+}
+
+// Slot s of the 8 outputs: value at (r, c) is sign * (s < 4 ? P[r][c] : P[c][r]).
+// Row signs (row_mask) apply in slots 2, 3, 5, 6; column signs (col_mask) in 1, 2, 6, 7.
+__device__ __forceinline__ bool slot_rows(int s) { return s == 2 || s == 3 || s == 5 || s == 6; }
+__device__ __forceinline__ bool slot_cols(int s) { return s == 1 || s == 2 || s == 6 || s == 7; }
+
+// Sum of gradients of slot s, summed sequentially in the reference order.
+__device__ float slot_gradient(const float* P, int s, uint32_t rm, uint32_t cm) {
+  const bool tr = s >= 4, ur = slot_rows(s), uc = slot_cols(s);
+  auto val = [&](int r, int c) -> float {
+    float x = tr ? P[c * 16 + r] : P[r * 16 + c];
+    bool neg = (ur && ((rm >> r) & 1u)) != (uc && ((cm >> c) & 1u));
+    return neg ? -x : x;
+  };
+  float g = 0.0f;
+  float prev[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) prev[c] = val(0, c);
+#pragma unroll 1
+  for (int r = 0; r < 15; ++r) {
+    float nxt[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) nxt[c] = val(r + 1, c);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      g = __fadd_rn(g, fabsf(__fsub_rn(prev[c], nxt[c])));
+      prev[c] = nxt[c];
+    }
+  }
+#pragma unroll 1
+  for (int r = 0; r < 16; ++r) {
+    float row[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) row[c] = val(r, c);
+#pragma unroll
+    for (int c = 0; c < 15; ++c) g = __fadd_rn(g, fabsf(__fsub_rn(row[c], row[c + 1])));
+  }
+  return g;
+}
+
+struct EpilogueOut {
+  uint8_t* hashes;   // [8][32]
+  float* quality;    // [8]
+  float* thresholds; // [8]
+  float* pdqf;       // [pdqf_slots][256]
+  int pdqf_slots;
+};
+
+// One warp turns a PDQF held in shared memory into the 8 slot hashes, thresholds and
+// qualities. With thr0_given the slot-0 threshold is taken from the caller.
+__device__ void epilogue_warp(const float* P, bool thr0_given, float thr0_in, uint32_t rm,
+                              uint32_t cm, int lane, const EpilogueOut& o) {
+  // lane owns flat elements k = 8*lane + e, i.e. row i = lane/2, columns j0 .. j0+7
+  const int i = lane >> 1, j0 = (lane & 1) << 3;
+  const bool rneg = (rm >> i) & 1u;
+  float x[8], xt[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    x[e] = P[i * 16 + j0 + e];
+    xt[e] = P[(j0 + e) * 16 + i];
+  }
+  float v[8][8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const bool cneg = (cm >> (j0 + e)) & 1u;
+    const float cx = cneg ? -x[e] : x[e];
+    const float cxt = cneg ? -xt[e] : xt[e];
+    v[0][e] = x[e];
+    v[1][e] = cx;
+    v[2][e] = rneg ? -cx : cx;
+    v[3][e] = rneg ? -x[e] : x[e];
+    v[4][e] = xt[e];
+    v[5][e] = rneg ? -xt[e] : xt[e];
+    v[6][e] = rneg ? -cxt : cxt;
+    v[7][e] = cxt;
+  }
+  float med[4];
+  {
+    float sel[4][8];
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+      for (int e = 0; e < 8; ++e) sel[s][e] = v[s][e];
+    select_rank127_x4(sel, med);
+  }
+  float thr[8];
+  thr[0] = thr0_given ? thr0_in : med[0];
+  thr[1] = med[1];
+  thr[2] = med[2];
+  thr[3] = med[3];
+  thr[4] = thr[0];
+  thr[5] = thr[1];
+  thr[6] = thr[2];
+  thr[7] = thr[3];
+  if (o.hashes) {
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      uint32_t byte = 0;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) byte |= (v[s][e] > thr[s] ? 1u : 0u) << e;
+      o.hashes[s * 32 + 31 - lane] = static_cast<uint8_t>(byte);
+    }
+  }
+  if (o.pdqf) {
+    const int slots = o.pdqf_slots == 8 ? 8 : 1;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      if (s < slots) {
+        float4* dst = reinterpret_cast<float4*>(o.pdqf + s * 256 + lane * 8);
+        dst[0] = make_float4(v[s][0], v[s][1], v[s][2], v[s][3]);
+        dst[1] = make_float4(v[s][4], v[s][5], v[s][6], v[s][7]);
+      }
+    }
+  }
+  if (lane < 8) {
+    float t = thr[0];
+#pragma unroll
+    for (int s = 1; s < 8; ++s)
+      if (lane == s) t = thr[s];
+    if (o.thresholds) o.thresholds[lane] = t;
+    if (o.quality) {
+      const float g = slot_gradient(P, lane, rm, cm);
+      o.quality[lane] = fminf(__fdiv_rn(g, 180.0f), 1.0f);
+    }
+  }
+}
+
+// ------------------------------------------------------------------- kernel
+
+template <typename Tin>
+__global__ void __launch_bounds__(kHashThreads) hash_kernel(const HashLaunch prm) {
+  constexpr int kRowBytes = InputTraits<Tin>::kRowBytes;
+  constexpr int kStageBytes = 4 * kRowBytes;
+  using Smem = HashSmem<kStageBytes>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+
+  for (int idx = tid; idx < 16 * 127; idx += kHashThreads) {
+    const int k = idx / 127, i = idx - k * 127;
+    const float d = g_dct[idx];
+    sm.dt[i][k] = d;
+    sm.dr[k][i] = d;
+  }
+  if (tid < 16) sm.dt[127][tid] = 0.0f;
+  if (tid == 0) {
+    for (int s = 0; s < kNumStages; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.empty[s], kComputeThreads / 32);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.pfull[b], kComputeThreads / 32);
+      mbar_init(&sm.pempty[b], 1);
+    }
+    sm.abort_flag = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  volatile int* abort_flag = &sm.abort_flag;
+  const int64_t n_images = prm.n;
+  const unsigned char* images = static_cast<const unsigned char*>(prm.images);
+  constexpr int64_t kImageBytes = 512ll * kRowBytes;
+
+  if (warp == kProducerWarp) {
+    if (lane != 0) return;
+    const uint64_t policy = policy_evict_first();
+    uint32_t g = 0;
+    bool ok = true;
+    for (int64_t n = blockIdx.x; n < n_images && ok; n += gridDim.x) {
+      const unsigned char* img = images + n * kImageBytes;
+      for (int s = 0; s < kStagesPerImage; ++s, ++g) {
+        const uint32_t slot = g % kNumStages;
+        if (!mbar_wait(&sm.empty[slot], ((g / kNumStages) & 1u) ^ 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        const uint32_t bytes = (s < kStagesPerImage - 1) ? 4 * kRowBytes : 2 * kRowBytes;
+        mbar_arrive_expect_tx(&sm.full[slot], bytes);
+        bulk_g2s(sm.ring[slot], img + static_cast<int64_t>(4 * s + 1) * kRowBytes, bytes,
+                 &sm.full[slot], policy);
+      }
+    }
+    if (!ok) {
+      *abort_flag = 1;
+      atomicOr(prm.dev_err, kDevErrTimeout);
+      // Let the copies already issued land before the CTA exits (bounded wait each).
+      for (uint32_t k = 1; k <= kNumStages && k <= g; ++k) {
+        const uint32_t gi = g - k;
+        const uint64_t t0 = globaltimer_ns();
+        while (!mbar_try_wait(&sm.full[gi % kNumStages], (gi / kNumStages) & 1u)) {
+          if (globaltimer_ns() - t0 > kWaitLimitNs / 4) break;
+        }
+      }
+    }
+    return;
+  }
+
+  if (warp == kEpilogueWarp) {
+    uint32_t it = 0;
+    for (int64_t n = blockIdx.x; n < n_images; n += gridDim.x, ++it) {
+      const int pb = it & 1;
+      if (!mbar_wait(&sm.pfull[pb], (it >> 1) & 1u, abort_flag)) {
+        *abort_flag = 1;
+        if (lane == 0) atomicOr(prm.dev_err, kDevErrTimeout);
+        return;
+      }
+      EpilogueOut o;
+      o.hashes = prm.hashes ? prm.hashes + n * 256 : nullptr;
+      o.quality = prm.quality ? prm.quality + n * 8 : nullptr;
+      o.thresholds = prm.thresholds ? prm.thresholds + n * 8 : nullptr;
+      o.pdqf_slots = prm.pdqf_slots;
+      o.pdqf = prm.pdqf ? prm.pdqf + n * (prm.pdqf_slots == 8 ? 8 : 1) * 256 : nullptr;
+      epilogue_warp(sm.p[pb], false, 0.0f, prm.row_mask, prm.col_mask, lane, o);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.pempty[pb]);
+    }
+    return;
+  }
+
+  // ---- compute warps: thread j <-> compressed column j
+  const int j = tid;
+  const bool active = j < 127;
+  uint32_t it = 0;
+  for (int64_t n = blockIdx.x; n < n_images; n += gridDim.x, ++it) {
+    const uint32_t g0 = it * kStagesPerImage;
+    float acc[16][4];
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[k][r] = 0.0f;
+
+    if (!mbar_wait(&sm.full[g0 % kNumStages], (g0 / kNumStages) & 1u, abort_flag)) goto fail;
+    for (int i0 = 0; i0 < 128; i0 += 4) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int i = i0 + r;
+        if (i < 127) {
+          const uint32_t ga = g0 + i, gb = ga + 1;
+          if (!mbar_wait(&sm.full[gb % kNumStages], (gb / kNumStages) & 1u, abort_flag))
+            goto fail;
+          float b = 0.0f;
+          if (active) {
+            const Tin* st0 = reinterpret_cast<const Tin*>(sm.ring[ga % kNumStages]);
+            const Tin* st1 = reinterpret_cast<const Tin*>(sm.ring[gb % kNumStages]);
+            b = compress_at<Tin>(st0, st1, j);
+            if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b;
+          }
+          const float4* d4 = reinterpret_cast<const float4*>(&sm.dt[i][0]);
+          const float4 da = d4[0], db = d4[1], dc = d4[2], dd = d4[3];
+          const float d[16] = {da.x, da.y, da.z, da.w, db.x, db.y, db.z, db.w,
+                               dc.x, dc.y, dc.z, dc.w, dd.x, dd.y, dd.z, dd.w};
+#pragma unroll
+          for (int k = 0; k < 16; ++k) acc[k][r] = __fadd_rn(acc[k][r], __fmul_rn(d[k], b));
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&sm.empty[ga % kNumStages]);
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.empty[(g0 + 127) % kNumStages]);
+
+    if (active) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        sm.t[k][j] = __fadd_rn(__fadd_rn(__fadd_rn(acc[k][0], acc[k][1]), acc[k][2]), acc[k][3]);
+    }
+    named_bar_sync(kComputeBarrier, kComputeThreads);
+    {
+      // stage 2: P[k][c] = sum_m T[k][m] * D[c][m]; thread -> (k, c0), (k, c0 + 1)
+      const int k = tid >> 3, c0 = (tid & 7) * 2;
+      float s0[4] = {0.f, 0.f, 0.f, 0.f}, s1[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int m0 = 0; m0 < 128; m0 += 4) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int m = m0 + r;
+          if (m < 127) {
+            const float tv = sm.t[k][m];
+            s0[r] = __fadd_rn(s0[r], __fmul_rn(tv, sm.dr[c0][m]));
+            s1[r] = __fadd_rn(s1[r], __fmul_rn(tv, sm.dr[c0 + 1][m]));
+          }
+        }
+      }
+      const float o0 = __fadd_rn(__fadd_rn(__fadd_rn(s0[0], s0[1]), s0[2]), s0[3]);
+      const float o1 = __fadd_rn(__fadd_rn(__fadd_rn(s1[0], s1[1]), s1[2]), s1[3]);
+      const int pb = it & 1;
+      if (!mbar_wait(&sm.pempty[pb], ((it >> 1) & 1u) ^ 1u, abort_flag)) goto fail;
+      sm.p[pb][k * 16 + c0] = o0;
+      sm.p[pb][k * 16 + c0 + 1] = o1;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.pfull[pb]);
+    }
+    named_bar_sync(kComputeBarrier, kComputeThreads);
+  }
+  return;
+fail:
+  *abort_flag = 1;
+  if (lane == 0) atomicOr(prm.dev_err, kDevErrTimeout);
+}
+
+// Dihedrals of given PDQF matrices: one warp per matrix.
+__global__ void __launch_bounds__(128) dihedral_kernel(const DihedralLaunch prm) {
+  __shared__ __align__(16) float P[4][256];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * 4 + w;
+  if (n >= prm.n) return;
+  const float4* src = reinterpret_cast<const float4*>(prm.pdqf + n * 256);
+  float4* dst = reinterpret_cast<float4*>(P[w]);
+  dst[lane] = src[lane];
+  dst[lane + 32] = src[lane + 32];
+  __syncwarp();
+  EpilogueOut o;
+  o.hashes = prm.hashes ? prm.hashes + n * 256 : nullptr;
+  o.quality = prm.quality ? prm.quality + n * 8 : nullptr;
+  o.thresholds = prm.thresholds ? prm.thresholds + n * 8 : nullptr;
+  o.pdqf = prm.pdqf_out ? prm.pdqf_out + n * 8 * 256 : nullptr;
+  o.pdqf_slots = 8;
+  const bool given = prm.thr_in != nullptr;
+  epilogue_warp(P[w], given, given ? prm.thr_in[n] : 0.0f, prm.row_mask, prm.col_mask, lane, o);
+}
+
+// ------------------------------------------------------------------ host side
+
+template <typename Tin>
+static size_t hash_smem_bytes() {
+  return sizeof(HashSmem<4 * InputTraits<Tin>::kRowBytes>);
+}
+
+cudaError_t upload_constants() {
+  float d[16 * 127];
+  for (int i = 0; i < 16 * 127; ++i) {
+    uint32_t b = YPDQ_DCT_F32_BITS[i];
+    memcpy(&d[i], &b, 4);
+  }
+  cudaError_t e = cudaMemcpyToSymbol(g_dct, d, sizeof(d));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(hash_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(hash_smem_bytes<float>()));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(hash_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(hash_smem_bytes<uint8_t>()));
+}
+
+cudaError_t hash_occupancy(int input_u8, int* ctas_per_sm) {
+  if (input_u8)
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        ctas_per_sm, hash_kernel<uint8_t>, kHashThreads, hash_smem_bytes<uint8_t>());
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, hash_kernel<float>,
+                                                       kHashThreads, hash_smem_bytes<float>());
+}
+
+cudaError_t launch_hash(const HashLaunch& p, int num_sms, int ctas_per_sm, cudaStream_t s) {
+  if (p.n <= 0) return cudaSuccess;
+  int64_t grid = static_cast<int64_t>(num_sms) * (ctas_per_sm > 0 ? ctas_per_sm : 1);
+  if (grid > p.n) grid = p.n;
+  if (p.input_u8) {
+    hash_kernel<uint8_t><<<static_cast<int>(grid), kHashThreads, hash_smem_bytes<uint8_t>(), s>>>(p);
+  } else {
+    hash_kernel<float><<<static_cast<int>(grid), kHashThreads, hash_smem_bytes<float>(), s>>>(p);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dihedrals(const DihedralLaunch& p, cudaStream_t s) {
+  if (p.n <= 0) return cudaSuccess;
+  const int64_t grid = (p.n + 3) / 4;
+  dihedral_kernel<<<static_cast<unsigned>(grid), 128, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace ypdq

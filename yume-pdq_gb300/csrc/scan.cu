@@ -1,0 +1,228 @@
+// Exact linear Hamming scan of 256-bit rows against a batch of 256-bit queries, with
+// warp-aggregated hit compaction.
+//
+// Reference: CpuMatcher::find (scalar, src/matching/mod.rs:336-362) reports every
+// (row, needle) with popcount(row ^ needle) <= threshold; the WGSL matcher
+// (src/matching/vulkan.rs:98-147) evaluates the same predicate, one row per thread.
+// Both kernels here return the full hit set with distances. They differ only in how
+// they compute distances:
+//   SIMT   one row per thread, eight 32-bit XOR + POPC per (row, query);
+//   B1MMA  16 rows x 8 queries per warp instruction with the binary tensor-core MMA
+//          (mma.sync m16n8k256 .b1 .xor.popc), whose accumulator is the distance.
+#include "ypdq_internal.cuh"
+
+namespace ypdq {
+
+constexpr int kScanThreads = 256;
+constexpr uint32_t kMaxSmemQueries = 2048;  // queries per launch (64 KiB of shared memory)
+
+// Hit emission from lanes that found a hit in the same converged step: one atomic per warp.
+__device__ __forceinline__ void emit_hits_ballot(bool pred, uint64_t row, uint32_t query,
+                                                 uint32_t dist, ypdq_hit* hits, uint64_t cap,
+                                                 unsigned long long* count) {
+  const uint32_t ballot = __ballot_sync(0xffffffffu, pred);
+  if (ballot == 0) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(ballot) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(count, static_cast<unsigned long long>(__popc(ballot)));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (pred) {
+    const uint64_t pos = base + __popc(ballot & lanemask_lt());
+    if (pos < cap) {
+      ypdq_hit h;
+      h.index = row;
+      h.query = query;
+      h.distance = dist;
+      hits[pos] = h;
+    }
+  }
+}
+
+__device__ __forceinline__ uint4 ld_stream(const uint4* p) {
+  uint4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p));
+  return v;
+}
+
+// ------------------------------------------------------------------- SIMT
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_simt_kernel(const uint4* __restrict__ rows, uint64_t n_rows,
+                     const uint4* __restrict__ queries, uint32_t nq, uint32_t q_base,
+                     uint32_t t, ypdq_hit* hits, uint64_t cap, unsigned long long* count) {
+  extern __shared__ uint4 sq[];
+  for (uint32_t i = threadIdx.x; i < 2 * nq; i += blockDim.x) sq[i] = queries[i];
+  __syncthreads();
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  // Every lane of a warp runs the same number of iterations so the ballots stay converged.
+  const uint64_t first = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t warp_first = first & ~31ull;
+  for (uint64_t base = warp_first; base < n_rows; base += stride) {
+    const uint64_t r = base + (threadIdx.x & 31);
+    const bool valid = r < n_rows;
+    uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
+    if (valid) {
+      a = ld_stream(rows + 2 * r);
+      b = ld_stream(rows + 2 * r + 1);
+    }
+#pragma unroll 4
+    for (uint32_t q = 0; q < nq; ++q) {
+      const uint4 qa = sq[2 * q], qb = sq[2 * q + 1];
+      const uint32_t d = __popc(a.x ^ qa.x) + __popc(a.y ^ qa.y) + __popc(a.z ^ qa.z) +
+                         __popc(a.w ^ qa.w) + __popc(b.x ^ qb.x) + __popc(b.y ^ qb.y) +
+                         __popc(b.z ^ qb.z) + __popc(b.w ^ qb.w);
+      const bool hit = valid && d <= t;
+      if (__any_sync(0xffffffffu, hit)) emit_hits_ballot(hit, r, q_base + q, d, hits, cap, count);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ B1 MMA
+
+__device__ __forceinline__ void mma_b1_xor_popc(uint32_t a0, uint32_t a1, uint32_t a2,
+                                                uint32_t a3, uint32_t b0, uint32_t b1,
+                                                uint32_t& d0, uint32_t& d1, uint32_t& d2,
+                                                uint32_t& d3) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k256.row.col.s32.b1.b1.s32.xor.popc "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%10,%10,%10,%10};"
+      : "=r"(d0), "=r"(d1), "=r"(d2), "=r"(d3)
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1), "r"(0));
+}
+
+// Fragment layout of m16n8k256 (.b1): lane = 4*g + tq holds
+//   a0: row g,   k = 32 tq .. 32 tq + 31      a2: row g,   k = 128 + 32 tq ..
+//   a1: row g+8, k = 32 tq ..                 a3: row g+8, k = 128 + 32 tq ..
+//   b0: col (query) g, k = 32 tq ..           b1: col g,   k = 128 + 32 tq ..
+//   d0,d1: row g, queries 2tq, 2tq+1          d2,d3: row g+8, queries 2tq, 2tq+1
+// The distance is a popcount over all k, so any fixed word <-> k-slot assignment works as
+// long as rows and queries use the same one: k-slot tq <-> word 2tq, slot 128+32tq <->
+// word 2tq+1. Each lane then loads one 8-byte pair of words per row.
+__global__ void __launch_bounds__(kScanThreads)
+    scan_b1_kernel(const uint2* __restrict__ rows, uint64_t n_rows,
+                   const uint2* __restrict__ queries, uint32_t nq, uint32_t q_base, uint32_t t,
+                   ypdq_hit* hits, uint64_t cap, unsigned long long* count) {
+  extern __shared__ uint2 sfrag[];  // [chunks][32 lanes]
+  const uint32_t chunks = (nq + 7) / 8;
+  for (uint32_t idx = threadIdx.x; idx < chunks * 32; idx += blockDim.x) {
+    const uint32_t c = idx >> 5, l = idx & 31, g = l >> 2, tq = l & 3;
+    const uint32_t qi = 8 * c + g;
+    sfrag[idx] = qi < nq ? queries[qi * 4 + tq] : make_uint2(0, 0);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const uint32_t g = lane >> 2, tq = lane & 3;
+  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  const uint64_t n_tiles = (n_rows + 15) / 16;
+  for (uint64_t tile = warp; tile < n_tiles; tile += n_warps) {
+    const uint64_t r0 = tile * 16 + g, r1 = r0 + 8;
+    uint2 A0 = make_uint2(0, 0), A1 = make_uint2(0, 0);
+    if (r0 < n_rows) A0 = rows[r0 * 4 + tq];
+    if (r1 < n_rows) A1 = rows[r1 * 4 + tq];
+    for (uint32_t c = 0; c < chunks; ++c) {
+      const uint2 B = sfrag[c * 32 + lane];
+      uint32_t d0, d1, d2, d3;
+      mma_b1_xor_popc(A0.x, A1.x, A0.y, A1.y, B.x, B.y, d0, d1, d2, d3);
+      const uint32_t q0 = 8 * c + 2 * tq, q1 = q0 + 1;
+      const bool h0 = r0 < n_rows && q0 < nq && d0 <= t;
+      const bool h1 = r0 < n_rows && q1 < nq && d1 <= t;
+      const bool h2 = r1 < n_rows && q0 < nq && d2 <= t;
+      const bool h3 = r1 < n_rows && q1 < nq && d3 <= t;
+      if (__any_sync(0xffffffffu, h0 | h1 | h2 | h3)) {
+        emit_hits_ballot(h0, r0, q_base + q0, d0, hits, cap, count);
+        emit_hits_ballot(h1, r0, q_base + q1, d1, hits, cap, count);
+        emit_hits_ballot(h2, r1, q_base + q0, d2, hits, cap, count);
+        emit_hits_ballot(h3, r1, q_base + q1, d3, hits, cap, count);
+      }
+    }
+  }
+}
+
+cudaError_t scan_init() {
+  const int smem = static_cast<int>(kMaxSmemQueries * 32);
+  cudaError_t e = cudaFuncSetAttribute(scan_simt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(scan_b1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(p.count, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess || p.n_rows == 0 || p.n_queries == 0) return e;
+  if (algo == YPDQ_SCAN_AUTO) algo = YPDQ_SCAN_SIMT;
+  for (uint32_t q0 = 0; q0 < p.n_queries; q0 += kMaxSmemQueries) {
+    const uint32_t nq = (p.n_queries - q0) < kMaxSmemQueries ? (p.n_queries - q0) : kMaxSmemQueries;
+    const uint8_t* qptr = p.queries + static_cast<size_t>(q0) * 32;
+    if (algo == YPDQ_SCAN_B1MMA) {
+      const uint64_t tiles = (p.n_rows + 15) / 16;
+      uint64_t blocks = (tiles + (kScanThreads / 32) - 1) / (kScanThreads / 32);
+      const uint64_t cap_blocks = static_cast<uint64_t>(num_sms) * 8;
+      if (blocks > cap_blocks) blocks = cap_blocks;
+      const size_t smem = static_cast<size_t>((nq + 7) / 8) * 32 * sizeof(uint2);
+      scan_b1_kernel<<<static_cast<unsigned>(blocks), kScanThreads, smem, s>>>(
+          reinterpret_cast<const uint2*>(p.rows), p.n_rows, reinterpret_cast<const uint2*>(qptr),
+          nq, q0, p.threshold, p.hits, p.capacity, p.count);
+    } else {
+      uint64_t blocks = (p.n_rows + kScanThreads - 1) / kScanThreads;
+      const uint64_t cap_blocks = static_cast<uint64_t>(num_sms) * 8;
+      if (blocks > cap_blocks) blocks = cap_blocks;
+      const size_t smem = static_cast<size_t>(nq) * 32;
+      scan_simt_kernel<<<static_cast<unsigned>(blocks), kScanThreads, smem, s>>>(
+          reinterpret_cast<const uint4*>(p.rows), p.n_rows, reinterpret_cast<const uint4*>(qptr),
+          nq, q0, p.threshold, p.hits, p.capacity, p.count);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------- hit sorting
+
+// Order by (index, query): the scalar matcher's visit order.
+__device__ __forceinline__ bool hit_less(const ypdq_hit& a, const ypdq_hit& b) {
+  return a.index < b.index || (a.index == b.index && a.query < b.query);
+}
+
+// One compare-exchange step of a bitonic sort in the "flip" form: every comparison puts
+// the smaller hit at the lower index, so the virtual +infinity padding past n (up to the
+// next power of two) never has to move and is never stored.
+__global__ void bitonic_step_kernel(ypdq_hit* h, uint64_t n, uint64_t k, uint64_t j, int flip) {
+  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t l;
+  if (flip) {
+    if (i & (k >> 1)) return;
+    l = i ^ (k - 1);
+  } else {
+    if (i & j) return;
+    l = i ^ j;
+  }
+  if (l >= n) return;  // partner is padding: the real element is already the smaller
+  const ypdq_hit a = h[i], b = h[l];
+  if (hit_less(b, a)) {
+    h[i] = b;
+    h[l] = a;
+  }
+}
+
+cudaError_t launch_sort_hits(ypdq_hit* hits, uint64_t n, cudaStream_t s) {
+  if (n < 2) return cudaSuccess;
+  uint64_t padded = 1;
+  while (padded < n) padded <<= 1;
+  const unsigned threads = 256;
+  const unsigned blocks = static_cast<unsigned>((n + threads - 1) / threads);
+  for (uint64_t k = 2; k <= padded; k <<= 1) {
+    bitonic_step_kernel<<<blocks, threads, 0, s>>>(hits, n, k, k >> 1, 1);
+    for (uint64_t j = k >> 2; j > 0; j >>= 1)
+      bitonic_step_kernel<<<blocks, threads, 0, s>>>(hits, n, k, j, 0);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace ypdq

@@ -1,0 +1,153 @@
+// Internal declarations shared by the CUDA translation units of libyumepdq_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ypdq.h"
+
+namespace ypdq {
+
+// Device-side error bits, OR-ed into the context's error word by a kernel that gives up.
+constexpr int kDevErrTimeout = 1;
+
+// Longest time a device-side wait spins before the kernel reports a timeout and returns.
+constexpr uint64_t kWaitLimitNs = 4ull * 1000 * 1000 * 1000;
+
+// ----------------------------------------------------------------- PTX helpers
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for the phase with the given parity. Gives up (returns false) when *abort_flag is
+// set by another warp or when kWaitLimitNs passes; the caller then raises the error.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          const volatile int* abort_flag) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+  }
+}
+
+// 1-D bulk copy global -> shared, completing `bytes` transactions on `bar`.
+// Both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gsrc, uint32_t bytes,
+                                         uint64_t* bar, uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
+      "[%0], [%1], %2, [%3], %4;" ::"r"(smem_u32(smem_dst)),
+      "l"(gsrc), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+__device__ __forceinline__ void named_bar_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ------------------------------------------------------------- launch plumbing
+
+struct HashLaunch {
+  const void* images;
+  int64_t n;
+  int input_u8;
+  uint32_t row_mask, col_mask;
+  uint8_t* hashes;
+  float* quality;
+  float* thresholds;
+  float* pdqf;
+  int pdqf_slots;
+  float* buf1;
+  int* dev_err;
+};
+
+struct DihedralLaunch {
+  const float* pdqf;
+  const float* thr_in;
+  int64_t n;
+  uint32_t row_mask, col_mask;
+  uint8_t* hashes;
+  float* quality;
+  float* thresholds;
+  float* pdqf_out;
+};
+
+struct ScanLaunch {
+  const uint8_t* rows;
+  uint64_t n_rows;
+  const uint8_t* queries;
+  uint32_t n_queries;
+  uint32_t threshold;
+  ypdq_hit* hits;
+  uint64_t capacity;
+  unsigned long long* count;
+};
+
+// hash.cu
+cudaError_t upload_constants();
+cudaError_t hash_occupancy(int input_u8, int* ctas_per_sm);
+cudaError_t launch_hash(const HashLaunch& p, int num_sms, int ctas_per_sm, cudaStream_t s);
+cudaError_t launch_dihedrals(const DihedralLaunch& p, cudaStream_t s);
+
+// scan.cu
+cudaError_t scan_init();
+cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t s);
+cudaError_t launch_sort_hits(ypdq_hit* hits, uint64_t n, cudaStream_t s);
+
+// synth.cu
+cudaError_t launch_synth_rows(uint8_t* rows, uint64_t n, uint64_t first, uint64_t seed,
+                              cudaStream_t s);
+
+}  // namespace ypdq
