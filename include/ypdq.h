@@ -95,7 +95,8 @@ typedef struct {
 typedef enum {
   YPDQ_SCAN_AUTO = 0,   /* pick by query count */
   YPDQ_SCAN_SIMT = 1,   /* XOR + popcount, one row per thread */
-  YPDQ_SCAN_B1MMA = 2   /* binary tensor-core MMA with XOR + popcount */
+  YPDQ_SCAN_B1MMA = 2,  /* legacy binary MMA (mma.sync .b1 .xor.popc) */
+  YPDQ_SCAN_TC = 3      /* tcgen05 FP8 tensor cores on +-1 vectors: dot = 256 - 2 d */
 } ypdq_scan_algo;
 
 /* ------------------------------------------------------------------ context */

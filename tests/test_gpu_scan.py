@@ -10,7 +10,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-ALGOS = [1, 2]  # YPDQ_SCAN_SIMT, YPDQ_SCAN_B1MMA
+ALGOS = [1, 2, 3]  # YPDQ_SCAN_SIMT, YPDQ_SCAN_B1MMA, YPDQ_SCAN_TC
 
 
 def as_tuples(h):

@@ -24,7 +24,7 @@ INPUT_F32, INPUT_U8 = 0, 1
 DCT_FP32, DCT_TF32, DCT_BF16X3 = 0, 1, 2
 DIHEDRAL_EXACT, DIHEDRAL_AVX2, DIHEDRAL_SCALAR = 0, 1, 2
 SEMANTICS = {"exact": DIHEDRAL_EXACT, "avx2": DIHEDRAL_AVX2, "scalar": DIHEDRAL_SCALAR}
-SCAN_AUTO, SCAN_SIMT, SCAN_B1MMA = 0, 1, 2
+SCAN_AUTO, SCAN_SIMT, SCAN_B1MMA, SCAN_TC = 0, 1, 2, 3
 H2D, D2H, D2D = 0, 1, 2
 
 

@@ -146,13 +146,16 @@ cudaError_t scan_init() {
   const int smem = static_cast<int>(kMaxSmemQueries * 32);
   cudaError_t e = cudaFuncSetAttribute(scan_simt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(scan_b1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  e = cudaFuncSetAttribute(scan_b1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return scan_tc_init();
 }
 
 cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(p.count, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess || p.n_rows == 0 || p.n_queries == 0) return e;
-  if (algo == YPDQ_SCAN_AUTO) algo = YPDQ_SCAN_SIMT;
+  if (algo == YPDQ_SCAN_AUTO) algo = p.n_queries <= 2 ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;
+  if (algo == YPDQ_SCAN_TC) return launch_scan_tc(p, num_sms, s);
   for (uint32_t q0 = 0; q0 < p.n_queries; q0 += kMaxSmemQueries) {
     const uint32_t nq = (p.n_queries - q0) < kMaxSmemQueries ? (p.n_queries - q0) : kMaxSmemQueries;
     const uint8_t* qptr = p.queries + static_cast<size_t>(q0) * 32;

@@ -1,0 +1,442 @@
+// Exact Hamming scan on the 5th-generation tensor cores (tcgen05, kind::f8f6f4).
+//
+// Each bit b of a 256-bit hash becomes the FP8 (e4m3) value s = 1 - 2b, i.e. +1.0 or -1.0.
+// For a database row r and a query q the dot product of the two sign vectors is
+//     sum_k s_r[k] s_q[k] = 256 - 2 * popcount(r ^ q),
+// an integer in [-256, 256]. Every product is exactly +-1 and every partial sum an integer
+// of magnitude <= 256, so the f32 accumulator holds it exactly and
+//     distance = (256 - dot) / 2,    hit  <=>  dot >= 256 - 2 * threshold.
+// The hit set equals the scalar matcher's (CpuMatcher::find, src/matching/mod.rs:336-362).
+//
+// CTA (one per SM, persistent over 128-row database tiles; 10 warps):
+//   warps 0-3  epilogue: tcgen05.ld the 128 x N accumulator (warp w reads TMEM lanes
+//              32w..32w+31 = tile rows), compare against the threshold, compact hits.
+//   warp 4     producer: one lane bulk-copies packed tiles (128 rows x 32 B) into a ring.
+//   warp 5     MMA: allocates TMEM; one lane issues 8 x tcgen05.mma (M=128, N, K=32) per
+//              tile into a double-buffered accumulator and commits to mbarriers.
+//   warps 6-9  expanders: packed bits -> FP8 +-1 in the 128B-swizzled K-major layout that
+//              the MMA descriptors describe (database tiles, and the queries once per pass).
+// Queries are processed in passes of N <= 256; the database streams once per pass.
+#include "ypdq_internal.cuh"
+
+namespace ypdq {
+
+namespace tc {
+
+constexpr int kThreads = 320;
+constexpr int kEpilogueWarps = 4;  // warps 0..3
+constexpr int kProducerWarp = 4;
+constexpr int kMmaWarp = 5;
+constexpr int kExpandWarp0 = 6;    // warps 6..9
+constexpr int kTileRows = 128;
+constexpr int kMaxN = 256;
+constexpr int kPackStages = 8;
+constexpr int kAStages = 2;
+constexpr int kAccStages = 2;
+constexpr int kChunkBytes = kTileRows * 128;  // one 128-byte K-chunk of a 128-row tile
+
+struct Smem {
+  uint8_t a[kAStages][2][kChunkBytes];    // expanded tiles: 2 K-chunks of 128 rows x 128 B
+  uint8_t b[2][kMaxN * 128];              // expanded queries: 2 K-chunks of N rows x 128 B
+  uint8_t packed[kPackStages][kTileRows * 32];
+  uint64_t pk_full[kPackStages], pk_empty[kPackStages];
+  uint64_t a_full[kAStages], a_empty[kAStages];
+  uint64_t acc_full[kAccStages], acc_empty[kAccStages];
+  uint64_t b_full, b_empty, epi_exit, mma_done;
+  uint32_t tmem_base;
+  int abort_flag;
+};
+constexpr size_t kSmemBytes = sizeof(Smem) + 1024;  // + slack to align the base to 1024 B
+
+// ---- tcgen05 wrappers
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                       uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4) |
+         (static_cast<uint64_t>(1) << 16) |              // leading byte offset (unused here)
+         (static_cast<uint64_t>(1024 >> 4) << 32) |      // stride byte offset
+         (static_cast<uint64_t>(1) << 46) |              // descriptor version (tcgen05)
+         (static_cast<uint64_t>(2) << 61);               // swizzle: 128 B
+}
+
+// Instruction descriptor: D f32, A and B e4m3, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_f8(uint32_t n) {
+  return (1u << 4) | (0u << 7) | (0u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+// 4 bits -> 4 e4m3 bytes: bit 0 -> 0x38 (+1.0), bit 1 -> 0xB8 (-1.0).
+__device__ __forceinline__ uint32_t expand4(uint32_t nib) {
+  return 0x38383838u | (((nib * 0x00204081u) & 0x01010101u) << 7);
+}
+
+// Expand one 32-byte row into the swizzled K-major layout: element k (bit k%8 of byte k/8)
+// goes to K-chunk k/128, 16-byte unit ((k%128)/16) XOR (row%8), byte k%16 within it.
+__device__ __forceinline__ void expand_row(const uint4 w0, const uint4 w1, uint8_t* chunk0,
+                                           uint8_t* chunk1, int row) {
+  const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+  const int sw = row & 7;
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    uint8_t* base = (c == 0 ? chunk0 : chunk1) + row * 128;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      // 16 bits = elements 128c + 16u .. +15 = bits 16u..16u+15 of words 4c..4c+3
+      const uint32_t word = words[4 * c + (u >> 1)];
+      const uint32_t bits = (word >> (16 * (u & 1))) & 0xFFFFu;
+      uint4 out;
+      out.x = expand4(bits & 15u);
+      out.y = expand4((bits >> 4) & 15u);
+      out.z = expand4((bits >> 8) & 15u);
+      out.w = expand4((bits >> 12) & 15u);
+      *reinterpret_cast<uint4*>(base + ((u ^ sw) << 4)) = out;
+    }
+  }
+}
+
+struct Params {
+  const uint8_t* rows;
+  uint64_t n_rows;
+  const uint8_t* queries;
+  uint32_t n_queries;
+  uint32_t n_tile;       // N: queries per pass (multiple of 32, <= 256)
+  uint32_t threshold;
+  ypdq_hit* hits;
+  uint64_t capacity;
+  unsigned long long* count;
+  int* dev_err;
+};
+
+__device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
+  *reinterpret_cast<volatile int*>(&sm.abort_flag) = 1;
+  atomicOr(dev_err, kDevErrTimeout);
+}
+
+__global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) {
+  extern __shared__ uint8_t smem_raw[];
+  Smem& sm = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                      ~static_cast<uintptr_t>(1023));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t N = prm.n_tile;
+  const uint64_t n_tiles = (prm.n_rows + kTileRows - 1) / kTileRows;
+  const uint32_t n_passes = (prm.n_queries + N - 1) / N;
+  // tiles of this CTA: blockIdx.x, blockIdx.x + gridDim.x, ...
+  const uint64_t my_tiles =
+      blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  volatile int* abort_flag = &sm.abort_flag;
+
+  if (tid == 0) {
+    for (int s = 0; s < kPackStages; ++s) {
+      mbar_init(&sm.pk_full[s], 1);
+      mbar_init(&sm.pk_empty[s], 4);
+    }
+    for (int s = 0; s < kAStages; ++s) {
+      mbar_init(&sm.a_full[s], 4);
+      mbar_init(&sm.a_empty[s], 1);
+    }
+    for (int s = 0; s < kAccStages; ++s) {
+      mbar_init(&sm.acc_full[s], 1);
+      mbar_init(&sm.acc_empty[s], kEpilogueWarps);
+    }
+    mbar_init(&sm.b_full, 4);
+    mbar_init(&sm.b_empty, 1);
+    mbar_init(&sm.epi_exit, kEpilogueWarps);
+    mbar_init(&sm.mma_done, 1);
+    sm.abort_flag = 0;
+    fence_mbar_init();
+  }
+  const uint32_t tmem_cols = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : (2 * N <= 256 ? 256 : 512)));
+  if (warp == kMmaWarp) {
+    tmem_alloc(&sm.tmem_base, tmem_cols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = sm.tmem_base;
+  if (my_tiles == 0) {
+    if (warp == kMmaWarp) tmem_dealloc(tmem_base, tmem_cols);
+    return;
+  }
+
+  if (warp == kProducerWarp) {
+    if (lane == 0) {
+      uint32_t g = 0;
+      bool ok = true;
+      for (uint32_t p = 0; p < n_passes && ok; ++p) {
+        for (uint64_t k = 0; k < my_tiles; ++k, ++g) {
+          const uint64_t tile = blockIdx.x + k * gridDim.x;
+          const uint32_t slot = g % kPackStages;
+          if (!mbar_wait(&sm.pk_empty[slot], ((g / kPackStages) & 1u) ^ 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          const uint64_t r0 = tile * kTileRows;
+          const uint64_t nr = (prm.n_rows - r0) < kTileRows ? (prm.n_rows - r0) : kTileRows;
+          const uint32_t bytes = static_cast<uint32_t>(nr * 32);
+          mbar_arrive_expect_tx(&sm.pk_full[slot], bytes);
+          bulk_g2s(sm.packed[slot], prm.rows + r0 * 32, bytes, &sm.pk_full[slot],
+                   policy_evict_first());
+        }
+      }
+      if (!ok) {
+        raise_abort(sm, prm.dev_err);
+        for (uint32_t k = 1; k <= kPackStages && k <= g; ++k) {
+          const uint32_t gi = g - k;
+          const uint64_t t0 = globaltimer_ns();
+          while (!mbar_try_wait(&sm.pk_full[gi % kPackStages], (gi / kPackStages) & 1u))
+            if (globaltimer_ns() - t0 > kWaitLimitNs / 4) break;
+        }
+      }
+    }
+    return;
+  }
+
+  if (warp >= kExpandWarp0) {
+    const int e = tid - kExpandWarp0 * 32;  // 0..127: tile row / query row
+    uint32_t g = 0, ga = 0;
+    for (uint32_t p = 0; p < n_passes; ++p) {
+      // queries of this pass into B (N rows; padding rows are zero = contributes nothing)
+      if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag)) goto fail;
+      for (uint32_t qr = e; qr < N; qr += 128) {
+        const uint64_t qi = static_cast<uint64_t>(p) * N + qr;
+        uint8_t* c0 = sm.b[0];
+        uint8_t* c1 = sm.b[1];
+        if (qi < prm.n_queries) {
+          const uint4* src = reinterpret_cast<const uint4*>(prm.queries + qi * 32);
+          expand_row(src[0], src[1], c0, c1, static_cast<int>(qr));
+        } else {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            *reinterpret_cast<uint4*>(c0 + qr * 128 + u * 16) = make_uint4(0, 0, 0, 0);
+            *reinterpret_cast<uint4*>(c1 + qr * 128 + u * 16) = make_uint4(0, 0, 0, 0);
+          }
+        }
+      }
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.b_full);
+
+      for (uint64_t k = 0; k < my_tiles; ++k, ++g, ++ga) {
+        const uint32_t slot = g % kPackStages;
+        const uint32_t as = ga % kAStages;
+        if (!mbar_wait(&sm.pk_full[slot], (g / kPackStages) & 1u, abort_flag)) goto fail;
+        const uint4* src = reinterpret_cast<const uint4*>(sm.packed[slot] + e * 32);
+        const uint4 w0 = src[0], w1 = src[1];
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.pk_empty[slot]);
+        if (!mbar_wait(&sm.a_empty[as], ((ga / kAStages) & 1u) ^ 1u, abort_flag)) goto fail;
+        expand_row(w0, w1, sm.a[as][0], sm.a[as][1], e);
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.a_full[as]);
+      }
+    }
+    return;
+  fail:
+    if (lane == 0) raise_abort(sm, prm.dev_err);
+    return;
+  }
+
+  if (warp == kMmaWarp) {
+    const uint32_t idesc = idesc_f8(N);
+    uint32_t ga = 0;
+    bool ok = true;
+    if (lane == 0) {
+      for (uint32_t p = 0; p < n_passes && ok; ++p) {
+        if (!mbar_wait(&sm.b_full, p & 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t b0 = smem_u32(sm.b[0]), b1 = smem_u32(sm.b[1]);
+        for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
+          const uint32_t as = ga % kAStages, ac = ga % kAccStages;
+          if (!mbar_wait(&sm.a_full[as], (ga / kAStages) & 1u, abort_flag) ||
+              !mbar_wait(&sm.acc_empty[ac], ((ga / kAccStages) & 1u) ^ 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(sm.a[as][0]), a1 = smem_u32(sm.a[as][1]);
+          const uint32_t d = tmem_base + ac * N;
+#pragma unroll
+          for (int ks = 0; ks < 8; ++ks) {
+            const uint32_t off = (ks & 3) * 32;
+            const uint64_t ad = sw128_desc((ks < 4 ? a0 : a1) + off);
+            const uint64_t bd = sw128_desc((ks < 4 ? b0 : b1) + off);
+            mma_f8(d, ad, bd, idesc, ks > 0 ? 1u : 0u);
+          }
+          mma_commit(&sm.a_empty[as]);
+          mma_commit(&sm.acc_full[ac]);
+        }
+        if (ok) mma_commit(&sm.b_empty);
+      }
+      if (!ok) raise_abort(sm, prm.dev_err);
+      // every MMA issued so far has completed once this commit arrives
+      mma_commit(&sm.mma_done);
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.mma_done, 0))
+        if (globaltimer_ns() - t0 > kWaitLimitNs) break;
+    }
+    __syncwarp();
+    // the epilogue warps arrive on epi_exit when they stop reading TMEM
+    {
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.epi_exit, 0))
+        if (globaltimer_ns() - t0 > kWaitLimitNs) break;
+    }
+    tc_fence_after();
+    tmem_dealloc(tmem_base, tmem_cols);
+    return;
+  }
+
+  // ---- epilogue warps 0..3: thread row = warp*32 + lane of the tile
+  {
+    const float dot_min = 256.0f - 2.0f * static_cast<float>(prm.threshold);
+    const uint32_t lane_addr = static_cast<uint32_t>(warp * 32) << 16;
+    uint32_t ga = 0;
+    bool ok = true;
+    for (uint32_t p = 0; p < n_passes && ok; ++p) {
+      const uint64_t q0 = static_cast<uint64_t>(p) * N;
+      for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
+        const uint64_t tile = blockIdx.x + k * gridDim.x;
+        const uint32_t ac = ga % kAccStages;
+        if (!mbar_wait(&sm.acc_full[ac], (ga / kAccStages) & 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint64_t row = tile * kTileRows + warp * 32 + lane;
+        const bool row_ok = row < prm.n_rows;
+        for (uint32_t c0 = 0; c0 < N; c0 += 32) {
+          float v[32];
+          tmem_ld32(tmem_base + lane_addr + ac * N + c0, v);
+          float m = v[0];
+#pragma unroll
+          for (int i = 1; i < 32; ++i) m = fmaxf(m, v[i]);
+          if (__any_sync(0xffffffffu, row_ok && m >= dot_min)) {
+#pragma unroll 1
+            for (int i = 0; i < 32; ++i) {
+              const uint64_t q = q0 + c0 + i;
+              float vi = v[0];
+#pragma unroll
+              for (int j = 1; j < 32; ++j)
+                if (i == j) vi = v[j];
+              const bool hit = row_ok && q < prm.n_queries && vi >= dot_min;
+              const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
+              if (ballot) {
+                const int leader = __ffs(ballot) - 1;
+                unsigned long long base = 0;
+                if (lane == leader)
+                  base = atomicAdd(prm.count, static_cast<unsigned long long>(__popc(ballot)));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (hit) {
+                  const uint64_t pos = base + __popc(ballot & lanemask_lt());
+                  if (pos < prm.capacity) {
+                    ypdq_hit h;
+                    h.index = row;
+                    h.query = static_cast<uint32_t>(q);
+                    h.distance = static_cast<uint32_t>((256.0f - vi) * 0.5f);
+                    prm.hits[pos] = h;
+                  }
+                }
+              }
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+      }
+    }
+    if (!ok && lane == 0) raise_abort(sm, prm.dev_err);
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.epi_exit);
+  }
+}
+
+}  // namespace tc
+
+cudaError_t scan_tc_init() {
+  return cudaFuncSetAttribute(tc::scan_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(tc::kSmemBytes));
+}
+
+cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
+  tc::Params prm{};
+  prm.rows = p.rows;
+  prm.n_rows = p.n_rows;
+  prm.queries = p.queries;
+  prm.n_queries = p.n_queries;
+  // N is a multiple of 32 so every 32-column TMEM load stays inside one accumulator.
+  uint32_t n = (p.n_queries + 31u) & ~31u;
+  prm.n_tile = n > static_cast<uint32_t>(tc::kMaxN) ? static_cast<uint32_t>(tc::kMaxN) : n;
+  prm.threshold = p.threshold;
+  prm.hits = p.hits;
+  prm.capacity = p.capacity;
+  prm.count = p.count;
+  prm.dev_err = p.dev_err;
+  const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
+  const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
+  tc::scan_tc_kernel<<<static_cast<unsigned>(grid), tc::kThreads, tc::kSmemBytes, s>>>(prm);
+  return cudaGetLastError();
+}
+
+}  // namespace ypdq

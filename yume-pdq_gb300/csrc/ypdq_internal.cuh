@@ -133,6 +133,7 @@ struct ScanLaunch {
   ypdq_hit* hits;
   uint64_t capacity;
   unsigned long long* count;
+  int* dev_err;
 };
 
 // hash.cu
@@ -145,6 +146,10 @@ cudaError_t launch_dihedrals(const DihedralLaunch& p, cudaStream_t s);
 cudaError_t scan_init();
 cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t s);
 cudaError_t launch_sort_hits(ypdq_hit* hits, uint64_t n, cudaStream_t s);
+
+// scan_tc.cu
+cudaError_t scan_tc_init();
+cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s);
 
 // synth.cu
 cudaError_t launch_synth_rows(uint8_t* rows, uint64_t n, uint64_t first, uint64_t seed,
