@@ -204,6 +204,27 @@ ypdq_status ypdq_event_destroy(ypdq_ctx *ctx, ypdq_event_t ev);
 ypdq_status ypdq_event_record(ypdq_ctx *ctx, ypdq_event_t ev, ypdq_stream_t stream);
 ypdq_status ypdq_event_elapsed_ms(ypdq_ctx *ctx, ypdq_event_t start, ypdq_event_t end, float *ms);
 
+/* ------------------------------------------------- screening without allocation */
+
+/*
+ * Screen n device-resident images against device-resident rows without allocating.
+ * This entry point has no counterpart in the reference. It is for callers that cannot call
+ * cudaMalloc, such as code inside a framework that owns all device memory through its own
+ * pool, or a latency-critical path where an allocation (which can synchronise the device)
+ * is not allowed. It hashes the images (FP32, bit-exact), derives the 8 dihedrals, and
+ * scans the 8n hashes (queries numbered image * 8 + slot) at `threshold`. Hits are
+ * unsorted; *d_count gets the total, or UINT64_MAX if a device-side wait timed out.
+ * The 8n hashes live in a fixed 1 MiB device array inside the library, so n is at most
+ * 4096 (larger n returns YPDQ_ERR_INVALID) and every GPU that loads the library holds
+ * that array until exit. All calls share the array: calls that overlap on the GPU race,
+ * so order them. The first call on a device sets it up there (symbol address, DCT table,
+ * kernel attributes); make that call before any stream capture. Asynchronous on stream.
+ */
+ypdq_status ypdq_screen_noalloc(const void *d_images, int64_t n, int input_kind, int semantics,
+                                const uint8_t *d_rows, uint64_t n_rows, uint32_t threshold,
+                                ypdq_hit *d_hits, uint64_t capacity, uint64_t *d_count,
+                                ypdq_stream_t stream);
+
 /* -------------------------------------------------------- synthetic workloads */
 
 /*

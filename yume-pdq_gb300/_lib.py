@@ -69,6 +69,7 @@ SIGNATURES = {
     "ypdq_event_elapsed_ms": (i32, [P, P, P, ctypes.POINTER(ctypes.c_float)]),
     "ypdq_synth_rows": (i32, [P, P, u64, u64, u64, P]),
     "ypdq_constants": (i32, [P, P]),
+    "ypdq_screen_noalloc": (i32, [P, i64, i32, i32, P, u64, u32, P, u64, P, P]),
     "yume_pdq_hash_smart_kernel": (f32, [P, P, P, P, P, P]),
     "yume_pdq_visit_dihedrals_smart_kernel": (ctypes.c_bool, [P, f32, P, P, P]),
 }

@@ -111,6 +111,10 @@ ypdq_status read_device_errors(ypdq_ctx* ctx) {
 
 }  // namespace
 
+namespace ypdq {
+void set_last_error_text(const char* text) { g_last_error = text; }
+}  // namespace ypdq
+
 extern "C" {
 
 // ----------------------------------------------------------------- context
