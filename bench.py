@@ -110,11 +110,19 @@ class ClockSampler:
 
 
 def measured_peaks():
+    """(HBM GB/s, dense bf16 TFLOP/s burst, source) from MEASURED_PEAKS.json, else fallback."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         d = json.load(open(path))
-        return d["hbm_gbs"], "measured"
-    return 6800.0, "fallback"
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def scan_algo_used(algo, nq):
+    """The algorithm ypdq_scan runs for YPDQ_SCAN_AUTO (mirrors launch_scan's choice)."""
+    if algo == 0:
+        return 1 if nq <= 2 else 3
+    return algo
 
 
 def setup_workload(yp, ctx, args, rank):
@@ -227,23 +235,40 @@ def run_ours(args):
     e2e_value = world * B / e2e_s
     ctx.lib.ypdq_free_host(ctx.handle, h_img)
 
-    peak, peak_kind = measured_peaks()
+    hbm_peak, bf16_peak, peak_kind = measured_peaks()
     hash_avg = statistics.mean(hash_ms)
     scan_avg = statistics.mean(scan_ms)
-    scan_launches = (nq + 2047) // 2048
-    if scan_avg >= hash_avg:
-        # one launch scans the whole database once for up to 2048 queries
-        dom_name = "scan"
-        dom_launches = scan_launches
-        alg_bytes = n * 32 + (hits_per_step / scan_launches) * 16
+    algo = scan_algo_used(args.algo, nq)
+    scan_launches = 1 if algo == 3 else (nq + 2047) // 2048
+    if scan_avg >= hash_avg and algo == 3:
+        # tensor-core scan: 2 * 256 FP8 flops per (row, query) pair, one launch per step;
+        # FP8 dense peak taken as 2x the measured bf16 dense burst (the nominal 4.5 : 2.25 ratio)
+        flops = 2.0 * 256 * nq * n
+        achieved = flops / (scan_avg / 1000.0) / 1e12
+        roofline = {"bound": "tensor", "kernel": "scan_tc_kernel (tcgen05 kind::f8f6f4)",
+                    "achieved": achieved, "peak": 2 * bf16_peak, "unit": "TFLOP/s",
+                    "frac": achieved / (2 * bf16_peak), "traffic": None,
+                    "peak_source": "%s bf16 burst x 2 (fp8 dense)" % peak_kind,
+                    "launch_ms": scan_avg, "launches_per_step": 1,
+                    "db_stream_gbs": (n * 32 * ((nq + 255) // 256)) / (scan_avg / 1e3) / 1e9}
+    elif scan_avg >= hash_avg:
+        # SIMT scan: one launch reads the whole database once for up to 2048 queries
         dom_ms = scan_avg / scan_launches
+        alg_bytes = n * 32 + (hits_per_step / scan_launches) * 16
+        achieved = alg_bytes / (dom_ms / 1000.0) / 1e9
+        roofline = {"bound": "hbm", "kernel": "scan_simt_kernel", "achieved": achieved,
+                    "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                    "traffic": None, "peak_source": peak_kind, "launch_ms": dom_ms,
+                    "launches_per_step": scan_launches}
     else:
-        # one launch reads every image once and writes 8 hashes + 8 qualities per image
-        dom_name = "hash"
-        dom_launches = 1
+        # hash kernel: reads every image once, writes 8 hashes + 8 qualities per image
         alg_bytes = B * (512 * 512 * 4) + B * (8 * 32 + 8 * 4)
-        dom_ms = hash_avg
-    achieved = alg_bytes / (dom_ms / 1000.0) / 1e9
+        achieved = alg_bytes / (hash_avg / 1000.0) / 1e9
+        roofline = {"bound": "hbm", "kernel": "hash_kernel<float>", "achieved": achieved,
+                    "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                    "traffic": None, "peak_source": peak_kind, "launch_ms": hash_avg,
+                    "launches_per_step": 1}
+    hash_gbs = (B * (512 * 512 * 4 + 288)) / (hash_avg / 1000.0) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
@@ -255,16 +280,14 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (images %d MiB, DB %d MiB > 129 MB L2)"
                          % (B * 4 * 512 * 512 >> 20, n * 32 >> 20),
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "scan_algo": args.algo},
+                   "scan_algo": {1: "simt", 2: "b1mma", 3: "tcgen05_fp8"}[algo]},
         "kernels_ms": {"hash": hash_avg, "scan": scan_avg},
         "latency_ms": {"p50": 1000 * statistics.median(lat),
                        "p99": 1000 * float(np.percentile(lat, 99))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": B * 512 * 512 * 4,
                 "d2h_bytes_per_step": hits_per_step * 16 + 8},
-        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                     "peak_source": peak_kind, "launch_ms": dom_ms,
-                     "launches_per_step": dom_launches},
+        "roofline": roofline,
+        "hash_kernel": {"ms": hash_avg, "GB/s": hash_gbs, "frac_hbm": hash_gbs / hbm_peak},
         "gpu_launches": args.steps * (1 + scan_launches),
         "clocks": clk,
     }

@@ -154,7 +154,8 @@ cudaError_t scan_init() {
 cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(p.count, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess || p.n_rows == 0 || p.n_queries == 0) return e;
-  if (algo == YPDQ_SCAN_AUTO) algo = p.n_queries <= 2 ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;
+  // SIMT is HBM-bound up to a few queries and beats the tensor-core pipeline up to ~16.
+  if (algo == YPDQ_SCAN_AUTO) algo = p.n_queries <= 16 ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;
   if (algo == YPDQ_SCAN_TC) return launch_scan_tc(p, num_sms, s);
   for (uint32_t q0 = 0; q0 < p.n_queries; q0 += kMaxSmemQueries) {
     const uint32_t nq = (p.n_queries - q0) < kMaxSmemQueries ? (p.n_queries - q0) : kMaxSmemQueries;

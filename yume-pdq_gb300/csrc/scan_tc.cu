@@ -4,49 +4,57 @@
 // For a database row r and a query q the dot product of the two sign vectors is
 //     sum_k s_r[k] s_q[k] = 256 - 2 * popcount(r ^ q),
 // an integer in [-256, 256]. Every product is exactly +-1 and every partial sum an integer
-// of magnitude <= 256, so the f32 accumulator holds it exactly and
+// of magnitude <= 256, so even an f16 accumulator (11-bit significand) holds it exactly and
 //     distance = (256 - dot) / 2,    hit  <=>  dot >= 256 - 2 * threshold.
 // The hit set equals the scalar matcher's (CpuMatcher::find, src/matching/mod.rs:336-362).
 //
-// CTA (one per SM, persistent over 128-row database tiles; 10 warps):
-//   warps 0-3  epilogue: tcgen05.ld the 128 x N accumulator (warp w reads TMEM lanes
-//              32w..32w+31 = tile rows), compare against the threshold, compact hits.
-//   warp 4     producer: one lane bulk-copies packed tiles (128 rows x 32 B) into a ring.
-//   warp 5     MMA: allocates TMEM; one lane issues 8 x tcgen05.mma (M=128, N, K=32) per
-//              tile into a double-buffered accumulator and commits to mbarriers.
-//   warps 6-9  expanders: packed bits -> FP8 +-1 in the 128B-swizzled K-major layout that
-//              the MMA descriptors describe (database tiles, and the queries once per pass).
-// Queries are processed in passes of N <= 256; the database streams once per pass.
+// CTA (one per SM, persistent over 128-row database tiles; 14 warps):
+//   warps 0-7   epilogue: tcgen05.ld the 128 x N f16 accumulator, two warps per TMEM lane
+//               quarter (warp w reads lanes 32(w%4).. = tile rows, alternate 64-column
+//               chunks), half2 max against the threshold, compact hits. Reading the
+//               accumulator out of TMEM is the scan's limit (one f16 per (row, query) pair
+//               against 256 MACs), so it gets twice the warps of the other roles.
+//   warp 8      producer: one lane bulk-copies packed tiles (128 rows x 32 B) into a ring.
+//   warp 9      MMA: allocates TMEM; one lane issues 8 x tcgen05.mma (M=128, N, K=32) per
+//               tile into a double-buffered accumulator and commits to mbarriers.
+//   warps 10-13 expanders: packed bits -> FP8 +-1 in the 128B-swizzled K-major layout that
+//               the MMA descriptors describe (database tiles, and the queries once per pass).
+// Queries are processed in passes of N <= 256; the database streams once per pass. The
+// shared memory left after the operands holds as many packed tiles in flight as fit.
+#include <cuda_fp16.h>
+
 #include "ypdq_internal.cuh"
 
 namespace ypdq {
 
 namespace tc {
 
-constexpr int kThreads = 320;
-constexpr int kEpilogueWarps = 4;  // warps 0..3
-constexpr int kProducerWarp = 4;
-constexpr int kMmaWarp = 5;
-constexpr int kExpandWarp0 = 6;    // warps 6..9
+constexpr int kEpilogueWarps = 8;  // warps 0..7
+constexpr int kProducerWarp = 8;
+constexpr int kMmaWarp = 9;
+constexpr int kExpandWarp0 = 10;   // warps 10..13
+constexpr int kThreads = 14 * 32;
 constexpr int kTileRows = 128;
 constexpr int kMaxN = 256;
-constexpr int kPackStages = 8;
-constexpr int kAStages = 2;
+constexpr int kMaxPackStages = 16;
+constexpr int kAStages = 4;
 constexpr int kAccStages = 2;
 constexpr int kChunkBytes = kTileRows * 128;  // one 128-byte K-chunk of a 128-row tile
+constexpr int kPackBytes = kTileRows * 32;
+constexpr size_t kSmemLimit = 227 * 1024;
 
+// Fixed part of shared memory; the expanded queries (2 K-chunks of N x 128 B) and the
+// packed ring follow it at 1024-byte aligned offsets computed per launch.
 struct Smem {
   uint8_t a[kAStages][2][kChunkBytes];    // expanded tiles: 2 K-chunks of 128 rows x 128 B
-  uint8_t b[2][kMaxN * 128];              // expanded queries: 2 K-chunks of N rows x 128 B
-  uint8_t packed[kPackStages][kTileRows * 32];
-  uint64_t pk_full[kPackStages], pk_empty[kPackStages];
+  uint64_t pk_full[kMaxPackStages], pk_empty[kMaxPackStages];
   uint64_t a_full[kAStages], a_empty[kAStages];
   uint64_t acc_full[kAccStages], acc_empty[kAccStages];
   uint64_t b_full, b_empty, epi_exit, mma_done;
   uint32_t tmem_base;
   int abort_flag;
 };
-constexpr size_t kSmemBytes = sizeof(Smem) + 1024;  // + slack to align the base to 1024 B
+constexpr size_t kBOffset = (sizeof(Smem) + 1023) & ~static_cast<size_t>(1023);
 
 // ---- tcgen05 wrappers
 
@@ -87,23 +95,34 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
           smem_u32(bar))
       : "memory");
 }
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+// Issue a load of 32 consecutive columns of this warp's 32 TMEM lanes. The registers are
+// written asynchronously: read them only through tmem_take() after tmem_ld_wait().
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-        "=r"(r[31])
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr)
       : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+// After tmem_ld_wait(): pass the registers through an empty volatile asm so that no use of
+// them can be scheduled above the wait.
+__device__ __forceinline__ void tmem_take(uint32_t (&r)[32], float (&v)[32]) {
+  asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]));
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Issue a load of 64 consecutive columns of this warp's 32 TMEM lanes holding 16-bit
+// values; column pairs (2i, 2i+1) arrive packed in r[i]. Valid only after tmem_ld_wait().
+__device__ __forceinline__ void tmem_ld64_pack16_nowait(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.pack::16b.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
@@ -115,9 +134,9 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
          (static_cast<uint64_t>(2) << 61);               // swizzle: 128 B
 }
 
-// Instruction descriptor: D f32, A and B e4m3, both K-major, M = 128, N = n.
+// Instruction descriptor: D f16, A and B e4m3, both K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t idesc_f8(uint32_t n) {
-  return (1u << 4) | (0u << 7) | (0u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+  return (0u << 4) | (0u << 7) | (0u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
 }
 
 // 4 bits -> 4 e4m3 bytes: bit 0 -> 0x38 (+1.0), bit 1 -> 0xB8 (-1.0).
@@ -160,7 +179,31 @@ struct Params {
   uint64_t capacity;
   unsigned long long* count;
   int* dev_err;
+  uint32_t pack_stages;   // packed tiles in flight (<= kMaxPackStages)
+  uint32_t pack_offset;   // byte offset of the packed ring in shared memory
 };
+
+// Compact one column of hits across the warp (one atomic per warp with a hit).
+__device__ __forceinline__ void emit_hit(bool row_ok, uint64_t row, uint64_t q, float v,
+                                         float dot_min, const Params& prm, int lane) {
+  const bool hit = row_ok && q < prm.n_queries && v >= dot_min;
+  const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
+  if (ballot == 0) return;
+  const int leader = __ffs(ballot) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(prm.count, static_cast<unsigned long long>(__popc(ballot)));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (hit) {
+    const uint64_t pos = base + __popc(ballot & lanemask_lt());
+    if (pos < prm.capacity) {
+      ypdq_hit h;
+      h.index = row;
+      h.query = static_cast<uint32_t>(q);
+      h.distance = static_cast<uint32_t>((256.0f - v) * 0.5f);
+      prm.hits[pos] = h;
+    }
+  }
+}
 
 __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
   *reinterpret_cast<volatile int*>(&sm.abort_flag) = 1;
@@ -169,10 +212,15 @@ __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
 
 __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) {
   extern __shared__ uint8_t smem_raw[];
-  Smem& sm = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                      ~static_cast<uintptr_t>(1023));
+  uint8_t* const smem_base = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  Smem& sm = *reinterpret_cast<Smem*>(smem_base);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t N = prm.n_tile;
+  const uint32_t n_pack = prm.pack_stages;
+  uint8_t* const bchunk0 = smem_base + kBOffset;      // N rows x 128 B (K 0..127)
+  uint8_t* const bchunk1 = bchunk0 + N * 128;         // N rows x 128 B (K 128..255)
+  uint8_t* const packed = smem_base + prm.pack_offset;
   const uint64_t n_tiles = (prm.n_rows + kTileRows - 1) / kTileRows;
   const uint32_t n_passes = (prm.n_queries + N - 1) / N;
   // tiles of this CTA: blockIdx.x, blockIdx.x + gridDim.x, ...
@@ -181,7 +229,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
   volatile int* abort_flag = &sm.abort_flag;
 
   if (tid == 0) {
-    for (int s = 0; s < kPackStages; ++s) {
+    for (uint32_t s = 0; s < n_pack; ++s) {
       mbar_init(&sm.pk_full[s], 1);
       mbar_init(&sm.pk_empty[s], 4);
     }
@@ -216,13 +264,12 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
 
   if (warp == kProducerWarp) {
     if (lane == 0) {
-      uint32_t g = 0;
+      uint32_t slot = 0, phase = 0, issued = 0;
       bool ok = true;
       for (uint32_t p = 0; p < n_passes && ok; ++p) {
-        for (uint64_t k = 0; k < my_tiles; ++k, ++g) {
+        for (uint64_t k = 0; k < my_tiles; ++k) {
           const uint64_t tile = blockIdx.x + k * gridDim.x;
-          const uint32_t slot = g % kPackStages;
-          if (!mbar_wait(&sm.pk_empty[slot], ((g / kPackStages) & 1u) ^ 1u, abort_flag)) {
+          if (!mbar_wait(&sm.pk_empty[slot], phase ^ 1u, abort_flag)) {
             ok = false;
             break;
           }
@@ -230,16 +277,24 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
           const uint64_t nr = (prm.n_rows - r0) < kTileRows ? (prm.n_rows - r0) : kTileRows;
           const uint32_t bytes = static_cast<uint32_t>(nr * 32);
           mbar_arrive_expect_tx(&sm.pk_full[slot], bytes);
-          bulk_g2s(sm.packed[slot], prm.rows + r0 * 32, bytes, &sm.pk_full[slot],
+          bulk_g2s(packed + slot * kPackBytes, prm.rows + r0 * 32, bytes, &sm.pk_full[slot],
                    policy_evict_first());
+          ++issued;
+          if (++slot == n_pack) {
+            slot = 0;
+            phase ^= 1u;
+          }
         }
       }
       if (!ok) {
         raise_abort(sm, prm.dev_err);
-        for (uint32_t k = 1; k <= kPackStages && k <= g; ++k) {
-          const uint32_t gi = g - k;
+        // let the copies already issued land (bounded): they sit in the n_pack slots before
+        // `slot`; those at or past `slot` were issued in the previous phase
+        for (uint32_t k = 1; k <= n_pack && k <= issued; ++k) {
+          const uint32_t sl = (slot + n_pack - k) % n_pack;
+          const uint32_t ph = (k <= slot) ? phase : (phase ^ 1u);
           const uint64_t t0 = globaltimer_ns();
-          while (!mbar_try_wait(&sm.pk_full[gi % kPackStages], (gi / kPackStages) & 1u))
+          while (!mbar_try_wait(&sm.pk_full[sl], ph))
             if (globaltimer_ns() - t0 > kWaitLimitNs / 4) break;
         }
       }
@@ -249,22 +304,20 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
 
   if (warp >= kExpandWarp0) {
     const int e = tid - kExpandWarp0 * 32;  // 0..127: tile row / query row
-    uint32_t g = 0, ga = 0;
+    uint32_t slot = 0, phase = 0, ga = 0;
     for (uint32_t p = 0; p < n_passes; ++p) {
       // queries of this pass into B (N rows; padding rows are zero = contributes nothing)
       if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag)) goto fail;
       for (uint32_t qr = e; qr < N; qr += 128) {
         const uint64_t qi = static_cast<uint64_t>(p) * N + qr;
-        uint8_t* c0 = sm.b[0];
-        uint8_t* c1 = sm.b[1];
         if (qi < prm.n_queries) {
           const uint4* src = reinterpret_cast<const uint4*>(prm.queries + qi * 32);
-          expand_row(src[0], src[1], c0, c1, static_cast<int>(qr));
+          expand_row(src[0], src[1], bchunk0, bchunk1, static_cast<int>(qr));
         } else {
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
-            *reinterpret_cast<uint4*>(c0 + qr * 128 + u * 16) = make_uint4(0, 0, 0, 0);
-            *reinterpret_cast<uint4*>(c1 + qr * 128 + u * 16) = make_uint4(0, 0, 0, 0);
+            *reinterpret_cast<uint4*>(bchunk0 + qr * 128 + u * 16) = make_uint4(0, 0, 0, 0);
+            *reinterpret_cast<uint4*>(bchunk1 + qr * 128 + u * 16) = make_uint4(0, 0, 0, 0);
           }
         }
       }
@@ -272,14 +325,17 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.b_full);
 
-      for (uint64_t k = 0; k < my_tiles; ++k, ++g, ++ga) {
-        const uint32_t slot = g % kPackStages;
+      for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
         const uint32_t as = ga % kAStages;
-        if (!mbar_wait(&sm.pk_full[slot], (g / kPackStages) & 1u, abort_flag)) goto fail;
-        const uint4* src = reinterpret_cast<const uint4*>(sm.packed[slot] + e * 32);
+        if (!mbar_wait(&sm.pk_full[slot], phase, abort_flag)) goto fail;
+        const uint4* src = reinterpret_cast<const uint4*>(packed + slot * kPackBytes + e * 32);
         const uint4 w0 = src[0], w1 = src[1];
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.pk_empty[slot]);
+        if (++slot == n_pack) {
+          slot = 0;
+          phase ^= 1u;
+        }
         if (!mbar_wait(&sm.a_empty[as], ((ga / kAStages) & 1u) ^ 1u, abort_flag)) goto fail;
         expand_row(w0, w1, sm.a[as][0], sm.a[as][1], e);
         fence_proxy_async_smem();
@@ -304,7 +360,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
           break;
         }
         tc_fence_after();
-        const uint32_t b0 = smem_u32(sm.b[0]), b1 = smem_u32(sm.b[1]);
+        const uint32_t b0 = smem_u32(bchunk0), b1 = smem_u32(bchunk1);
         for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
           const uint32_t as = ga % kAStages, ac = ga % kAccStages;
           if (!mbar_wait(&sm.a_full[as], (ga / kAStages) & 1u, abort_flag) ||
@@ -346,10 +402,13 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
     return;
   }
 
-  // ---- epilogue warps 0..3: thread row = warp*32 + lane of the tile
+  // ---- epilogue warps 0..7: rows (warp % 4) * 32 + lane of the tile; warp / 4 picks
+  // alternate 64-column chunks of the accumulator
   {
     const float dot_min = 256.0f - 2.0f * static_cast<float>(prm.threshold);
-    const uint32_t lane_addr = static_cast<uint32_t>(warp * 32) << 16;
+    const uint32_t quarter = static_cast<uint32_t>(warp & 3);
+    const uint32_t group = static_cast<uint32_t>(warp >> 2);
+    const uint32_t lane_addr = (quarter * 32) << 16;
     uint32_t ga = 0;
     bool ok = true;
     for (uint32_t p = 0; p < n_passes && ok; ++p) {
@@ -362,41 +421,26 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
           break;
         }
         tc_fence_after();
-        const uint64_t row = tile * kTileRows + warp * 32 + lane;
+        const uint64_t row = tile * kTileRows + quarter * 32 + lane;
         const bool row_ok = row < prm.n_rows;
-        for (uint32_t c0 = 0; c0 < N; c0 += 32) {
-          float v[32];
-          tmem_ld32(tmem_base + lane_addr + ac * N + c0, v);
-          float m = v[0];
+        for (uint32_t c0 = 64 * group; c0 < N; c0 += 64 * (kEpilogueWarps / 4)) {
+          uint32_t raw[32];
+          float unused[32];
+          tmem_ld64_pack16_nowait(tmem_base + lane_addr + ac * N + c0, raw);
+          tmem_ld_wait();
+          tmem_take(raw, unused);
+          __half2 mh = *reinterpret_cast<const __half2*>(&raw[0]);
 #pragma unroll
-          for (int i = 1; i < 32; ++i) m = fmaxf(m, v[i]);
+          for (int i = 1; i < 32; ++i) mh = __hmax2(mh, *reinterpret_cast<const __half2*>(&raw[i]));
+          const float m = fmaxf(__low2float(mh), __high2float(mh));
           if (__any_sync(0xffffffffu, row_ok && m >= dot_min)) {
-#pragma unroll 1
-            for (int i = 0; i < 32; ++i) {
-              const uint64_t q = q0 + c0 + i;
-              float vi = v[0];
+            // rare: some lane holds a hit in these 64 columns; fully unrolled so that the
+            // accumulator words stay in registers
 #pragma unroll
-              for (int j = 1; j < 32; ++j)
-                if (i == j) vi = v[j];
-              const bool hit = row_ok && q < prm.n_queries && vi >= dot_min;
-              const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
-              if (ballot) {
-                const int leader = __ffs(ballot) - 1;
-                unsigned long long base = 0;
-                if (lane == leader)
-                  base = atomicAdd(prm.count, static_cast<unsigned long long>(__popc(ballot)));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (hit) {
-                  const uint64_t pos = base + __popc(ballot & lanemask_lt());
-                  if (pos < prm.capacity) {
-                    ypdq_hit h;
-                    h.index = row;
-                    h.query = static_cast<uint32_t>(q);
-                    h.distance = static_cast<uint32_t>((256.0f - vi) * 0.5f);
-                    prm.hits[pos] = h;
-                  }
-                }
-              }
+            for (int j = 0; j < 32; ++j) {
+              const __half2 h2 = *reinterpret_cast<const __half2*>(&raw[j]);
+              emit_hit(row_ok, row, q0 + c0 + 2 * j, __low2float(h2), dot_min, prm, lane);
+              emit_hit(row_ok, row, q0 + c0 + 2 * j + 1, __high2float(h2), dot_min, prm, lane);
             }
           }
         }
@@ -416,7 +460,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
 
 cudaError_t scan_tc_init() {
   return cudaFuncSetAttribute(tc::scan_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(tc::kSmemBytes));
+                              static_cast<int>(tc::kSmemLimit));
 }
 
 cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
@@ -425,17 +469,26 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   prm.n_rows = p.n_rows;
   prm.queries = p.queries;
   prm.n_queries = p.n_queries;
-  // N is a multiple of 32 so every 32-column TMEM load stays inside one accumulator.
-  uint32_t n = (p.n_queries + 31u) & ~31u;
+  // N is a multiple of 64 so every 64-column TMEM load stays inside one accumulator.
+  uint32_t n = (p.n_queries + 63u) & ~63u;
   prm.n_tile = n > static_cast<uint32_t>(tc::kMaxN) ? static_cast<uint32_t>(tc::kMaxN) : n;
   prm.threshold = p.threshold;
   prm.hits = p.hits;
   prm.capacity = p.capacity;
   prm.count = p.count;
   prm.dev_err = p.dev_err;
+  // layout: [fixed Smem][B: 2 x N x 128][packed ring: stages x 4 KB], base aligned to 1024
+  const size_t b_end = tc::kBOffset + 2 * static_cast<size_t>(prm.n_tile) * 128;
+  const size_t avail = tc::kSmemLimit - 1024 - b_end;
+  size_t stages = avail / tc::kPackBytes;
+  if (stages > static_cast<size_t>(tc::kMaxPackStages)) stages = tc::kMaxPackStages;
+  if (stages < 2) return cudaErrorInvalidConfiguration;
+  prm.pack_stages = static_cast<uint32_t>(stages);
+  prm.pack_offset = static_cast<uint32_t>(b_end);
+  const size_t smem = b_end + stages * tc::kPackBytes + 1024;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
-  tc::scan_tc_kernel<<<static_cast<unsigned>(grid), tc::kThreads, tc::kSmemBytes, s>>>(prm);
+  tc::scan_tc_kernel<<<static_cast<unsigned>(grid), tc::kThreads, smem, s>>>(prm);
   return cudaGetLastError();
 }
 
