@@ -245,9 +245,14 @@ def run_ours(args):
         # FP8 dense peak taken as 2x the measured bf16 dense burst (the nominal 4.5 : 2.25 ratio)
         flops = 2.0 * 256 * nq * n
         achieved = flops / (scan_avg / 1000.0) / 1e12
+        # DRAM traffic: 320.5 MB per query pass of 256 (ncu capture of the 10M-row scan at
+        # 2,048 queries, profiles/scan_tc_10M_rows_2048_queries.md), scaled by passes and rows
+        passes = (nq + 255) // 256
+        traffic = passes * 320.5e6 * (n / 10_000_000)
         roofline = {"bound": "tensor", "kernel": "scan_tc_kernel (tcgen05 kind::f8f6f4)",
                     "achieved": achieved, "peak": 2 * bf16_peak, "unit": "TFLOP/s",
-                    "frac": achieved / (2 * bf16_peak), "traffic": None,
+                    "frac": achieved / (2 * bf16_peak), "traffic": traffic,
+                    "traffic_unit": "bytes per launch (scaled from an ncu capture)",
                     "peak_source": "%s bf16 burst x 2 (fp8 dense)" % peak_kind,
                     "launch_ms": scan_avg, "launches_per_step": 1,
                     "db_stream_gbs": (n * 32 * ((nq + 255) // 256)) / (scan_avg / 1e3) / 1e9}

@@ -159,3 +159,22 @@ def test_synth_rows_match_cpu_twin(ctx, yp, oracle):
     yp._lib.check(ctx.lib.ypdq_synth_rows(ctx.handle, d.ptr, n, 5, 42, None))
     ctx.sync()
     assert np.array_equal(d.download((n, 32), np.uint8), oracle.synth_rows(n, 42, first=5))
+
+
+def test_screen_host_chunked(ctx, yp, oracle):
+    """ypdq_screen_host with >= 256 images runs in chunks whose copies overlap compute; the
+    hit list must still equal the oracle's, with query numbers image * 8 + slot."""
+    imgs = yp.synth.blob_images(300, seed=44)
+    h, q, t, _ = oracle.hash_batch(imgs)
+    queries = h.reshape(-1, 32)
+    rows = yp.synth.rows_128(60000, seed=45)
+    yp.synth.plant(rows, queries, 2000, 0, 40, seed=46)
+    db = yp.Database(ctx, rows)
+    hits, hashes = yp.screen_host(ctx, db, imgs, threshold=31, want_hashes=True)
+    assert np.array_equal(hashes, h)
+    want = oracle.find_all(rows, queries, 31)
+    assert np.array_equal(as_tuples(hits), as_tuples(want))
+    u8 = yp.synth.to_u8(imgs)
+    hu, _, _, _ = oracle.hash_batch(u8)
+    hits_u8 = yp.screen_host(ctx, db, u8, threshold=31)
+    assert np.array_equal(as_tuples(hits_u8), as_tuples(oracle.find_all(rows, hu.reshape(-1, 32), 31)))

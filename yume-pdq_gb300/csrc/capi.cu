@@ -19,7 +19,10 @@ struct ypdq_ctx {
   int hash_ctas_f32 = 1;
   int hash_ctas_u8 = 1;
   int* d_err = nullptr;
-  cudaStream_t stream = nullptr;  // used by the blocking _host calls
+  cudaStream_t stream = nullptr;       // compute stream of the blocking _host calls
+  cudaStream_t copy_stream = nullptr;  // host->device copies that overlap that compute
+  static constexpr int kMaxChunks = 8;
+  cudaEvent_t chunk_copied[kMaxChunks] = {};
   std::mutex mu;                  // guards the scratch buffers below
   void* scratch[8] = {};
   size_t scratch_bytes[8] = {};
@@ -139,6 +142,9 @@ ypdq_status ypdq_ctx_create(int device, ypdq_ctx** out) {
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+  for (int i = 0; i < ypdq_ctx::kMaxChunks && e == cudaSuccess; ++i)
+    e = cudaEventCreateWithFlags(&ctx->chunk_copied[i], cudaEventDisableTiming);
   if (e != cudaSuccess) {
     if (ctx->d_err) cudaFree(ctx->d_err);
     delete ctx;
@@ -162,6 +168,9 @@ ypdq_status ypdq_ctx_destroy(ypdq_ctx* ctx) {
     if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+  for (int i = 0; i < ypdq_ctx::kMaxChunks; ++i)
+    if (ctx->chunk_copied[i]) cudaEventDestroy(ctx->chunk_copied[i]);
   delete ctx;
   return YPDQ_OK;
 }
@@ -343,6 +352,9 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
   if (!db || !n_hits || (n > 0 && !h_images) || (capacity > 0 && !h_hits))
     return fail(YPDQ_ERR_INVALID, "NULL argument");
   if (n < 0 || n * 8 > 0xffffffffll) return fail(YPDQ_ERR_INVALID, "n out of range");
+  if (input_kind != YPDQ_INPUT_F32 && input_kind != YPDQ_INPUT_U8)
+    return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
+  if (threshold > 256) return fail(YPDQ_ERR_INVALID, "threshold %u > 256", threshold);
   std::lock_guard<std::mutex> lock(ctx->mu);
   cudaStream_t s = ctx->stream;
   const size_t img_bytes = (input_kind == YPDQ_INPUT_U8 ? 1u : 4u) * 512u * 512u;
@@ -352,16 +364,52 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
   if ((st = scratch(ctx, 2, 32 * (n > 0 ? n : 1), &d_q))) return st;
   if ((st = scratch(ctx, 3, sizeof(ypdq_hit) * (capacity > 0 ? capacity : 1), &d_hits))) return st;
   if ((st = scratch(ctx, 4, 64, &d_cnt))) return st;
-  if (n > 0) CK(cudaMemcpyAsync(d_img, h_images, img_bytes * n, cudaMemcpyHostToDevice, s), "H2D images");
-  if ((st = ypdq_hash_batch(ctx, d_img, n, input_kind, dct_precision, semantics,
-                            static_cast<uint8_t*>(d_hash), static_cast<float*>(d_q), nullptr,
-                            nullptr, 1, nullptr, reinterpret_cast<ypdq_stream_t>(s))))
-    return st;
-  if ((st = ypdq_scan(ctx, db->d_rows, db->n_rows, static_cast<uint8_t*>(d_hash),
-                      static_cast<uint32_t>(n * 8), threshold, static_cast<ypdq_hit*>(d_hits),
-                      capacity, static_cast<uint64_t*>(d_cnt), YPDQ_SCAN_AUTO,
-                      reinterpret_cast<ypdq_stream_t>(s))))
-    return st;
+  CK(cudaMemsetAsync(d_cnt, 0, sizeof(uint64_t), s), "clear count");
+  // Chunks of at least 128 images: the copy of chunk c+1 (copy stream) overlaps the hash
+  // and scan of chunk c (compute stream); every chunk's scan appends to one hit list.
+  const int nch = n >= 256 ? static_cast<int>(n / 128 < ypdq_ctx::kMaxChunks ? n / 128
+                                                                              : ypdq_ctx::kMaxChunks)
+                           : 1;
+  uint32_t rm, cm;
+  semantics_masks(semantics, &rm, &cm);
+  if (dct_precision != YPDQ_DCT_FP32)
+    return fail(dct_precision == YPDQ_DCT_TF32 || dct_precision == YPDQ_DCT_BF16X3
+                    ? YPDQ_ERR_UNSUPPORTED : YPDQ_ERR_INVALID,
+                "dct_precision %d", dct_precision);
+  for (int c = 0; c < nch && n > 0; ++c) {
+    const int64_t i0 = n * c / nch, i1 = n * (c + 1) / nch;
+    const uint8_t* src = static_cast<const uint8_t*>(h_images) + i0 * img_bytes;
+    uint8_t* dst = static_cast<uint8_t*>(d_img) + i0 * img_bytes;
+    CK(cudaMemcpyAsync(dst, src, (i1 - i0) * img_bytes, cudaMemcpyHostToDevice, ctx->copy_stream),
+       "H2D images");
+    CK(cudaEventRecord(ctx->chunk_copied[c], ctx->copy_stream), "record copy");
+    CK(cudaStreamWaitEvent(s, ctx->chunk_copied[c], 0), "wait copy");
+    HashLaunch hp{};
+    hp.images = dst;
+    hp.n = i1 - i0;
+    hp.input_u8 = input_kind == YPDQ_INPUT_U8;
+    hp.row_mask = rm;
+    hp.col_mask = cm;
+    hp.hashes = static_cast<uint8_t*>(d_hash) + i0 * 256;
+    hp.quality = static_cast<float*>(d_q) + i0 * 8;
+    hp.pdqf_slots = 1;
+    hp.dev_err = ctx->d_err;
+    CK(launch_hash(hp, ctx->num_sms, hp.input_u8 ? ctx->hash_ctas_u8 : ctx->hash_ctas_f32, s),
+       "hash launch");
+    ScanLaunch sp{};
+    sp.rows = db->d_rows;
+    sp.n_rows = db->n_rows;
+    sp.queries = static_cast<uint8_t*>(d_hash) + i0 * 256;
+    sp.n_queries = static_cast<uint32_t>((i1 - i0) * 8);
+    sp.threshold = threshold;
+    sp.hits = static_cast<ypdq_hit*>(d_hits);
+    sp.capacity = capacity;
+    sp.count = static_cast<unsigned long long*>(d_cnt);
+    sp.dev_err = ctx->d_err;
+    sp.append = 1;
+    sp.query_base = static_cast<uint32_t>(i0 * 8);
+    CK(launch_scan(sp, YPDQ_SCAN_AUTO, ctx->num_sms, s), "scan launch");
+  }
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, d_cnt, sizeof(uint64_t), cudaMemcpyDeviceToHost, s), "D2H count");
   CK(cudaStreamSynchronize(s), "screen sync");

@@ -152,7 +152,7 @@ cudaError_t scan_init() {
 }
 
 cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(p.count, 0, sizeof(unsigned long long), s);
+  cudaError_t e = p.append ? cudaSuccess : cudaMemsetAsync(p.count, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess || p.n_rows == 0 || p.n_queries == 0) return e;
   // SIMT is HBM-bound up to a few queries and beats the tensor-core pipeline up to ~16.
   if (algo == YPDQ_SCAN_AUTO) algo = p.n_queries <= 16 ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;
@@ -168,7 +168,7 @@ cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t
       const size_t smem = static_cast<size_t>((nq + 7) / 8) * 32 * sizeof(uint2);
       scan_b1_kernel<<<static_cast<unsigned>(blocks), kScanThreads, smem, s>>>(
           reinterpret_cast<const uint2*>(p.rows), p.n_rows, reinterpret_cast<const uint2*>(qptr),
-          nq, q0, p.threshold, p.hits, p.capacity, p.count);
+          nq, p.query_base + q0, p.threshold, p.hits, p.capacity, p.count);
     } else {
       uint64_t blocks = (p.n_rows + kScanThreads - 1) / kScanThreads;
       const uint64_t cap_blocks = static_cast<uint64_t>(num_sms) * 8;
@@ -176,7 +176,7 @@ cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t
       const size_t smem = static_cast<size_t>(nq) * 32;
       scan_simt_kernel<<<static_cast<unsigned>(blocks), kScanThreads, smem, s>>>(
           reinterpret_cast<const uint4*>(p.rows), p.n_rows, reinterpret_cast<const uint4*>(qptr),
-          nq, q0, p.threshold, p.hits, p.capacity, p.count);
+          nq, p.query_base + q0, p.threshold, p.hits, p.capacity, p.count);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;

@@ -179,6 +179,7 @@ struct Params {
   uint64_t capacity;
   unsigned long long* count;
   int* dev_err;
+  uint32_t query_base;    // added to reported query numbers
   uint32_t pack_stages;   // packed tiles in flight (<= kMaxPackStages)
   uint32_t pack_offset;   // byte offset of the packed ring in shared memory
 };
@@ -198,7 +199,7 @@ __device__ __forceinline__ void emit_hit(bool row_ok, uint64_t row, uint64_t q, 
     if (pos < prm.capacity) {
       ypdq_hit h;
       h.index = row;
-      h.query = static_cast<uint32_t>(q);
+      h.query = static_cast<uint32_t>(q) + prm.query_base;
       h.distance = static_cast<uint32_t>((256.0f - v) * 0.5f);
       prm.hits[pos] = h;
     }
@@ -477,6 +478,7 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   prm.capacity = p.capacity;
   prm.count = p.count;
   prm.dev_err = p.dev_err;
+  prm.query_base = p.query_base;
   // layout: [fixed Smem][B: 2 x N x 128][packed ring: stages x 4 KB], base aligned to 1024
   const size_t b_end = tc::kBOffset + 2 * static_cast<size_t>(prm.n_tile) * 128;
   const size_t avail = tc::kSmemLimit - 1024 - b_end;

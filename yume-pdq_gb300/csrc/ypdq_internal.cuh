@@ -134,6 +134,8 @@ struct ScanLaunch {
   uint64_t capacity;
   unsigned long long* count;
   int* dev_err;
+  int append;            // nonzero: add to *count instead of resetting it first
+  uint32_t query_base;   // added to every reported query number
 };
 
 // hash.cu
