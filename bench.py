@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--threshold", type=int, default=31)
     ap.add_argument("--algo", type=int, default=0, help="scan algorithm (0 auto, 1 SIMT, 2 B1MMA)")
     ap.add_argument("--seed", type=int, default=2025)
+    ap.add_argument("--dct", type=int, default=0, choices=[0, 1, 2],
+                    help="DCT stage 1: 0 FP32 SIMT (bit-exact), 1 TF32, 2 BF16x3 tensor cores")
     ap.add_argument("--cpu-sample", type=int, default=256,
                     help="images per CPU-baseline sample (about 10 s of work on 16 cores)")
     return ap.parse_args()
@@ -170,7 +172,8 @@ def run_ours(args):
     def step(record=False):
         if record:
             ctx.record(ev[0], stream)
-        yp.core.hash_batch_device(ctx, d_img, B, yp._lib.INPUT_F32, d_hash, d_q, stream=stream)
+        yp.core.hash_batch_device(ctx, d_img, B, yp._lib.INPUT_F32, d_hash, d_q, dct=args.dct,
+                                  stream=stream)
         if record:
             ctx.record(ev[1], stream)
         yp.core.scan_device(ctx, d_rows, n, d_hash, nq, args.threshold, d_hits, cap, d_cnt,
@@ -220,7 +223,7 @@ def run_ours(args):
 
     def e2e_step():
         yp._lib.check(ctx.lib.ypdq_screen_host(
-            ctx.handle, db.handle, h_img, B, yp._lib.INPUT_F32, 0, 0, args.threshold,
+            ctx.handle, db.handle, h_img, B, yp._lib.INPUT_F32, args.dct, 0, args.threshold,
             h_hits.ctypes.data_as(ctypes.c_void_p), len(h_hits), ctypes.byref(nh), None, None))
 
     for _ in range(max(1, args.warmup)):
@@ -277,7 +280,8 @@ def run_ours(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {0: "f32", 1: "f32 (DCT stage 1 tf32)", 2: "f32 (DCT stage 1 bf16x3)"}[args.dct],
         "data": "synthetic (seeded blob images; 10M rows of exactly 128 set bits + planted near-duplicates)",
         "config": {"workload": "screen %d f32 images x 8 dihedrals vs %d-row DB at t=%d" % (B, n, args.threshold),
                    "images_per_step": B, "queries_per_step": nq, "db_rows": n,

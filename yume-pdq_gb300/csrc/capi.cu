@@ -18,6 +18,7 @@ struct ypdq_ctx {
   int num_sms = 0;
   int hash_ctas_f32 = 1;
   int hash_ctas_u8 = 1;
+  int hash_ctas[2][3] = {{1, 1, 1}, {1, 1, 1}};  // [input u8][dct precision]
   int* d_err = nullptr;
   cudaStream_t stream = nullptr;       // compute stream of the blocking _host calls
   cudaStream_t copy_stream = nullptr;  // host->device copies that overlap that compute
@@ -139,6 +140,8 @@ ypdq_status ypdq_ctx_create(int device, ypdq_ctx** out) {
   if (e == cudaSuccess) e = scan_init();
   if (e == cudaSuccess) e = hash_occupancy(0, &ctx->hash_ctas_f32);
   if (e == cudaSuccess) e = hash_occupancy(1, &ctx->hash_ctas_u8);
+  for (int u = 0; u < 2 && e == cudaSuccess; ++u)
+    for (int d = 0; d < 3 && e == cudaSuccess; ++d) e = hash_occupancy_dct(u, d, &ctx->hash_ctas[u][d]);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -209,12 +212,8 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
     return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
   if (semantics < YPDQ_DIHEDRAL_EXACT || semantics > YPDQ_DIHEDRAL_SCALAR)
     return fail(YPDQ_ERR_INVALID, "semantics %d", semantics);
-  if (dct_precision != YPDQ_DCT_FP32) {
-    if (dct_precision == YPDQ_DCT_TF32 || dct_precision == YPDQ_DCT_BF16X3)
-      return fail(YPDQ_ERR_UNSUPPORTED, "dct_precision %d is not available in this build",
-                  dct_precision);
+  if (dct_precision < YPDQ_DCT_FP32 || dct_precision > YPDQ_DCT_BF16X3)
     return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
-  }
   if (d_pdqf && pdqf_slots != 1 && pdqf_slots != 8)
     return fail(YPDQ_ERR_INVALID, "pdqf_slots must be 1 or 8");
   if (!aligned16(d_images)) return fail(YPDQ_ERR_ALIGN, "d_images must be 16-byte aligned");
@@ -231,7 +230,8 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
   p.pdqf_slots = pdqf_slots;
   p.buf1 = d_buf1;
   p.dev_err = ctx->d_err;
-  CK(launch_hash(p, ctx->num_sms, p.input_u8 ? ctx->hash_ctas_u8 : ctx->hash_ctas_f32,
+  p.dct = dct_precision;
+  CK(launch_hash(p, ctx->num_sms, ctx->hash_ctas[p.input_u8][dct_precision],
                  reinterpret_cast<cudaStream_t>(stream)),
      "hash kernel launch");
   return YPDQ_OK;
@@ -372,10 +372,8 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
                            : 1;
   uint32_t rm, cm;
   semantics_masks(semantics, &rm, &cm);
-  if (dct_precision != YPDQ_DCT_FP32)
-    return fail(dct_precision == YPDQ_DCT_TF32 || dct_precision == YPDQ_DCT_BF16X3
-                    ? YPDQ_ERR_UNSUPPORTED : YPDQ_ERR_INVALID,
-                "dct_precision %d", dct_precision);
+  if (dct_precision < YPDQ_DCT_FP32 || dct_precision > YPDQ_DCT_BF16X3)
+    return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
   for (int c = 0; c < nch && n > 0; ++c) {
     const int64_t i0 = n * c / nch, i1 = n * (c + 1) / nch;
     const uint8_t* src = static_cast<const uint8_t*>(h_images) + i0 * img_bytes;
@@ -394,7 +392,8 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
     hp.quality = static_cast<float*>(d_q) + i0 * 8;
     hp.pdqf_slots = 1;
     hp.dev_err = ctx->d_err;
-    CK(launch_hash(hp, ctx->num_sms, hp.input_u8 ? ctx->hash_ctas_u8 : ctx->hash_ctas_f32, s),
+    hp.dct = dct_precision;
+    CK(launch_hash(hp, ctx->num_sms, ctx->hash_ctas[hp.input_u8][dct_precision], s),
        "hash launch");
     ScanLaunch sp{};
     sp.rows = db->d_rows;

@@ -25,6 +25,8 @@
 //              bulk async copies (4 input rows = one stage), NSTAGE stages deep.
 //   warp 5     epilogue: quality, exact medians, bits and dihedrals of image k while the
 //              compute warps already work on image k+1 (double-buffered PDQF).
+#include <cuda_bf16.h>
+
 #include <cstring>
 
 #include "ypdq_internal.cuh"
@@ -39,13 +41,39 @@ constexpr int kStagesPerImage = 128;  // stage s holds rows 4s+1 .. 4s+4 (stage 
 constexpr int kComputeThreads = 128;
 constexpr int kProducerWarp = 4;
 constexpr int kEpilogueWarp = 5;
-constexpr int kHashThreads = 192;
+constexpr int kMmaWarpHash = 6;   // tensor-core DCT only: allocates TMEM, issues the MMAs
+template <int kDct>
+constexpr int hash_threads() { return kDct == 0 ? 192 : 224; }
 constexpr int kComputeBarrier = 1;  // named barrier id used by the 128 compute threads
 
-template <int kStageBytes>
+// Stage 1 of the DCT on tensor cores (kDct = 1: TF32, 2: BF16x3). The compressed values
+// are written, chunk by chunk of compressed rows, into a 128-byte-swizzled K-major operand
+// A[j][i] (M = 128 columns j, K = rows i); B is the DCT matrix D[k][i] (N = 16).
+template <int kDct>
+struct DctTraits {
+  static constexpr int kRowsPerChunk = 128;  // unused for kDct = 0
+  static constexpr int kBufBytes = 16;
+  static constexpr int kDBytes = 16;
+};
+template <>
+struct DctTraits<1> {  // TF32: 32 rows x 4 B = 128 B per column per chunk
+  static constexpr int kRowsPerChunk = 32;
+  static constexpr int kBufBytes = 128 * 128;
+  static constexpr int kDBytes = 4 * 2048;  // 4 K-chunks x 16 rows x 128 B
+};
+template <>
+struct DctTraits<2> {  // BF16x3: 64 rows x 2 B, hi and lo operands
+  static constexpr int kRowsPerChunk = 64;
+  static constexpr int kBufBytes = 2 * 128 * 128;
+  static constexpr int kDBytes = 2 * 2 * 2048;  // hi, lo x 2 K-chunks x 16 rows x 128 B
+};
+
+template <int kStageBytes, int kDct>
 struct HashSmem {
+  alignas(1024) uint8_t ops[2][DctTraits<kDct>::kBufBytes];  // A operand, double-buffered
+  alignas(1024) uint8_t dops[DctTraits<kDct>::kDBytes];      // B operand (DCT matrix)
   alignas(128) unsigned char ring[kNumStages][kStageBytes];
-  alignas(16) float dt[128][16];  // dt[i][k] = D[k][i]; row 127 is zero
+  alignas(16) float dt[kDct == 0 ? 128 : 1][16];  // dt[i][k] = D[k][i]; row 127 is zero
   float dr[16][129];              // D[k][m], padded against bank conflicts
   float t[16][129];               // DCT stage 1 result T = D * B
   alignas(16) float p[2][256];    // PDQF, double-buffered between compute and epilogue
@@ -53,6 +81,8 @@ struct HashSmem {
   uint64_t empty[kNumStages];
   uint64_t pfull[2];
   uint64_t pempty[2];
+  uint64_t a_full[2], a_empty[2], acc_full[2], acc_empty[2], tc_exit, mma_done;
+  uint32_t tmem_base;
   int abort_flag;
 };
 
@@ -287,24 +317,100 @@ __device__ void epilogue_warp(const float* P, bool thr0_given, float thr0_in, ui
 
 // ------------------------------------------------------------------- kernel
 
-template <typename Tin>
-__global__ void __launch_bounds__(kHashThreads) hash_kernel(const HashLaunch prm) {
+// tcgen05 MMAs for the tensor-core DCT (M = 128, N = 16, f32 accumulate in TMEM).
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// D f32, A/B tf32 (format 2) or bf16 (format 1), K-major, M = 128, N = 16.
+constexpr uint32_t kIdescTf32 = (1u << 4) | (2u << 7) | (2u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t kIdescBf16 = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ void split_bf16(float x, uint16_t& hi, uint16_t& lo) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(x);
+  const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+  hi = __bfloat16_as_ushort(h);
+  lo = __bfloat16_as_ushort(l);
+}
+// Byte offset of element e (of `esize` bytes) in row r of a 128B-swizzled K-major chunk.
+__device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t e, uint32_t esize) {
+  const uint32_t byte = e * esize;
+  return r * 128 + ((((byte >> 4) ^ (r & 7))) << 4) + (byte & 15);
+}
+// 16 consecutive TMEM columns of this warp's 32 lanes (valid after tmem_ld_wait).
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_take16(uint32_t (&r)[16]) {
+  asm volatile(""
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
+}
+
+template <typename Tin, int kDct>
+__global__ void __launch_bounds__(hash_threads<kDct>()) hash_kernel(const HashLaunch prm) {
   constexpr int kRowBytes = InputTraits<Tin>::kRowBytes;
   constexpr int kStageBytes = 4 * kRowBytes;
-  using Smem = HashSmem<kStageBytes>;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  constexpr int kThreads = hash_threads<kDct>();
+  using Smem = HashSmem<kStageBytes, kDct>;
+  extern __shared__ unsigned char smem_raw[];
+  // Align by offsetting the shared array itself so the compiler keeps the shared address
+  // space (an integer round trip would turn every access into a generic one).
+  Smem& sm = *reinterpret_cast<Smem*>(smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u));
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
 
-  for (int idx = tid; idx < 16 * 127; idx += kHashThreads) {
+  for (int idx = tid; idx < 16 * 127; idx += kThreads) {
     const int k = idx / 127, i = idx - k * 127;
     const float d = g_dct[idx];
-    sm.dt[i][k] = d;
+    if constexpr (kDct == 0) sm.dt[i][k] = d;
     sm.dr[k][i] = d;
   }
-  if (tid < 16) sm.dt[127][tid] = 0.0f;
+  if constexpr (kDct == 0) {
+    if (tid < 16) sm.dt[127][tid] = 0.0f;
+  } else {
+    // the DCT matrix as the MMA's B operand: N = 16 rows k, K = 128 (column 127 is zero)
+    for (int idx = tid; idx < 16 * 128; idx += kThreads) {
+      const int k = idx >> 7, i = idx & 127;
+      const float d = i < 127 ? g_dct[k * 127 + i] : 0.0f;
+      if constexpr (kDct == 1) {
+        *reinterpret_cast<uint32_t*>(sm.dops + (i >> 5) * 2048 + sw128_offset(k, i & 31, 4)) = to_tf32(d);
+      } else {
+        uint16_t hi, lo;
+        split_bf16(d, hi, lo);
+        const uint32_t off = (i >> 6) * 2048 + sw128_offset(k, i & 63, 2);
+        *reinterpret_cast<uint16_t*>(sm.dops + off) = hi;
+        *reinterpret_cast<uint16_t*>(sm.dops + 4096 + off) = lo;
+      }
+    }
+    fence_proxy_async_smem();
+  }
   if (tid == 0) {
     for (int s = 0; s < kNumStages; ++s) {
       mbar_init(&sm.full[s], 1);
@@ -313,11 +419,25 @@ __global__ void __launch_bounds__(kHashThreads) hash_kernel(const HashLaunch prm
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.pfull[b], kComputeThreads / 32);
       mbar_init(&sm.pempty[b], 1);
+      mbar_init(&sm.a_full[b], kComputeThreads / 32);
+      mbar_init(&sm.a_empty[b], 1);
+      mbar_init(&sm.acc_full[b], 1);
+      mbar_init(&sm.acc_empty[b], kComputeThreads / 32);
     }
+    mbar_init(&sm.tc_exit, kComputeThreads / 32);
+    mbar_init(&sm.mma_done, 1);
     sm.abort_flag = 0;
     fence_mbar_init();
   }
+  if constexpr (kDct != 0) {
+    if (warp == kMmaWarpHash) {
+      tmem_alloc(&sm.tmem_base, 32);  // two 16-column accumulators
+      tmem_relinquish();
+    }
+    tc_fence_before();
+  }
   __syncthreads();
+  if constexpr (kDct != 0) tc_fence_after();
 
   volatile int* abort_flag = &sm.abort_flag;
   const int64_t n_images = prm.n;
@@ -380,13 +500,146 @@ __global__ void __launch_bounds__(kHashThreads) hash_kernel(const HashLaunch prm
     return;
   }
 
+  if constexpr (kDct != 0) {
+    if (warp == kMmaWarpHash) {
+      constexpr int kChunks = 128 / DctTraits<kDct>::kRowsPerChunk;
+      const uint32_t tmem = sm.tmem_base;
+      if (lane == 0) {
+        bool ok = true;
+        uint32_t gc = 0, it = 0;
+        for (int64_t n = blockIdx.x; n < n_images && ok; n += gridDim.x, ++it) {
+          const uint32_t acc = it & 1;
+          if (!mbar_wait(&sm.acc_empty[acc], ((it >> 1) & 1u) ^ 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          for (int c = 0; c < kChunks; ++c, ++gc) {
+            const uint32_t buf = gc & 1;
+            if (!mbar_wait(&sm.a_full[buf], (gc >> 1) & 1u, abort_flag)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t a = smem_u32(sm.ops[buf]);
+            const uint32_t d = smem_u32(sm.dops) + c * 2048;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint32_t accumulate = (c > 0 || ks > 0) ? 1u : 0u;
+              if constexpr (kDct == 1) {
+                mma_tf32(tmem + acc * 16, sw128_desc(a + ks * 32), sw128_desc(d + ks * 32),
+                         kIdescTf32, accumulate);
+              } else {
+                // x * y ~ xh*yh + xh*yl + xl*yh   (x = A, y = D; lo operands 16 KB / 4 KB on)
+                mma_bf16(tmem + acc * 16, sw128_desc(a + ks * 32), sw128_desc(d + ks * 32),
+                         kIdescBf16, accumulate);
+                mma_bf16(tmem + acc * 16, sw128_desc(a + ks * 32),
+                         sw128_desc(d + 4096 + ks * 32), kIdescBf16, 1u);
+                mma_bf16(tmem + acc * 16, sw128_desc(a + 16384 + ks * 32),
+                         sw128_desc(d + ks * 32), kIdescBf16, 1u);
+              }
+            }
+            mma_commit(&sm.a_empty[buf]);
+          }
+          if (ok) mma_commit(&sm.acc_full[acc]);
+        }
+        if (!ok) {
+          *abort_flag = 1;
+          atomicOr(prm.dev_err, kDevErrTimeout);
+        }
+        mma_commit(&sm.mma_done);
+        const uint64_t t0 = globaltimer_ns();
+        while (!mbar_try_wait(&sm.mma_done, 0))
+          if (globaltimer_ns() - t0 > kWaitLimitNs) break;
+      }
+      __syncwarp();
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.tc_exit, 0))
+        if (globaltimer_ns() - t0 > kWaitLimitNs) break;
+      tc_fence_after();
+      tmem_dealloc(tmem, 32);
+      return;
+    }
+  }
+
   // ---- compute warps: thread j <-> compressed column j
   const int j = tid;
   const bool active = j < 127;
   uint32_t it = 0;
   for (int64_t n = blockIdx.x; n < n_images; n += gridDim.x, ++it) {
     const uint32_t g0 = it * kStagesPerImage;
+    if constexpr (kDct != 0) {
+      // stage 1 on tensor cores: write the compressed column into the operand chunks
+      constexpr int kR = DctTraits<kDct>::kRowsPerChunk;
+      constexpr uint32_t kChunks = 128 / kR;
+      const uint32_t gc0 = it * kChunks;
+      if (!mbar_wait(&sm.full[g0 % kNumStages], (g0 / kNumStages) & 1u, abort_flag)) goto fail;
+      for (int i0 = 0; i0 < 128; i0 += 4) {
+        float b[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int i = i0 + r;
+          b[r] = 0.0f;
+          if (i < 127) {
+            const uint32_t ga = g0 + i, gb = ga + 1;
+            if (!mbar_wait(&sm.full[gb % kNumStages], (gb / kNumStages) & 1u, abort_flag))
+              goto fail;
+            if (active) {
+              const Tin* st0 = reinterpret_cast<const Tin*>(sm.ring[ga % kNumStages]);
+              const Tin* st1 = reinterpret_cast<const Tin*>(sm.ring[gb % kNumStages]);
+              b[r] = compress_at<Tin>(st0, st1, j);
+              if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b[r];
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sm.empty[ga % kNumStages]);
+          }
+        }
+        const uint32_t within = static_cast<uint32_t>(i0 % kR);
+        const uint32_t chunk = gc0 + static_cast<uint32_t>(i0 / kR);
+        const uint32_t buf = chunk & 1;
+        if (within == 0 &&
+            !mbar_wait(&sm.a_empty[buf], ((chunk >> 1) & 1u) ^ 1u, abort_flag))
+          goto fail;
+        if constexpr (kDct == 1) {
+          const uint4 w = make_uint4(to_tf32(b[0]), to_tf32(b[1]), to_tf32(b[2]), to_tf32(b[3]));
+          *reinterpret_cast<uint4*>(sm.ops[buf] + sw128_offset(j, within, 4)) = w;
+        } else {
+          uint16_t h[4], l[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) split_bf16(b[r], h[r], l[r]);
+          const uint32_t off = sw128_offset(j, within, 2);
+          *reinterpret_cast<uint2*>(sm.ops[buf] + off) =
+              make_uint2(h[0] | (static_cast<uint32_t>(h[1]) << 16), h[2] | (static_cast<uint32_t>(h[3]) << 16));
+          *reinterpret_cast<uint2*>(sm.ops[buf] + 16384 + off) =
+              make_uint2(l[0] | (static_cast<uint32_t>(l[1]) << 16), l[2] | (static_cast<uint32_t>(l[3]) << 16));
+        }
+        if (within + 4 == static_cast<uint32_t>(kR)) {
+          fence_proxy_async_smem();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&sm.a_full[buf]);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.empty[(g0 + 127) % kNumStages]);
+      {
+        const uint32_t acc = it & 1;
+        if (!mbar_wait(&sm.acc_full[acc], (it >> 1) & 1u, abort_flag)) goto fail;
+        tc_fence_after();
+        uint32_t tr[16];
+        tmem_ld16_nowait(sm.tmem_base + (static_cast<uint32_t>(warp * 32) << 16) + acc * 16, tr);
+        tmem_ld_wait();
+        tmem_take16(tr);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.acc_empty[acc]);
+        if (active) {
+#pragma unroll
+          for (int k = 0; k < 16; ++k) sm.t[k][j] = __uint_as_float(tr[k]);
+        }
+      }
+    } else {
     float acc[16][4];
+
 #pragma unroll
     for (int k = 0; k < 16; ++k)
 #pragma unroll
@@ -427,6 +680,7 @@ __global__ void __launch_bounds__(kHashThreads) hash_kernel(const HashLaunch prm
       for (int k = 0; k < 16; ++k)
         sm.t[k][j] = __fadd_rn(__fadd_rn(__fadd_rn(acc[k][0], acc[k][1]), acc[k][2]), acc[k][3]);
     }
+    }  // FP32 stage 1
     named_bar_sync(kComputeBarrier, kComputeThreads);
     {
       // stage 2: P[k][c] = sum_m T[k][m] * D[c][m]; thread -> (k, c0), (k, c0 + 1)
@@ -454,10 +708,20 @@ __global__ void __launch_bounds__(kHashThreads) hash_kernel(const HashLaunch prm
     }
     named_bar_sync(kComputeBarrier, kComputeThreads);
   }
+  if constexpr (kDct != 0) {
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.tc_exit);
+  }
   return;
 fail:
   *abort_flag = 1;
   if (lane == 0) atomicOr(prm.dev_err, kDevErrTimeout);
+  if constexpr (kDct != 0) {
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.tc_exit);
+  }
 }
 
 // Dihedrals of given PDQF matrices: one warp per matrix.
@@ -483,9 +747,15 @@ __global__ void __launch_bounds__(128) dihedral_kernel(const DihedralLaunch prm)
 
 // ------------------------------------------------------------------ host side
 
-template <typename Tin>
+template <typename Tin, int kDct>
 static size_t hash_smem_bytes() {
-  return sizeof(HashSmem<4 * InputTraits<Tin>::kRowBytes>);
+  return sizeof(HashSmem<4 * InputTraits<Tin>::kRowBytes, kDct>) + 1024;  // + base alignment
+}
+
+template <typename Tin, int kDct>
+static cudaError_t set_smem_attr() {
+  return cudaFuncSetAttribute(hash_kernel<Tin, kDct>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(hash_smem_bytes<Tin, kDct>()));
 }
 
 cudaError_t upload_constants() {
@@ -495,30 +765,49 @@ cudaError_t upload_constants() {
     memcpy(&d[i], &b, 4);
   }
   cudaError_t e = cudaMemcpyToSymbol(g_dct, d, sizeof(d));
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(hash_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(hash_smem_bytes<float>()));
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(hash_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(hash_smem_bytes<uint8_t>()));
+  if (e == cudaSuccess) e = set_smem_attr<float, 0>();
+  if (e == cudaSuccess) e = set_smem_attr<uint8_t, 0>();
+  if (e == cudaSuccess) e = set_smem_attr<float, 1>();
+  if (e == cudaSuccess) e = set_smem_attr<uint8_t, 1>();
+  if (e == cudaSuccess) e = set_smem_attr<float, 2>();
+  if (e == cudaSuccess) e = set_smem_attr<uint8_t, 2>();
+  return e;
+}
+
+template <typename Tin, int kDct>
+static cudaError_t occupancy_of(int* ctas) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, hash_kernel<Tin, kDct>,
+                                                       hash_threads<kDct>(),
+                                                       hash_smem_bytes<Tin, kDct>());
 }
 
 cudaError_t hash_occupancy(int input_u8, int* ctas_per_sm) {
-  if (input_u8)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        ctas_per_sm, hash_kernel<uint8_t>, kHashThreads, hash_smem_bytes<uint8_t>());
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, hash_kernel<float>,
-                                                       kHashThreads, hash_smem_bytes<float>());
+  return input_u8 ? occupancy_of<uint8_t, 0>(ctas_per_sm) : occupancy_of<float, 0>(ctas_per_sm);
+}
+
+cudaError_t hash_occupancy_dct(int input_u8, int dct, int* ctas_per_sm) {
+  if (dct == 1) return input_u8 ? occupancy_of<uint8_t, 1>(ctas_per_sm) : occupancy_of<float, 1>(ctas_per_sm);
+  if (dct == 2) return input_u8 ? occupancy_of<uint8_t, 2>(ctas_per_sm) : occupancy_of<float, 2>(ctas_per_sm);
+  return hash_occupancy(input_u8, ctas_per_sm);
+}
+
+template <typename Tin, int kDct>
+static void launch_one(const HashLaunch& p, int64_t grid, cudaStream_t s) {
+  hash_kernel<Tin, kDct><<<static_cast<int>(grid), hash_threads<kDct>(), hash_smem_bytes<Tin, kDct>(), s>>>(p);
 }
 
 cudaError_t launch_hash(const HashLaunch& p, int num_sms, int ctas_per_sm, cudaStream_t s) {
   if (p.n <= 0) return cudaSuccess;
   int64_t grid = static_cast<int64_t>(num_sms) * (ctas_per_sm > 0 ? ctas_per_sm : 1);
   if (grid > p.n) grid = p.n;
-  if (p.input_u8) {
-    hash_kernel<uint8_t><<<static_cast<int>(grid), kHashThreads, hash_smem_bytes<uint8_t>(), s>>>(p);
-  } else {
-    hash_kernel<float><<<static_cast<int>(grid), kHashThreads, hash_smem_bytes<float>(), s>>>(p);
+  switch (p.dct * 2 + (p.input_u8 ? 1 : 0)) {
+    case 0: launch_one<float, 0>(p, grid, s); break;
+    case 1: launch_one<uint8_t, 0>(p, grid, s); break;
+    case 2: launch_one<float, 1>(p, grid, s); break;
+    case 3: launch_one<uint8_t, 1>(p, grid, s); break;
+    case 4: launch_one<float, 2>(p, grid, s); break;
+    case 5: launch_one<uint8_t, 2>(p, grid, s); break;
+    default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }

@@ -56,30 +56,6 @@ struct Smem {
 };
 constexpr size_t kBOffset = (sizeof(Smem) + 1023) & ~static_cast<size_t>(1023);
 
-// ---- tcgen05 wrappers
-
-__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                   smem_u32(dst_smem)),
-               "r"(ncols)
-               : "memory");
-}
-__device__ __forceinline__ void tmem_relinquish() {
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
-               : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
 __device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                        uint32_t idesc, uint32_t accumulate) {
   asm volatile(
@@ -88,15 +64,6 @@ __device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t
       "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tmem_ld_wait() {
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 // Issue a load of 32 consecutive columns of this warp's 32 TMEM lanes. The registers are
 // written asynchronously: read them only through tmem_take() after tmem_ld_wait().
@@ -123,15 +90,6 @@ __device__ __forceinline__ void tmem_ld64_pack16_nowait(uint32_t taddr, uint32_t
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr)
       : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  return static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4) |
-         (static_cast<uint64_t>(1) << 16) |              // leading byte offset (unused here)
-         (static_cast<uint64_t>(1024 >> 4) << 32) |      // stride byte offset
-         (static_cast<uint64_t>(1) << 46) |              // descriptor version (tcgen05)
-         (static_cast<uint64_t>(2) << 61);               // swizzle: 128 B
 }
 
 // Instruction descriptor: D f16, A and B e4m3, both K-major, M = 128, N = n.
@@ -213,8 +171,9 @@ __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
 
 __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) {
   extern __shared__ uint8_t smem_raw[];
-  uint8_t* const smem_base = reinterpret_cast<uint8_t*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  // Align by offsetting the shared array itself so the compiler keeps the shared address
+  // space (an integer round trip would turn every access into a generic one).
+  uint8_t* const smem_base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   Smem& sm = *reinterpret_cast<Smem*>(smem_base);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t N = prm.n_tile;

@@ -97,6 +97,48 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
+// ------------------------------------------------------------- tcgen05 helpers
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4) |
+         (static_cast<uint64_t>(1) << 16) |              // leading byte offset (unused here)
+         (static_cast<uint64_t>(1024 >> 4) << 32) |      // stride byte offset
+         (static_cast<uint64_t>(1) << 46) |              // descriptor version (tcgen05)
+         (static_cast<uint64_t>(2) << 61);               // swizzle: 128 B
+}
+
 // ------------------------------------------------------------- launch plumbing
 
 struct HashLaunch {
@@ -111,6 +153,7 @@ struct HashLaunch {
   int pdqf_slots;
   float* buf1;
   int* dev_err;
+  int dct;  // 0 FP32 SIMT (bit-exact), 1 TF32, 2 BF16x3 tensor cores
 };
 
 struct DihedralLaunch {
@@ -141,6 +184,7 @@ struct ScanLaunch {
 // hash.cu
 cudaError_t upload_constants();
 cudaError_t hash_occupancy(int input_u8, int* ctas_per_sm);
+cudaError_t hash_occupancy_dct(int input_u8, int dct, int* ctas_per_sm);
 cudaError_t launch_hash(const HashLaunch& p, int num_sms, int ctas_per_sm, cudaStream_t s);
 cudaError_t launch_dihedrals(const DihedralLaunch& p, cudaStream_t s);
 
