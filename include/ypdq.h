@@ -22,6 +22,9 @@
  *   ypdq_db_*         VulkanVectorDatabase (src/matching/vulkan.rs:40-65).
  *   ypdq_screen_host  the hash + 8-dihedral match loop of examples/end_to_end.rs:68-140,
  *                     as one call from host buffers.
+ *   ypdq_server_*     the CLI's two-thread read -> hash -> write loop (`pipe`,
+ *                     src/main.rs:391-836, 1091-1304), as a continuous-batching service
+ *                     that hashes and matches requests of any image count.
  */
 #ifndef YPDQ_GB300_H
 #define YPDQ_GB300_H
@@ -45,7 +48,8 @@ typedef enum {
   YPDQ_ERR_NOMEM = 4,     /* device or pinned-host allocation failed */
   YPDQ_ERR_OVERFLOW = 5,  /* more hits than capacity; the count holds the true total */
   YPDQ_ERR_TIMEOUT = 6,   /* a device-side wait ran past its limit and the kernel gave up */
-  YPDQ_ERR_UNSUPPORTED = 7
+  YPDQ_ERR_UNSUPPORTED = 7,
+  YPDQ_ERR_BUSY = 8       /* the server's request queue is full; submit again later */
 } ypdq_status;
 
 /* Input pixel format of 512x512 grayscale images, row-major, values 0..255. */
@@ -224,6 +228,104 @@ ypdq_status ypdq_screen_noalloc(const void *d_images, int64_t n, int input_kind,
                                 const uint8_t *d_rows, uint64_t n_rows, uint32_t threshold,
                                 ypdq_hit *d_hits, uint64_t capacity, uint64_t *d_count,
                                 ypdq_stream_t stream);
+
+/* ------------------------------------------------------------ serving loop */
+
+/*
+ * A continuous-batching screening service over one device-resident database. Each request
+ * carries 1..max_step_images images; the server hashes them (8 dihedrals each) and matches
+ * every hash exactly against the database, like ypdq_screen_host on that request alone.
+ *
+ * Device steps. A worker thread packs waiting requests, oldest first, into a device step
+ * of at most max_step_images images and launches it as soon as a step slot is free. Each
+ * slot owns the device memory of one step (images, hashes, hits) and its own stream, so
+ * up to `slots` steps are on the device at once: the image copy of one step overlaps the
+ * hash and scan of another. A step replays a CUDA graph captured for the smallest batch
+ * bucket (a power of two) that holds its images; the graph reads the step's image count
+ * from device memory, so one graph serves every count up to its bucket.
+ *
+ * Admission by memory. The slots are sized at creation from the device memory the server
+ * may take (device_bytes), so requests join the device exactly as slots and their memory
+ * free up. Requests wait in a host queue before that; the queue holds at most
+ * max_queued_images images, and a submit beyond that returns YPDQ_ERR_BUSY.
+ *
+ * Results. A request's hits are sorted by (database index, query) with query numbers local
+ * to the request (image i, slot s -> 8 i + s) and are identical to those of the same images
+ * screened alone. Hits past the step's device capacity are recovered by an exact re-scan.
+ */
+typedef struct ypdq_server ypdq_server;
+
+typedef struct {
+  int input_kind;              /* ypdq_input_kind */
+  int dct_precision;           /* ypdq_dct_precision */
+  int semantics;               /* ypdq_dihedral_semantics */
+  uint32_t threshold;          /* Hamming distance bound, <= 256 */
+  uint32_t max_step_images;    /* largest batch bucket, a power of two; 0 -> 1024 */
+  uint32_t slots;              /* device steps in flight at most; 0 -> 3 */
+  uint64_t step_hit_capacity;  /* hits a step keeps on the device; 0 -> 1 << 20 */
+  uint64_t device_bytes;       /* device memory for all slots; 0 -> half the free memory */
+  uint64_t max_queued_images;  /* host queue bound in images; 0 -> 4 x max_step_images */
+  int autotune;                /* nonzero: time each bucket's scan variants at creation
+                                  and keep the fastest per bucket */
+  double target_step_ms;       /* with autotune: largest bucket kept is the biggest whose
+                                  step takes at most this long; 0 -> no bound */
+} ypdq_server_config;
+
+typedef struct {
+  uint64_t request_id;
+  uint64_t user_tag;
+  int32_t status;      /* YPDQ_OK, YPDQ_ERR_OVERFLOW (more hits than hit_capacity: the first
+                          hit_capacity in order were written), or the step's error */
+  uint32_t n_images;
+  uint64_t n_hits;     /* the request's true number of hits */
+  uint64_t step;       /* sequence number of the device step that carried the request */
+  double latency_us;   /* from ypdq_server_submit to the completion being posted */
+} ypdq_completion;
+
+#define YPDQ_SERVER_MAX_BUCKETS 16
+
+typedef struct {
+  uint64_t submitted, rejected, completed;
+  uint64_t images_completed, hits_completed, steps, rescans;
+  uint32_t queued_requests, queued_images, inflight_steps, slots;
+  uint32_t max_step_images;
+  double p50_us, p99_us, mean_us, max_us;  /* latency of the requests completed since reset */
+  double mean_step_images;
+  double elapsed_s;                         /* since creation or the last reset */
+  uint32_t n_buckets;
+  uint32_t bucket_images[YPDQ_SERVER_MAX_BUCKETS];
+  int32_t bucket_algo[YPDQ_SERVER_MAX_BUCKETS];     /* ypdq_scan_algo the bucket's graph uses */
+  uint32_t bucket_n_tile[YPDQ_SERVER_MAX_BUCKETS];  /* tensor-core queries per pass (0: SIMT) */
+  float bucket_ms[YPDQ_SERVER_MAX_BUCKETS];         /* step time measured by the autotuner */
+  uint64_t bucket_steps[YPDQ_SERVER_MAX_BUCKETS];   /* steps launched per bucket */
+} ypdq_server_stats;
+
+/* Fills cfg with the defaults above (threshold 31, f32 input, FP32 DCT, exact semantics). */
+ypdq_status ypdq_server_config_default(ypdq_server_config *cfg);
+/* Creates the slots, captures the bucket graphs and starts the worker thread. The database
+ * must outlive the server. */
+ypdq_status ypdq_server_create(ypdq_ctx *ctx, ypdq_db *db, const ypdq_server_config *cfg,
+                               ypdq_server **out);
+/*
+ * Queues one request. h_images (n_images x 512 x 512 of the configured input kind; pinned
+ * memory copies fastest) must stay valid until the completion is polled. h_hits (hit_capacity
+ * entries), h_hashes (n_images x 8 x 32 bytes) and h_quality (n_images x 8 floats) are written
+ * before the completion is posted; each may be NULL. Returns YPDQ_ERR_BUSY (and counts a
+ * rejection) when the queue is full, YPDQ_ERR_INVALID for n_images outside
+ * 1..max_step_images. Thread-safe.
+ */
+ypdq_status ypdq_server_submit(ypdq_server *srv, const void *h_images, uint32_t n_images,
+                               ypdq_hit *h_hits, uint64_t hit_capacity, uint8_t *h_hashes,
+                               float *h_quality, uint64_t user_tag, uint64_t *request_id);
+/* Takes up to max completions, waiting up to timeout_us (0: no wait, < 0: until at least one
+ * is there or nothing is pending). Thread-safe. */
+ypdq_status ypdq_server_poll(ypdq_server *srv, ypdq_completion *out, uint32_t max,
+                             uint32_t *n_out, int64_t timeout_us);
+/* Latency percentiles, counters and the bucket table; reset != 0 starts a new window. */
+ypdq_status ypdq_server_get_stats(ypdq_server *srv, ypdq_server_stats *out, int reset);
+/* Finishes every queued and in-flight request, stops the worker and frees the slots.
+ * Completions not yet polled are dropped. */
+ypdq_status ypdq_server_destroy(ypdq_server *srv);
 
 /* -------------------------------------------------------- synthetic workloads */
 

@@ -89,3 +89,67 @@ def test_plant_distances_exact(yp):
     pos, qid, dist = yp.synth.plant(rows, q, 50, 0, 40, seed=4)
     d = np.unpackbits(rows[pos] ^ q[qid], axis=1).sum(1)
     assert np.array_equal(d, dist)
+
+
+def test_server_config_default_and_argument_checks(yp):
+    """ypdq_server_config_default is host-only; create/submit/poll reject NULL handles."""
+    lib = yp._lib.load()
+    cfg = yp._lib.ServerConfig()
+    assert lib.ypdq_server_config_default(ctypes.byref(cfg)) == yp._lib.OK
+    assert (cfg.threshold, cfg.max_step_images, cfg.slots) == (31, 1024, 3)
+    assert (cfg.input_kind, cfg.dct_precision, cfg.semantics) == (0, 0, 0)
+    assert cfg.step_hit_capacity == 1 << 20 and cfg.autotune == 0
+    assert lib.ypdq_server_config_default(None) == yp._lib.ERR_INVALID
+    out = ctypes.c_void_p()
+    assert lib.ypdq_server_create(None, None, ctypes.byref(cfg), ctypes.byref(out)) == yp._lib.ERR_INVALID
+    n = ctypes.c_uint32()
+    assert lib.ypdq_server_poll(None, None, 0, ctypes.byref(n), 0) == yp._lib.ERR_INVALID
+    assert lib.ypdq_server_submit(None, None, 1, None, 0, None, None, 0, None) == yp._lib.ERR_INVALID
+    assert lib.ypdq_server_destroy(None) == yp._lib.ERR_INVALID
+
+
+LAYOUT_PROBE = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include "ypdq.h"
+#define F(T, m) printf(#T " " #m " %zu\n", offsetof(T, m))
+int main(void) {
+  printf("ypdq_server_config size %zu\n", sizeof(ypdq_server_config));
+  printf("ypdq_completion size %zu\n", sizeof(ypdq_completion));
+  printf("ypdq_server_stats size %zu\n", sizeof(ypdq_server_stats));
+  printf("ypdq_hit size %zu\n", sizeof(ypdq_hit));
+  F(ypdq_server_config, target_step_ms); F(ypdq_server_config, autotune);
+  F(ypdq_completion, latency_us); F(ypdq_completion, n_hits);
+  F(ypdq_server_stats, p50_us); F(ypdq_server_stats, n_buckets);
+  F(ypdq_server_stats, bucket_ms); F(ypdq_server_stats, bucket_steps);
+  return 0;
+}
+"""
+
+
+def test_struct_layouts_match_header(yp, tmp_path):
+    """The ctypes mirrors of the server structs have the C compiler's layout of include/ypdq.h."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    src = tmp_path / "probe.c"
+    src.write_text(LAYOUT_PROBE)
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        t, m, v = line.split()
+        got[(t, m)] = int(v)
+    L = yp._lib
+    mirrors = {"ypdq_server_config": L.ServerConfig, "ypdq_completion": L.Completion,
+               "ypdq_server_stats": L.ServerStats}
+    for (t, m), v in got.items():
+        if t == "ypdq_hit":
+            assert v == L.HIT_DTYPE.itemsize
+        elif m == "size":
+            assert ctypes.sizeof(mirrors[t]) == v, t
+        else:
+            assert getattr(mirrors[t], m).offset == v, (t, m)

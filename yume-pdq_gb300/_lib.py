@@ -14,10 +14,11 @@ LIB_PATH = _build.LIB_PATH
 
 HIT_DTYPE = np.dtype([("index", "<u8"), ("query", "<u4"), ("distance", "<u4")])
 
-OK, ERR_INVALID, ERR_ALIGN, ERR_CUDA, ERR_NOMEM, ERR_OVERFLOW, ERR_TIMEOUT, ERR_UNSUPPORTED = range(8)
+(OK, ERR_INVALID, ERR_ALIGN, ERR_CUDA, ERR_NOMEM, ERR_OVERFLOW, ERR_TIMEOUT, ERR_UNSUPPORTED,
+ ERR_BUSY) = range(9)
 STATUS_NAMES = {
     0: "OK", 1: "INVALID", 2: "ALIGN", 3: "CUDA", 4: "NOMEM", 5: "OVERFLOW", 6: "TIMEOUT",
-    7: "UNSUPPORTED",
+    7: "UNSUPPORTED", 8: "BUSY",
 }
 
 INPUT_F32, INPUT_U8 = 0, 1
@@ -32,6 +33,46 @@ class YpdqError(RuntimeError):
     def __init__(self, status, message):
         super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
         self.status = status
+
+
+SERVER_MAX_BUCKETS = 16
+
+
+class ServerConfig(ctypes.Structure):
+    """ypdq_server_config."""
+    _fields_ = [("input_kind", ctypes.c_int), ("dct_precision", ctypes.c_int),
+                ("semantics", ctypes.c_int), ("threshold", ctypes.c_uint32),
+                ("max_step_images", ctypes.c_uint32), ("slots", ctypes.c_uint32),
+                ("step_hit_capacity", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64),
+                ("max_queued_images", ctypes.c_uint64), ("autotune", ctypes.c_int),
+                ("target_step_ms", ctypes.c_double)]
+
+
+class Completion(ctypes.Structure):
+    """ypdq_completion."""
+    _fields_ = [("request_id", ctypes.c_uint64), ("user_tag", ctypes.c_uint64),
+                ("status", ctypes.c_int32), ("n_images", ctypes.c_uint32),
+                ("n_hits", ctypes.c_uint64), ("step", ctypes.c_uint64),
+                ("latency_us", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    """ypdq_server_stats."""
+    _fields_ = [("submitted", ctypes.c_uint64), ("rejected", ctypes.c_uint64),
+                ("completed", ctypes.c_uint64), ("images_completed", ctypes.c_uint64),
+                ("hits_completed", ctypes.c_uint64), ("steps", ctypes.c_uint64),
+                ("rescans", ctypes.c_uint64), ("queued_requests", ctypes.c_uint32),
+                ("queued_images", ctypes.c_uint32), ("inflight_steps", ctypes.c_uint32),
+                ("slots", ctypes.c_uint32), ("max_step_images", ctypes.c_uint32),
+                ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double),
+                ("mean_us", ctypes.c_double), ("max_us", ctypes.c_double),
+                ("mean_step_images", ctypes.c_double), ("elapsed_s", ctypes.c_double),
+                ("n_buckets", ctypes.c_uint32),
+                ("bucket_images", ctypes.c_uint32 * SERVER_MAX_BUCKETS),
+                ("bucket_algo", ctypes.c_int32 * SERVER_MAX_BUCKETS),
+                ("bucket_n_tile", ctypes.c_uint32 * SERVER_MAX_BUCKETS),
+                ("bucket_ms", ctypes.c_float * SERVER_MAX_BUCKETS),
+                ("bucket_steps", ctypes.c_uint64 * SERVER_MAX_BUCKETS)]
 
 
 # name -> (restype, argtypes); the exported surface of include/*.h
@@ -70,6 +111,13 @@ SIGNATURES = {
     "ypdq_synth_rows": (i32, [P, P, u64, u64, u64, P]),
     "ypdq_constants": (i32, [P, P]),
     "ypdq_screen_noalloc": (i32, [P, i64, i32, i32, P, u64, u32, P, u64, P, P]),
+    "ypdq_server_config_default": (i32, [ctypes.POINTER(ServerConfig)]),
+    "ypdq_server_create": (i32, [P, P, ctypes.POINTER(ServerConfig), PP]),
+    "ypdq_server_submit": (i32, [P, P, u32, P, u64, P, P, u64, ctypes.POINTER(ctypes.c_uint64)]),
+    "ypdq_server_poll": (i32, [P, ctypes.POINTER(Completion), u32, ctypes.POINTER(ctypes.c_uint32),
+                               i64]),
+    "ypdq_server_get_stats": (i32, [P, ctypes.POINTER(ServerStats), i32]),
+    "ypdq_server_destroy": (i32, [P]),
     "yume_pdq_hash_smart_kernel": (f32, [P, P, P, P, P, P]),
     "yume_pdq_visit_dihedrals_smart_kernel": (ctypes.c_bool, [P, f32, P, P, P]),
 }

@@ -7,38 +7,18 @@
 #include <mutex>
 #include <string>
 
+#include "capi_internal.h"
 #include "ypdq_internal.cuh"
 #include "ypdq_tables.h"
 #include "yume_pdq.h"
 
 using namespace ypdq;
 
-struct ypdq_ctx {
-  int device = 0;
-  int num_sms = 0;
-  int hash_ctas_f32 = 1;
-  int hash_ctas_u8 = 1;
-  int hash_ctas[2][3] = {{1, 1, 1}, {1, 1, 1}};  // [input u8][dct precision]
-  int* d_err = nullptr;
-  cudaStream_t stream = nullptr;       // compute stream of the blocking _host calls
-  cudaStream_t copy_stream = nullptr;  // host->device copies that overlap that compute
-  static constexpr int kMaxChunks = 8;
-  cudaEvent_t chunk_copied[kMaxChunks] = {};
-  std::mutex mu;                  // guards the scratch buffers below
-  void* scratch[8] = {};
-  size_t scratch_bytes[8] = {};
-};
-
-struct ypdq_db {
-  ypdq_ctx* ctx;
-  const uint8_t* d_rows;
-  uint64_t n_rows;
-  bool owned;
-};
-
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
+
+namespace ypdq {
 
 ypdq_status fail(ypdq_status st, const char* fmt, ...) {
   char buf[512];
@@ -56,14 +36,6 @@ ypdq_status cuda_fail(cudaError_t e, const char* what) {
   return fail(YPDQ_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define CK(call, what)                       \
-  do {                                       \
-    cudaError_t e_ = (call);                 \
-    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-  } while (0)
-
-bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
-
 void semantics_masks(int sem, uint32_t* rm, uint32_t* cm) {
   switch (sem) {
     case YPDQ_DIHEDRAL_AVX2:
@@ -80,6 +52,12 @@ void semantics_masks(int sem, uint32_t* rm, uint32_t* cm) {
       break;
   }
 }
+
+}  // namespace ypdq
+
+namespace {
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 // Grow-only scratch buffer `slot` of ctx to at least `bytes`. Caller holds ctx->mu.
 ypdq_status scratch(ypdq_ctx* ctx, int slot, size_t bytes, void** out) {

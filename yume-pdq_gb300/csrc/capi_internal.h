@@ -1,0 +1,50 @@
+// Internal C++ view of the C ABI's opaque handles, shared by the translation units that
+// implement include/ypdq.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+
+#include "ypdq.h"
+
+struct ypdq_ctx {
+  int device = 0;
+  int num_sms = 0;
+  int hash_ctas_f32 = 1;
+  int hash_ctas_u8 = 1;
+  int hash_ctas[2][3] = {{1, 1, 1}, {1, 1, 1}};  // [input u8][dct precision]
+  int* d_err = nullptr;
+  cudaStream_t stream = nullptr;       // compute stream of the blocking _host calls
+  cudaStream_t copy_stream = nullptr;  // host->device copies that overlap that compute
+  static constexpr int kMaxChunks = 8;
+  cudaEvent_t chunk_copied[kMaxChunks] = {};
+  std::mutex mu;                  // guards the scratch buffers below
+  void* scratch[8] = {};
+  size_t scratch_bytes[8] = {};
+};
+
+struct ypdq_db {
+  ypdq_ctx* ctx;
+  const uint8_t* d_rows;
+  uint64_t n_rows;
+  bool owned;
+};
+
+namespace ypdq {
+
+// Record a formatted message for ypdq_last_error() on the calling thread; returns st.
+ypdq_status fail(ypdq_status st, const char* fmt, ...);
+// Map a CUDA error to YPDQ_ERR_NOMEM or YPDQ_ERR_CUDA with its text.
+ypdq_status cuda_fail(cudaError_t e, const char* what);
+// Row and column sign masks of the dihedral derivation for a ypdq_dihedral_semantics.
+void semantics_masks(int sem, uint32_t* rm, uint32_t* cm);
+
+}  // namespace ypdq
+
+#define CK(call, what)                                           \
+  do {                                                           \
+    cudaError_t e_ = (call);                                     \
+    if (e_ != cudaSuccess) return ::ypdq::cuda_fail(e_, what);   \
+  } while (0)

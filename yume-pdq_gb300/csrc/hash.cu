@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(hash_threads<kDct>()) hash_kernel(const HashLa
   if constexpr (kDct != 0) tc_fence_after();
 
   volatile int* abort_flag = &sm.abort_flag;
-  const int64_t n_images = prm.n;
+  const int64_t n_images = prm.n_dev ? min(*prm.n_dev, prm.n) : prm.n;
   const unsigned char* images = static_cast<const unsigned char*>(prm.images);
   constexpr int64_t kImageBytes = 512ll * kRowBytes;
 

@@ -52,8 +52,10 @@ __device__ __forceinline__ uint4 ld_stream(const uint4* p) {
 __global__ void __launch_bounds__(kScanThreads)
     scan_simt_kernel(const uint4* __restrict__ rows, uint64_t n_rows,
                      const uint4* __restrict__ queries, uint32_t nq, uint32_t q_base,
-                     uint32_t t, ypdq_hit* hits, uint64_t cap, unsigned long long* count) {
+                     uint32_t t, ypdq_hit* hits, uint64_t cap, unsigned long long* count,
+                     const uint32_t* nq_dev) {
   extern __shared__ uint4 sq[];
+  if (nq_dev) nq = min(*nq_dev, nq);
   for (uint32_t i = threadIdx.x; i < 2 * nq; i += blockDim.x) sq[i] = queries[i];
   __syncthreads();
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
@@ -157,6 +159,9 @@ cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t
   // SIMT is HBM-bound up to a few queries and beats the tensor-core pipeline up to ~16.
   if (algo == YPDQ_SCAN_AUTO) algo = p.n_queries <= 16 ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;
   if (algo == YPDQ_SCAN_TC) return launch_scan_tc(p, num_sms, s);
+  // a device-side query count needs the whole query set in one launch
+  if (p.nq_dev && (algo != YPDQ_SCAN_SIMT || p.n_queries > kMaxSmemQueries))
+    return cudaErrorInvalidValue;
   for (uint32_t q0 = 0; q0 < p.n_queries; q0 += kMaxSmemQueries) {
     const uint32_t nq = (p.n_queries - q0) < kMaxSmemQueries ? (p.n_queries - q0) : kMaxSmemQueries;
     const uint8_t* qptr = p.queries + static_cast<size_t>(q0) * 32;
@@ -176,7 +181,7 @@ cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t
       const size_t smem = static_cast<size_t>(nq) * 32;
       scan_simt_kernel<<<static_cast<unsigned>(blocks), kScanThreads, smem, s>>>(
           reinterpret_cast<const uint4*>(p.rows), p.n_rows, reinterpret_cast<const uint4*>(qptr),
-          nq, p.query_base + q0, p.threshold, p.hits, p.capacity, p.count);
+          nq, p.query_base + q0, p.threshold, p.hits, p.capacity, p.count, p.nq_dev);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;

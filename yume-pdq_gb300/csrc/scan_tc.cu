@@ -138,14 +138,16 @@ struct Params {
   unsigned long long* count;
   int* dev_err;
   uint32_t query_base;    // added to reported query numbers
+  const uint32_t* nq_dev; // device-side query count (graph replay), bounded by n_queries
   uint32_t pack_stages;   // packed tiles in flight (<= kMaxPackStages)
   uint32_t pack_offset;   // byte offset of the packed ring in shared memory
 };
 
 // Compact one column of hits across the warp (one atomic per warp with a hit).
 __device__ __forceinline__ void emit_hit(bool row_ok, uint64_t row, uint64_t q, float v,
-                                         float dot_min, const Params& prm, int lane) {
-  const bool hit = row_ok && q < prm.n_queries && v >= dot_min;
+                                         float dot_min, const Params& prm, int lane,
+                                         uint32_t n_queries) {
+  const bool hit = row_ok && q < n_queries && v >= dot_min;
   const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
   if (ballot == 0) return;
   const int leader = __ffs(ballot) - 1;
@@ -178,11 +180,12 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t N = prm.n_tile;
   const uint32_t n_pack = prm.pack_stages;
+  const uint32_t n_queries = prm.nq_dev ? min(*prm.nq_dev, prm.n_queries) : prm.n_queries;
   uint8_t* const bchunk0 = smem_base + kBOffset;      // N rows x 128 B (K 0..127)
   uint8_t* const bchunk1 = bchunk0 + N * 128;         // N rows x 128 B (K 128..255)
   uint8_t* const packed = smem_base + prm.pack_offset;
   const uint64_t n_tiles = (prm.n_rows + kTileRows - 1) / kTileRows;
-  const uint32_t n_passes = (prm.n_queries + N - 1) / N;
+  const uint32_t n_passes = (n_queries + N - 1) / N;
   // tiles of this CTA: blockIdx.x, blockIdx.x + gridDim.x, ...
   const uint64_t my_tiles =
       blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
@@ -270,7 +273,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
       if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag)) goto fail;
       for (uint32_t qr = e; qr < N; qr += 128) {
         const uint64_t qi = static_cast<uint64_t>(p) * N + qr;
-        if (qi < prm.n_queries) {
+        if (qi < n_queries) {
           const uint4* src = reinterpret_cast<const uint4*>(prm.queries + qi * 32);
           expand_row(src[0], src[1], bchunk0, bchunk1, static_cast<int>(qr));
         } else {
@@ -399,8 +402,9 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const __half2 h2 = *reinterpret_cast<const __half2*>(&raw[j]);
-              emit_hit(row_ok, row, q0 + c0 + 2 * j, __low2float(h2), dot_min, prm, lane);
-              emit_hit(row_ok, row, q0 + c0 + 2 * j + 1, __high2float(h2), dot_min, prm, lane);
+              emit_hit(row_ok, row, q0 + c0 + 2 * j, __low2float(h2), dot_min, prm, lane, n_queries);
+              emit_hit(row_ok, row, q0 + c0 + 2 * j + 1, __high2float(h2), dot_min, prm, lane,
+                       n_queries);
             }
           }
         }
@@ -432,12 +436,18 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   // N is a multiple of 64 so every 64-column TMEM load stays inside one accumulator.
   uint32_t n = (p.n_queries + 63u) & ~63u;
   prm.n_tile = n > static_cast<uint32_t>(tc::kMaxN) ? static_cast<uint32_t>(tc::kMaxN) : n;
+  if (p.n_tile) {
+    if (p.n_tile % 64u != 0 || p.n_tile > static_cast<uint32_t>(tc::kMaxN))
+      return cudaErrorInvalidValue;
+    prm.n_tile = p.n_tile;
+  }
   prm.threshold = p.threshold;
   prm.hits = p.hits;
   prm.capacity = p.capacity;
   prm.count = p.count;
   prm.dev_err = p.dev_err;
   prm.query_base = p.query_base;
+  prm.nq_dev = p.nq_dev;
   // layout: [fixed Smem][B: 2 x N x 128][packed ring: stages x 4 KB], base aligned to 1024
   const size_t b_end = tc::kBOffset + 2 * static_cast<size_t>(prm.n_tile) * 128;
   const size_t avail = tc::kSmemLimit - 1024 - b_end;

@@ -154,6 +154,7 @@ struct HashLaunch {
   float* buf1;
   int* dev_err;
   int dct;  // 0 FP32 SIMT (bit-exact), 1 TF32, 2 BF16x3 tensor cores
+  const int64_t* n_dev;  // if set, the image count is read from here (graph replay); n is the bound
 };
 
 struct DihedralLaunch {
@@ -179,6 +180,10 @@ struct ScanLaunch {
   int* dev_err;
   int append;            // nonzero: add to *count instead of resetting it first
   uint32_t query_base;   // added to every reported query number
+  const uint32_t* nq_dev;  // if set, the query count is read from here when the kernel runs
+                           // (graph replay); n_queries is then its upper bound
+  uint32_t n_tile;         // tensor-core scan: queries per pass (multiple of 64, <= 256);
+                           // 0 picks min(256, n_queries rounded up to 64)
 };
 
 // hash.cu
