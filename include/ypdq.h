@@ -337,6 +337,17 @@ ypdq_status ypdq_server_destroy(ypdq_server *srv);
 ypdq_status ypdq_synth_rows(ypdq_ctx *ctx, uint8_t *d_rows, uint64_t n_rows, uint64_t first_row,
                             uint64_t seed, ypdq_stream_t stream);
 
+/*
+ * Clustered rows: global row g = first_row + r is a member of centre c = g /
+ * members_per_centre, where centre c is row c of ypdq_synth_rows for the same seed (128 set
+ * bits). The member flips d distinct bits of its centre, d ~ Binomial(flip_trials, 1/2)
+ * (flip_trials <= 64; 40 gives a distance around 20). Row g depends only on (seed, g,
+ * members_per_centre, flip_trials).
+ */
+ypdq_status ypdq_synth_clustered_rows(ypdq_ctx *ctx, uint8_t *d_rows, uint64_t n_rows,
+                                      uint64_t first_row, uint64_t members_per_centre,
+                                      uint32_t flip_trials, uint64_t seed, ypdq_stream_t stream);
+
 /* The f32 DCT matrix (16 x 127) and tent weights (7 x 7) compiled into the library. */
 ypdq_status ypdq_constants(float *h_dct16x127, float *h_tent7x7);
 

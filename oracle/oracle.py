@@ -57,6 +57,8 @@ def lib():
             "ypdqo_count_all": (i64, [P, i64, P, i32, u32, i32]),
             "ypdqo_fm_sine_image": (None, [P]),
             "ypdqo_synth_rows": (None, [P, i64, ctypes.c_uint64, ctypes.c_uint64, i32]),
+            "ypdqo_synth_clustered": (None, [P, i64, ctypes.c_uint64, ctypes.c_uint64,
+                                             ctypes.c_uint32, ctypes.c_uint64, i32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -210,4 +212,12 @@ def synth_rows(n, seed, first=0, nthreads=None):
     """CPU twin of the library's ypdq_synth_rows (identical rows for the same seed)."""
     out = np.empty((n, 32), np.uint8)
     lib().ypdqo_synth_rows(_p(out), n, first, seed, nthreads or os.cpu_count() or 1)
+    return out
+
+
+def synth_clustered(n, members, trials, seed, first=0, nthreads=None):
+    """CPU twin of the library's ypdq_synth_clustered_rows (identical rows)."""
+    out = np.empty((n, 32), np.uint8)
+    lib().ypdqo_synth_clustered(_p(out), n, first, members, trials, seed,
+                                nthreads or os.cpu_count() or 1)
     return out

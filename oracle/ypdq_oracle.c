@@ -552,3 +552,45 @@ YPDQO_EXPORT void ypdqo_synth_rows(uint8_t* out, int64_t n, uint64_t first, uint
   synth_ctx c = {(uint64_t*)out, first, seed};
   parallel_ranges(synth_range, &c, n, nthreads);
 }
+
+/* Clustered rows (CPU twin of ypdq_synth_clustered_rows): global row g is centre
+ * g / members (row g / members of the generator above) with d distinct bits flipped,
+ * d = popcount of `trials` bits of a second splitmix64 stream, positions from the same
+ * stream, duplicates redrawn. */
+typedef struct {
+  uint64_t* out;
+  uint64_t first, members, seed;
+  uint32_t trials;
+} clustered_ctx;
+
+static void clustered_range(void* vctx, int64_t b, int64_t e) {
+  clustered_ctx* c = (clustered_ctx*)vctx;
+  for (int64_t r = b; r < e; r++) {
+    const uint64_t g = c->first + (uint64_t)r;
+    uint64_t w[4];
+    synth_ctx one = {w, g / c->members, c->seed};
+    synth_range(&one, 0, 1);
+    uint64_t state = mix64((c->seed ^ 0xC13FA9A902A6328Full) ^ mix64(g + 0x632BE59BD9B4E019ull));
+    state += 0x9E3779B97F4A7C15ull;
+    const uint64_t mask = c->trials >= 64 ? ~0ull : ((1ull << c->trials) - 1);
+    const int d = __builtin_popcountll(mix64(state) & mask);
+    uint64_t f[4] = {0, 0, 0, 0};
+    for (int k = 0; k < d;) {
+      state += 0x9E3779B97F4A7C15ull;
+      const uint32_t pos = (uint32_t)(mix64(state) & 255u);
+      const uint64_t bit = 1ull << (pos & 63);
+      if (!(f[pos >> 6] & bit)) {
+        f[pos >> 6] |= bit;
+        k++;
+      }
+    }
+    for (int k = 0; k < 4; k++) w[k] ^= f[k];
+    memcpy(c->out + r * 4, w, 32);
+  }
+}
+
+YPDQO_EXPORT void ypdqo_synth_clustered(uint8_t* out, int64_t n, uint64_t first, uint64_t members,
+                                        uint32_t trials, uint64_t seed, int nthreads) {
+  clustered_ctx c = {(uint64_t*)out, first, members, seed, trials};
+  parallel_ranges(clustered_range, &c, n, nthreads);
+}

@@ -171,3 +171,17 @@ def test_find_all_order_and_threads(oracle, yp):
     # distances are the exact popcounts
     d = np.unpackbits(rows[a["index"]] ^ q[a["query"]], axis=1).sum(1)
     assert np.array_equal(d, a["distance"])
+
+
+def test_clustered_rows_twin(oracle):
+    """Clustered workload rows: member g of centre g // members sits at Hamming distance
+    d ~ Binomial(trials, 1/2) from centre row g // members of the 128-bit generator."""
+    members, trials, seed = 1000, 40, 77
+    rows = oracle.synth_clustered(20_000, members, trials, seed, first=3_000_000)
+    centres = oracle.synth_rows(20, seed, first=3_000)
+    d = np.unpackbits(rows ^ np.repeat(centres, members, axis=0), axis=1).sum(1)
+    assert d.max() <= trials and abs(d.mean() - trials / 2) < 0.2
+    assert abs(d.std() - np.sqrt(trials) / 2) < 0.2
+    # rows are a pure function of the global row number
+    again = oracle.synth_clustered(100, members, trials, seed, first=3_000_000 + 500)
+    assert np.array_equal(again, rows[500:600])

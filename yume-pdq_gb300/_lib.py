@@ -109,6 +109,7 @@ SIGNATURES = {
     "ypdq_event_record": (i32, [P, P, P]),
     "ypdq_event_elapsed_ms": (i32, [P, P, P, ctypes.POINTER(ctypes.c_float)]),
     "ypdq_synth_rows": (i32, [P, P, u64, u64, u64, P]),
+    "ypdq_synth_clustered_rows": (i32, [P, P, u64, u64, u64, u32, u64, P]),
     "ypdq_constants": (i32, [P, P]),
     "ypdq_screen_noalloc": (i32, [P, i64, i32, i32, P, u64, u32, P, u64, P, P]),
     "ypdq_server_config_default": (i32, [ctypes.POINTER(ServerConfig)]),

@@ -510,6 +510,21 @@ ypdq_status ypdq_synth_rows(ypdq_ctx* ctx, uint8_t* d_rows, uint64_t n_rows, uin
   return YPDQ_OK;
 }
 
+ypdq_status ypdq_synth_clustered_rows(ypdq_ctx* ctx, uint8_t* d_rows, uint64_t n_rows,
+                                      uint64_t first_row, uint64_t members_per_centre,
+                                      uint32_t flip_trials, uint64_t seed, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (n_rows > 0 && !d_rows) return fail(YPDQ_ERR_INVALID, "d_rows is NULL");
+  if (!aligned16(d_rows)) return fail(YPDQ_ERR_ALIGN, "d_rows must be 16-byte aligned");
+  if (members_per_centre == 0) return fail(YPDQ_ERR_INVALID, "members_per_centre is 0");
+  if (flip_trials > 64) return fail(YPDQ_ERR_INVALID, "flip_trials %u > 64", flip_trials);
+  CK(launch_synth_clustered(d_rows, n_rows, first_row, members_per_centre, flip_trials, seed,
+                            reinterpret_cast<cudaStream_t>(stream)),
+     "synth launch");
+  return YPDQ_OK;
+}
+
 // ------------------------------------------------------------ drop-in ABI
 
 __attribute__((visibility("default"))) const uint32_t YUME_PDQ_VERSION_MAJOR = 1;

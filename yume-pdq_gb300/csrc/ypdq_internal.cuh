@@ -205,5 +205,7 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s);
 // synth.cu
 cudaError_t launch_synth_rows(uint8_t* rows, uint64_t n, uint64_t first, uint64_t seed,
                               cudaStream_t s);
+cudaError_t launch_synth_clustered(uint8_t* rows, uint64_t n, uint64_t first, uint64_t members,
+                                   uint32_t trials, uint64_t seed, cudaStream_t s);
 
 }  // namespace ypdq
