@@ -115,6 +115,10 @@ const char *ypdq_last_error(void);
 ypdq_status ypdq_check_device_errors(ypdq_ctx *ctx);
 /* Number of SMs and the hash kernel's resident CTAs per SM (for sizing batches). */
 ypdq_status ypdq_device_info(ypdq_ctx *ctx, int *num_sms, int *hash_ctas_per_sm);
+/* CTAs per SM the hash kernel of this input kind and DCT precision runs with (its grid is
+ * that many per SM, persistent over the images). */
+ypdq_status ypdq_hash_occupancy(ypdq_ctx *ctx, int input_kind, int dct_precision,
+                                int *ctas_per_sm);
 
 /* ------------------------------------------------------------------ hashing */
 

@@ -86,6 +86,7 @@ SIGNATURES = {
     "ypdq_last_error": (ctypes.c_char_p, []),
     "ypdq_check_device_errors": (i32, [P]),
     "ypdq_device_info": (i32, [P, P, P]),
+    "ypdq_hash_occupancy": (i32, [P, i32, i32, ctypes.POINTER(ctypes.c_int)]),
     "ypdq_hash_batch": (i32, [P, P, i64, i32, i32, i32, P, P, P, P, i32, P, P]),
     "ypdq_dihedrals_batch": (i32, [P, P, P, i64, i32, P, P, P, P, P]),
     "ypdq_scan": (i32, [P, P, u64, P, u32, u32, P, u64, P, i32, P]),

@@ -163,6 +163,19 @@ ypdq_status ypdq_check_device_errors(ypdq_ctx* ctx) {
   return read_device_errors(ctx);
 }
 
+ypdq_status ypdq_hash_occupancy(ypdq_ctx* ctx, int input_kind, int dct_precision,
+                                int* ctas_per_sm) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (!ctas_per_sm) return fail(YPDQ_ERR_INVALID, "ctas_per_sm is NULL");
+  if (input_kind != YPDQ_INPUT_F32 && input_kind != YPDQ_INPUT_U8)
+    return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
+  if (dct_precision < YPDQ_DCT_FP32 || dct_precision > YPDQ_DCT_BF16X3)
+    return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
+  *ctas_per_sm = ctx->hash_ctas[input_kind][dct_precision];
+  return YPDQ_OK;
+}
+
 ypdq_status ypdq_device_info(ypdq_ctx* ctx, int* num_sms, int* hash_ctas_per_sm) {
   if (!ctx) return fail(YPDQ_ERR_INVALID, "ctx is NULL");
   if (num_sms) *num_sms = ctx->num_sms;

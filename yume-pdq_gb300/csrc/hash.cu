@@ -36,7 +36,6 @@ namespace ypdq {
 
 __device__ float g_dct[16 * 127];  // D[k][i] = sqrt(2/127) cos(pi (k+1) (2i+1) / 254), f32
 
-constexpr int kNumStages = 8;
 constexpr int kStagesPerImage = 128;  // stage s holds rows 4s+1 .. 4s+4 (stage 127: 509, 510)
 constexpr int kComputeThreads = 128;
 constexpr int kProducerWarp = 4;
@@ -44,6 +43,25 @@ constexpr int kEpilogueWarp = 5;
 constexpr int kMmaWarpHash = 6;   // tensor-core DCT only: allocates TMEM, issues the MMAs
 template <int kDct>
 constexpr int hash_threads() { return kDct == 0 ? 192 : 224; }
+// Depth of the input ring (4-row stages). The tensor-core variants with f32 input use 6
+// stages so that two CTAs fit on an SM next to their operand buffers.
+#ifndef YPDQ_RING_U8
+#define YPDQ_RING_U8 8
+#endif
+#ifndef YPDQ_RING_U8_TC
+#define YPDQ_RING_U8_TC 16
+#endif
+#ifndef YPDQ_U8_TC_CTAS
+#define YPDQ_U8_TC_CTAS 2
+#endif
+template <typename Tin, int kDct>
+constexpr int ring_stages() {
+  return sizeof(Tin) == 4 ? (kDct != 0 ? 6 : 8) : (kDct != 0 ? YPDQ_RING_U8_TC : YPDQ_RING_U8);
+}
+// The tensor-core variants need no DCT accumulators in registers: with u8 input (issue-
+// bound, not HBM-bound) they run 3 CTAs per SM.
+template <typename Tin, int kDct>
+constexpr int hash_min_blocks() { return (kDct != 0 && sizeof(Tin) == 1) ? YPDQ_U8_TC_CTAS : 2; }
 constexpr int kComputeBarrier = 1;  // named barrier id used by the 128 compute threads
 
 // Stage 1 of the DCT on tensor cores (kDct = 1: TF32, 2: BF16x3). The compressed values
@@ -60,15 +78,20 @@ struct DctTraits<1> {  // TF32: 32 rows x 4 B = 128 B per column per chunk
   static constexpr int kRowsPerChunk = 32;
   static constexpr int kBufBytes = 128 * 128;
   static constexpr int kDBytes = 4 * 2048;  // 4 K-chunks x 16 rows x 128 B
+  static constexpr int kDChunkBytes = 2048;
+  static constexpr int kKSteps = 4;         // MMAs of K = 8 (32 B) per chunk
 };
 template <>
-struct DctTraits<2> {  // BF16x3: 64 rows x 2 B, hi and lo operands
-  static constexpr int kRowsPerChunk = 64;
-  static constexpr int kBufBytes = 2 * 128 * 128;
-  static constexpr int kDBytes = 2 * 2 * 2048;  // hi, lo x 2 K-chunks x 16 rows x 128 B
+struct DctTraits<2> {  // BF16x3: 32 rows x 2 B (64-byte swizzle), hi at +0 and lo at +8192
+  static constexpr int kRowsPerChunk = 32;
+  static constexpr int kBufBytes = 2 * 128 * 64;
+  static constexpr int kDBytes = 2 * 4 * 1024;  // hi, lo x 4 K-chunks x 16 rows x 64 B
+  static constexpr int kDChunkBytes = 1024;
+  static constexpr int kKSteps = 2;             // MMAs of K = 16 (32 B) per chunk
+  static constexpr int kALo = 8192, kDLo = 4096;  // byte offsets of the lo operands
 };
 
-template <int kStageBytes, int kDct>
+template <int kStageBytes, int kNumStages, int kDct>
 struct HashSmem {
   alignas(1024) uint8_t ops[2][DctTraits<kDct>::kBufBytes];  // A operand, double-buffered
   alignas(1024) uint8_t dops[DctTraits<kDct>::kDBytes];      // B operand (DCT matrix)
@@ -349,10 +372,30 @@ __device__ __forceinline__ void split_bf16(float x, uint16_t& hi, uint16_t& lo) 
   hi = __bfloat16_as_ushort(h);
   lo = __bfloat16_as_ushort(l);
 }
+// split_bf16 of two values at once (packed conversions); a in the low halves.
+__device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
 // Byte offset of element e (of `esize` bytes) in row r of a 128B-swizzled K-major chunk.
 __device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t e, uint32_t esize) {
   const uint32_t byte = e * esize;
   return r * 128 + ((((byte >> 4) ^ (r & 7))) << 4) + (byte & 15);
+}
+// Byte offset of element e (of esize bytes) of row r in a 64-byte-swizzled K-major tile:
+// rows of 64 B, 8-row atoms of 512 B, 16-byte chunk c stored at c ^ ((r >> 1) & 3).
+__device__ __forceinline__ uint32_t sw64_offset(uint32_t r, uint32_t e, uint32_t esize) {
+  const uint32_t byte = e * esize;
+  return r * 64 + ((((byte >> 4) ^ ((r >> 1) & 3))) << 4) + (byte & 15);
+}
+// Operand descriptor of the tensor-core DCT's layout (TF32: 128 B swizzle, BF16: 64 B).
+template <int kDct>
+__device__ __forceinline__ uint64_t dct_desc(uint32_t saddr) {
+  if constexpr (kDct == 1) return sw128_desc(saddr);
+  else return sw64_desc(saddr);
 }
 // 16 consecutive TMEM columns of this warp's 32 lanes (valid after tmem_ld_wait).
 __device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
@@ -373,11 +416,13 @@ __device__ __forceinline__ void tmem_take16(uint32_t (&r)[16]) {
 }
 
 template <typename Tin, int kDct>
-__global__ void __launch_bounds__(hash_threads<kDct>()) hash_kernel(const HashLaunch prm) {
+__global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kDct>()))
+    hash_kernel(const HashLaunch prm) {
   constexpr int kRowBytes = InputTraits<Tin>::kRowBytes;
   constexpr int kStageBytes = 4 * kRowBytes;
+  constexpr int kNumStages = ring_stages<Tin, kDct>();
   constexpr int kThreads = hash_threads<kDct>();
-  using Smem = HashSmem<kStageBytes, kDct>;
+  using Smem = HashSmem<kStageBytes, kNumStages, kDct>;
   extern __shared__ unsigned char smem_raw[];
   // Align by offsetting the shared array itself so the compiler keeps the shared address
   // space (an integer round trip would turn every access into a generic one).
@@ -404,7 +449,7 @@ __global__ void __launch_bounds__(hash_threads<kDct>()) hash_kernel(const HashLa
       } else {
         uint16_t hi, lo;
         split_bf16(d, hi, lo);
-        const uint32_t off = (i >> 6) * 2048 + sw128_offset(k, i & 63, 2);
+        const uint32_t off = (i >> 5) * 1024 + sw64_offset(k, i & 31, 2);
         *reinterpret_cast<uint16_t*>(sm.dops + off) = hi;
         *reinterpret_cast<uint16_t*>(sm.dops + 4096 + off) = lo;
       }
@@ -522,21 +567,22 @@ __global__ void __launch_bounds__(hash_threads<kDct>()) hash_kernel(const HashLa
             }
             tc_fence_after();
             const uint32_t a = smem_u32(sm.ops[buf]);
-            const uint32_t d = smem_u32(sm.dops) + c * 2048;
+            using TR = DctTraits<kDct>;
+            const uint32_t d = smem_u32(sm.dops) + c * TR::kDChunkBytes;
 #pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
+            for (int ks = 0; ks < TR::kKSteps; ++ks) {
               const uint32_t accumulate = (c > 0 || ks > 0) ? 1u : 0u;
               if constexpr (kDct == 1) {
-                mma_tf32(tmem + acc * 16, sw128_desc(a + ks * 32), sw128_desc(d + ks * 32),
+                mma_tf32(tmem + acc * 16, dct_desc<kDct>(a + ks * 32), dct_desc<kDct>(d + ks * 32),
                          kIdescTf32, accumulate);
               } else {
-                // x * y ~ xh*yh + xh*yl + xl*yh   (x = A, y = D; lo operands 16 KB / 4 KB on)
-                mma_bf16(tmem + acc * 16, sw128_desc(a + ks * 32), sw128_desc(d + ks * 32),
-                         kIdescBf16, accumulate);
-                mma_bf16(tmem + acc * 16, sw128_desc(a + ks * 32),
-                         sw128_desc(d + 4096 + ks * 32), kIdescBf16, 1u);
-                mma_bf16(tmem + acc * 16, sw128_desc(a + 16384 + ks * 32),
-                         sw128_desc(d + ks * 32), kIdescBf16, 1u);
+                // x * y ~ xh*yh + xh*yl + xl*yh   (x = A, y = D)
+                mma_bf16(tmem + acc * 16, dct_desc<kDct>(a + ks * 32),
+                         dct_desc<kDct>(d + ks * 32), kIdescBf16, accumulate);
+                mma_bf16(tmem + acc * 16, dct_desc<kDct>(a + ks * 32),
+                         dct_desc<kDct>(d + TR::kDLo + ks * 32), kIdescBf16, 1u);
+                mma_bf16(tmem + acc * 16, dct_desc<kDct>(a + TR::kALo + ks * 32),
+                         dct_desc<kDct>(d + ks * 32), kIdescBf16, 1u);
               }
             }
             mma_commit(&sm.a_empty[buf]);
@@ -604,14 +650,12 @@ __global__ void __launch_bounds__(hash_threads<kDct>()) hash_kernel(const HashLa
           const uint4 w = make_uint4(to_tf32(b[0]), to_tf32(b[1]), to_tf32(b[2]), to_tf32(b[3]));
           *reinterpret_cast<uint4*>(sm.ops[buf] + sw128_offset(j, within, 4)) = w;
         } else {
-          uint16_t h[4], l[4];
-#pragma unroll
-          for (int r = 0; r < 4; ++r) split_bf16(b[r], h[r], l[r]);
-          const uint32_t off = sw128_offset(j, within, 2);
-          *reinterpret_cast<uint2*>(sm.ops[buf] + off) =
-              make_uint2(h[0] | (static_cast<uint32_t>(h[1]) << 16), h[2] | (static_cast<uint32_t>(h[3]) << 16));
-          *reinterpret_cast<uint2*>(sm.ops[buf] + 16384 + off) =
-              make_uint2(l[0] | (static_cast<uint32_t>(l[1]) << 16), l[2] | (static_cast<uint32_t>(l[3]) << 16));
+          uint32_t h01, l01, h23, l23;
+          split_bf16x2(b[0], b[1], h01, l01);
+          split_bf16x2(b[2], b[3], h23, l23);
+          const uint32_t off = sw64_offset(j, within, 2);
+          *reinterpret_cast<uint2*>(sm.ops[buf] + off) = make_uint2(h01, h23);
+          *reinterpret_cast<uint2*>(sm.ops[buf] + DctTraits<kDct>::kALo + off) = make_uint2(l01, l23);
         }
         if (within + 4 == static_cast<uint32_t>(kR)) {
           fence_proxy_async_smem();
@@ -749,13 +793,21 @@ __global__ void __launch_bounds__(128) dihedral_kernel(const DihedralLaunch prm)
 
 template <typename Tin, int kDct>
 static size_t hash_smem_bytes() {
-  return sizeof(HashSmem<4 * InputTraits<Tin>::kRowBytes, kDct>) + 1024;  // + base alignment
+  return sizeof(HashSmem<4 * InputTraits<Tin>::kRowBytes, ring_stages<Tin, kDct>(), kDct>) +
+         1024;  // + base alignment
 }
 
+// Dynamic shared memory size, and the largest shared-memory carveout so that the
+// occupancy query (and the grid) count the two CTAs per SM that fit.
 template <typename Tin, int kDct>
 static cudaError_t set_smem_attr() {
-  return cudaFuncSetAttribute(hash_kernel<Tin, kDct>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(hash_smem_bytes<Tin, kDct>()));
+  cudaError_t e = cudaFuncSetAttribute(hash_kernel<Tin, kDct>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(hash_smem_bytes<Tin, kDct>()));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(hash_kernel<Tin, kDct>,
+                              cudaFuncAttributePreferredSharedMemoryCarveout,
+                              static_cast<int>(cudaSharedmemCarveoutMaxShared));
 }
 
 cudaError_t upload_constants() {
@@ -774,11 +826,38 @@ cudaError_t upload_constants() {
   return e;
 }
 
+// Resident CTAs per SM. The runtime's occupancy query answers 1 for the tcgen05 variants
+// although their registers and shared memory admit 2 (ncu's occupancy section agrees on 2),
+// so the count is also derived from the per-SM limits and the larger answer is used.
 template <typename Tin, int kDct>
 static cudaError_t occupancy_of(int* ctas) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, hash_kernel<Tin, kDct>,
-                                                       hash_threads<kDct>(),
-                                                       hash_smem_bytes<Tin, kDct>());
+  int api = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &api, hash_kernel<Tin, kDct>, hash_threads<kDct>(), hash_smem_bytes<Tin, kDct>());
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa{};
+  int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0, threads_sm = 0;
+  e = cudaFuncGetAttributes(&fa, hash_kernel<Tin, kDct>);
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  if (e != cudaSuccess) return e;
+  const int threads = hash_threads<kDct>();
+  const size_t smem_block = hash_smem_bytes<Tin, kDct>() + fa.sharedSizeBytes + reserved;
+  const int regs_warp = ((fa.numRegs * 32 + 255) / 256) * 256;  // allocation unit: 256
+  const int by_smem = static_cast<int>(smem_sm / smem_block);
+  const int by_regs = regs_sm / (regs_warp * (threads / 32));
+  const int by_threads = threads_sm / threads;
+  int derived = by_smem < by_regs ? by_smem : by_regs;
+  if (by_threads < derived) derived = by_threads;
+  *ctas = api > derived ? api : derived;
+  return cudaSuccess;
 }
 
 cudaError_t hash_occupancy(int input_u8, int* ctas_per_sm) {

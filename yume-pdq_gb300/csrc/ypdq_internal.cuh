@@ -139,6 +139,15 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
          (static_cast<uint64_t>(2) << 61);               // swizzle: 128 B
 }
 
+// The same for a 64-byte-swizzled K-major operand: rows of 64 B, 8-row atoms of 512 B.
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+  return static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4) |
+         (static_cast<uint64_t>(1) << 16) |              // leading byte offset (unused here)
+         (static_cast<uint64_t>(512 >> 4) << 32) |       // stride byte offset
+         (static_cast<uint64_t>(1) << 46) |              // descriptor version (tcgen05)
+         (static_cast<uint64_t>(4) << 61);               // swizzle: 64 B
+}
+
 // ------------------------------------------------------------- launch plumbing
 
 struct HashLaunch {
