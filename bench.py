@@ -54,6 +54,8 @@ def parse():
                     help="arrival window per serving rate (and for the saturation run)")
     ap.add_argument("--large-rows", type=int, default=100_000_000,
                     help="rows of the clustered heavy-hit database (0 skips it)")
+    ap.add_argument("--dct-variants", type=int, default=1,
+                    help="1: time and check the FP32 / TF32 / BF16x3 hash variants")
     return ap.parse_args()
 
 
@@ -269,6 +271,57 @@ def large_db(yp, ctx, args, members=1000, trials=40, n_queries=1024):
             "db_bytes": n * 32, "points": points}
 
 
+def dct_variants(yp, ctx, args, n_distinct=512, n_launch=4096):
+    """4,096 images per launch (blob images with 25 % noise and 5 % constant ones), f32 and
+    u8 input, DCT stage 1 in FP32 SIMT / TF32 / BF16x3: launch throughput, coefficient error
+    against an FP64 DCT of the same compressed images, hash-bit disagreement with FP32."""
+    import ctypes
+    imgs, kind = yp.synth.mixed_images(n_distinct, seed=args.seed + 11)
+    live = kind != 2  # constant images: PDQF is rounding noise, bits carry no information
+    d = np.arange(127)
+    d64 = np.sqrt(2.0 / 127.0) * np.cos(np.pi * np.outer(np.arange(1, 17), 2 * d + 1) / 254.0)
+    stream = ctx.stream()
+    e0, e1 = ctx.event(), ctx.event()
+    out = {"images_per_launch": n_launch, "distinct_images": n_distinct,
+           "mix": "%d blob, %d noise, %d constant" % ((kind == 0).sum(), (kind == 1).sum(),
+                                                      (kind == 2).sum()), "variants": []}
+    for name, data in (("f32", imgs), ("u8", yp.synth.to_u8(imgs))):
+        ik = yp._lib.INPUT_U8 if name == "u8" else yp._lib.INPUT_F32
+        d_img = ctx.to_device(np.concatenate([data] * (n_launch // n_distinct)))
+        d_h, d_q = ctx.alloc(n_launch * 256), ctx.alloc(n_launch * 32)
+        ref = yp.hash_batch(ctx, data, dct=0)
+        for dct in (0, 1, 2):
+            ms = []
+            for rep in range(6):
+                ctx.record(e0, stream)
+                yp.core.hash_batch_device(ctx, d_img, n_launch, ik, d_h, d_q, dct=dct,
+                                          stream=stream)
+                ctx.record(e1, stream)
+                ctx.sync(stream)
+                if rep:
+                    ms.append(ctx.elapsed_ms(e0, e1))
+            t = statistics.median(ms)
+            c = ctypes.c_int()
+            yp._lib.check(ctx.lib.ypdq_hash_occupancy(ctx.handle, ik, dct, ctypes.byref(c)))
+            v = {"input": name, "dct": ("fp32", "tf32", "bf16x3")[dct], "ms": t,
+                 "images_s": n_launch / (t / 1e3), "ctas_per_sm": c.value,
+                 "input_GB_s": n_launch * data[0].nbytes / (t / 1e3) / 1e9}
+            got = yp.hash_batch(ctx, data, dct=dct, want_pdqf=True, want_buf1=True)
+            b = got["buf1"][live].astype(np.float64)
+            p64 = np.einsum("ki,nij,lj->nkl", d64, b, d64)
+            err = np.abs(got["pdqf"][live, 0].astype(np.float64) - p64).max(axis=(1, 2))
+            scale = np.abs(p64).max(axis=(1, 2))
+            v["max_abs_coef_err"] = float(err.max())
+            v["max_rel_coef_err"] = float((err / np.maximum(scale, 1e-30)).max())
+            v["bit_disagreement_vs_fp32"] = float(
+                np.unpackbits(got["hashes"][live] ^ ref["hashes"][live]).mean())
+            v["quality_max_abs_diff_vs_fp32"] = float(
+                np.abs(got["quality"][live] - ref["quality"][live]).max())
+            out["variants"].append(v)
+        d_img.free()
+    return out
+
+
 def run_ours(args):
     import __graft_entry__ as g
     yp = g.load_package()
@@ -358,6 +411,7 @@ def run_ours(args):
     ctx.lib.ypdq_free_host(ctx.handle, h_img)
     serve = serving(yp, ctx, db, batch, args)
     large = large_db(yp, ctx, args)
+    dctv = dct_variants(yp, ctx, args) if args.dct_variants else None
 
     hbm_peak, bf16_peak, peak_kind = measured_peaks()
     hash_avg = statistics.mean(hash_ms)
@@ -420,6 +474,7 @@ def run_ours(args):
                              "at": "ypdq_screen_host of %d images" % B},
         "serving": serve,
         "large_db": large,
+        "dct_variants": dctv,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": B * 512 * 512 * 4,
                 "d2h_bytes_per_step": hits_per_step * 16 + 8},
         "roofline": roofline,
