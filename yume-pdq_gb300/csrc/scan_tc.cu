@@ -98,30 +98,30 @@ __host__ __device__ constexpr uint32_t idesc_f8(uint32_t n) {
 }
 
 // 4 bits -> 4 e4m3 bytes: bit 0 -> 0x38 (+1.0), bit 1 -> 0xB8 (-1.0).
-__device__ __forceinline__ uint32_t expand4(uint32_t nib) {
-  return 0x38383838u | (((nib * 0x00204081u) & 0x01010101u) << 7);
-}
-
-// Expand one 32-byte row into the swizzled K-major layout: element k (bit k%8 of byte k/8)
-// goes to K-chunk k/128, 16-byte unit ((k%128)/16) XOR (row%8), byte k%16 within it.
+// Expand one packed 32-byte row (database row or query) into the 128B-swizzled K-major e4m3
+// operand, +1 (0x38) for a clear bit and -1 (0xB8) for a set bit. The dot product of two
+// expanded rows is 256 - 2 * Hamming distance for ANY bijection between the 256 bit
+// positions and the 256 K positions, as long as rows and queries use the same one. This one
+// makes each 4-byte output word a shift, a mask and an OR: byte i of output word m (m = 0..7)
+// of packed word p holds bit 8i + 7 - m of that word, which `<< m` moves to the byte's sign
+// bit. Output word (p, m) goes to K chunk p / 4, 16-byte unit 2 (p % 4) + m / 4.
 __device__ __forceinline__ void expand_row(const uint4 w0, const uint4 w1, uint8_t* chunk0,
                                            uint8_t* chunk1, int row) {
   const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
   const int sw = row & 7;
 #pragma unroll
-  for (int c = 0; c < 2; ++c) {
-    uint8_t* base = (c == 0 ? chunk0 : chunk1) + row * 128;
+  for (int p = 0; p < 8; ++p) {
+    uint8_t* base = (p < 4 ? chunk0 : chunk1) + row * 128;
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      // 16 bits = elements 128c + 16u .. +15 = bits 16u..16u+15 of words 4c..4c+3
-      const uint32_t word = words[4 * c + (u >> 1)];
-      const uint32_t bits = (word >> (16 * (u & 1))) & 0xFFFFu;
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t w = words[p];
       uint4 out;
-      out.x = expand4(bits & 15u);
-      out.y = expand4((bits >> 4) & 15u);
-      out.z = expand4((bits >> 8) & 15u);
-      out.w = expand4((bits >> 12) & 15u);
-      *reinterpret_cast<uint4*>(base + ((u ^ sw) << 4)) = out;
+      out.x = ((w << (4 * h + 0)) & 0x80808080u) | 0x38383838u;
+      out.y = ((w << (4 * h + 1)) & 0x80808080u) | 0x38383838u;
+      out.z = ((w << (4 * h + 2)) & 0x80808080u) | 0x38383838u;
+      out.w = ((w << (4 * h + 3)) & 0x80808080u) | 0x38383838u;
+      const int unit = 2 * (p & 3) + h;
+      *reinterpret_cast<uint4*>(base + ((unit ^ sw) << 4)) = out;
     }
   }
 }
