@@ -59,6 +59,19 @@ def parse():
     return ap.parse_args()
 
 
+def aggregate_over_ranks(pg, local_ms, world, images_per_rank):
+    """Replicas: every rank screened `images_per_rank` images in its own `local_ms`. The job
+    time is the slowest rank's (all-reduce MAX over the process group, if any) and the
+    job's value is all ranks' images over that time, in images/s."""
+    t = float(local_ms)
+    if pg is not None:
+        import torch
+        x = torch.tensor([t], dtype=torch.float64)
+        pg.all_reduce(x, op=pg.ReduceOp.MAX)
+        t = float(x.item())
+    return t, world * images_per_rank / (t / 1000.0)
+
+
 def dist_info():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -376,13 +389,8 @@ def run_ours(args):
     ctx.sync(stream)
     total_ms = ctx.elapsed_ms(t_start, t_end)
     clk = clocks.stop()
-    if pg:
-        import torch
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, value = aggregate_over_ranks(pg, total_ms, world, B * args.steps)
     ms_per_step = total_ms / args.steps
-    value = world * B / (ms_per_step / 1000.0)
 
     # end to end through the public C ABI from pinned host memory
     db = yp.Database(ctx, device_buffer=d_rows, n_rows=n)
