@@ -286,8 +286,9 @@ def large_db(yp, ctx, args, members=1000, trials=40, n_queries=1024):
 
 def dct_variants(yp, ctx, args, n_distinct=512, n_launch=4096):
     """4,096 images per launch (blob images with 25 % noise and 5 % constant ones), f32 and
-    u8 input, DCT stage 1 in FP32 SIMT / TF32 / BF16x3: launch throughput, coefficient error
-    against an FP64 DCT of the same compressed images, hash-bit disagreement with FP32."""
+    u8 input, DCT stage 1 in FP32 SIMT / TF32 / BF16x3, each with the reference-order and the
+    separable compress: launch throughput, coefficient error against an FP64 DCT of the
+    variant's own compressed images, hash-bit disagreement with the exact FP32 kernel."""
     import ctypes
     imgs, kind = yp.synth.mixed_images(n_distinct, seed=args.seed + 11)
     live = kind != 2  # constant images: PDQF is rounding noise, bits carry no information
@@ -303,7 +304,7 @@ def dct_variants(yp, ctx, args, n_distinct=512, n_launch=4096):
         d_img = ctx.to_device(np.concatenate([data] * (n_launch // n_distinct)))
         d_h, d_q = ctx.alloc(n_launch * 256), ctx.alloc(n_launch * 32)
         ref = yp.hash_batch(ctx, data, dct=0)
-        for dct in (0, 1, 2):
+        for dct in (0, 1, 2, 0x100, 0x101, 0x102):  # 0x100: YPDQ_COMPRESS_SEPARABLE
             ms = []
             for rep in range(6):
                 ctx.record(e0, stream)
@@ -316,7 +317,8 @@ def dct_variants(yp, ctx, args, n_distinct=512, n_launch=4096):
             t = statistics.median(ms)
             c = ctypes.c_int()
             yp._lib.check(ctx.lib.ypdq_hash_occupancy(ctx.handle, ik, dct, ctypes.byref(c)))
-            v = {"input": name, "dct": ("fp32", "tf32", "bf16x3")[dct], "ms": t,
+            v = {"input": name, "dct": ("fp32", "tf32", "bf16x3")[dct & 0xFF],
+                 "compress": "separable" if dct & 0x100 else "reference order", "ms": t,
                  "images_s": n_launch / (t / 1e3), "ctas_per_sm": c.value,
                  "input_GB_s": n_launch * data[0].nbytes / (t / 1e3) / 1e9}
             got = yp.hash_batch(ctx, data, dct=dct, want_pdqf=True, want_buf1=True)

@@ -63,6 +63,15 @@ typedef enum {
 } ypdq_dct_precision;
 
 /*
+ * OR'd into a dct_precision argument: compute the 512 -> 127 compress separably,
+ * out = (c^T X c) / 81 with c = (0,1,2,3,2,1,0), instead of the reference's 27-tap order.
+ * Exact integer sums for u8 input (one rounding, the final scale); it drops the reference
+ * table's two subnormal taps (~1e-40). Not bit-exact with yume-pdq; a fast path for callers
+ * within the stated coefficient tolerance.
+ */
+#define YPDQ_COMPRESS_SEPARABLE 0x100
+
+/*
  * Sign conventions of the dihedral derivation. yume-pdq's kernels disagree:
  *   EXACT  = Avx512F32Kernel: negate rows 0,2,..,14 and columns 0,2,..,14, which is the
  *            sign pattern of a real flip/flop of the image (src/kernel/x86.rs:989-1079).

@@ -16,7 +16,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 TOL = {1: 5e-3, 2: 1e-4}
-MAX_BIT_RATE = {1: 0.02, 2: 0.002}
+MAX_BIT_RATE = {0: 0.002, 1: 0.02, 2: 0.002}
 
 
 def rel_errors(oracle, buf1, pdqf):
@@ -76,3 +76,44 @@ def test_screen_host_with_tensor_core_dct(ctx, yp, oracle):
     hits = yp.screen_host(ctx, db, imgs, threshold=31, dct=2)
     want = oracle.find_all(rows, queries, 31)
     assert np.array_equal(hits[["index", "query", "distance"]], want[["index", "query", "distance"]])
+
+
+SEPARABLE = 0x100  # YPDQ_COMPRESS_SEPARABLE
+# FP32: the f32 DCT's own rounding (the bit-exact kernel measures ~2e-6 against FP64 too)
+TOL_SEP = {0: 1e-5, 1: 5e-3, 2: 1e-4}
+
+
+def separable_compress_f64(img):
+    """(c^T X c) / 81 with c = (0,1,2,3,2,1,0), windows at 4i+1 .. 4i+7, in float64."""
+    c = np.array([0, 1, 2, 3, 2, 1, 0], np.float64)
+    idx = 4 * np.arange(127)[:, None] + 1 + np.arange(7)[None, :]
+    x = img.astype(np.float64)
+    rows = np.einsum("d,idc->ic", c, x[idx])  # 127 x 512
+    return (rows[:, idx] @ c) / 81.0
+
+
+@pytest.mark.parametrize("dct", [0, 1, 2])
+@pytest.mark.parametrize("u8", [False, True])
+def test_separable_compress_variants(ctx, yp, oracle, dct, u8):
+    """YPDQ_COMPRESS_SEPARABLE: the compress is (c^T X c)/81, exact up to the final f32
+    scale for u8; with the reference's compressed image as the FP64 baseline the PDQF stays
+    within the variant's coefficient tolerance and the bits within its disagreement bound."""
+    imgs, kind = yp.synth.mixed_images(64, seed=400 + dct)
+    if u8:
+        imgs = yp.synth.to_u8(imgs)
+    got = yp.hash_batch(ctx, imgs, dct=dct | SEPARABLE, want_pdqf=True, want_buf1=True)
+    ref = yp.hash_batch(ctx, imgs, dct=0)
+    live = kind != 2
+    for n in range(0, len(imgs), 5):
+        want = separable_compress_f64(imgs[n])
+        scale = max(np.abs(want).max(), 1.0)
+        assert np.abs(got["buf1"][n].astype(np.float64) - want).max() / scale <= (2e-7 if u8 else 1e-6)
+        exact = oracle.compress(imgs[n].astype(np.float32))
+        assert np.abs(got["buf1"][n] - exact).max() / scale <= 2e-6
+    errs = []
+    for img, p in zip(imgs[live], got["pdqf"][live, 0]):
+        p64 = oracle.dct2d_f64(oracle.compress(img.astype(np.float32)))
+        errs.append(np.max(np.abs(p.astype(np.float64) - p64)) / np.max(np.abs(p64)))
+    assert max(errs) <= TOL_SEP[dct], max(errs)
+    rate = np.unpackbits(got["hashes"][live] ^ ref["hashes"][live]).mean()
+    assert rate <= MAX_BIT_RATE.get(dct, 0.002), rate

@@ -119,7 +119,9 @@ ypdq_status ypdq_ctx_create(int device, ypdq_ctx** out) {
   if (e == cudaSuccess) e = hash_occupancy(0, &ctx->hash_ctas_f32);
   if (e == cudaSuccess) e = hash_occupancy(1, &ctx->hash_ctas_u8);
   for (int u = 0; u < 2 && e == cudaSuccess; ++u)
-    for (int d = 0; d < 3 && e == cudaSuccess; ++d) e = hash_occupancy_dct(u, d, &ctx->hash_ctas[u][d]);
+    for (int d = 0; d < 3 && e == cudaSuccess; ++d)
+      for (int sp = 0; sp < 2 && e == cudaSuccess; ++sp)
+        e = hash_occupancy_variant(u, d, sp, &ctx->hash_ctas[u][d][sp]);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -170,9 +172,10 @@ ypdq_status ypdq_hash_occupancy(ypdq_ctx* ctx, int input_kind, int dct_precision
   if (!ctas_per_sm) return fail(YPDQ_ERR_INVALID, "ctas_per_sm is NULL");
   if (input_kind != YPDQ_INPUT_F32 && input_kind != YPDQ_INPUT_U8)
     return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
-  if (dct_precision < YPDQ_DCT_FP32 || dct_precision > YPDQ_DCT_BF16X3)
+  int dct = 0, sep = 0;
+  if (!parse_precision(dct_precision, &dct, &sep))
     return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
-  *ctas_per_sm = ctx->hash_ctas[input_kind][dct_precision];
+  *ctas_per_sm = ctx->hash_ctas[input_kind][dct][sep];
   return YPDQ_OK;
 }
 
@@ -203,7 +206,8 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
     return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
   if (semantics < YPDQ_DIHEDRAL_EXACT || semantics > YPDQ_DIHEDRAL_SCALAR)
     return fail(YPDQ_ERR_INVALID, "semantics %d", semantics);
-  if (dct_precision < YPDQ_DCT_FP32 || dct_precision > YPDQ_DCT_BF16X3)
+  int dct = 0, sep = 0;
+  if (!parse_precision(dct_precision, &dct, &sep))
     return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
   if (d_pdqf && pdqf_slots != 1 && pdqf_slots != 8)
     return fail(YPDQ_ERR_INVALID, "pdqf_slots must be 1 or 8");
@@ -221,8 +225,9 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
   p.pdqf_slots = pdqf_slots;
   p.buf1 = d_buf1;
   p.dev_err = ctx->d_err;
-  p.dct = dct_precision;
-  CK(launch_hash(p, ctx->num_sms, ctx->hash_ctas[p.input_u8][dct_precision],
+  p.dct = dct;
+  p.separable = sep;
+  CK(launch_hash(p, ctx->num_sms, ctx->hash_ctas[p.input_u8][dct][sep],
                  reinterpret_cast<cudaStream_t>(stream)),
      "hash kernel launch");
   return YPDQ_OK;
@@ -363,7 +368,8 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
                            : 1;
   uint32_t rm, cm;
   semantics_masks(semantics, &rm, &cm);
-  if (dct_precision < YPDQ_DCT_FP32 || dct_precision > YPDQ_DCT_BF16X3)
+  int dct = 0, sep = 0;
+  if (!parse_precision(dct_precision, &dct, &sep))
     return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
   for (int c = 0; c < nch && n > 0; ++c) {
     const int64_t i0 = n * c / nch, i1 = n * (c + 1) / nch;
@@ -383,8 +389,9 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
     hp.quality = static_cast<float*>(d_q) + i0 * 8;
     hp.pdqf_slots = 1;
     hp.dev_err = ctx->d_err;
-    hp.dct = dct_precision;
-    CK(launch_hash(hp, ctx->num_sms, ctx->hash_ctas[hp.input_u8][dct_precision], s),
+    hp.dct = dct;
+    hp.separable = sep;
+    CK(launch_hash(hp, ctx->num_sms, ctx->hash_ctas[hp.input_u8][dct][sep], s),
        "hash launch");
     ScanLaunch sp{};
     sp.rows = db->d_rows;

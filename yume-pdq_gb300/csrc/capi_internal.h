@@ -14,7 +14,7 @@ struct ypdq_ctx {
   int num_sms = 0;
   int hash_ctas_f32 = 1;
   int hash_ctas_u8 = 1;
-  int hash_ctas[2][3] = {{1, 1, 1}, {1, 1, 1}};  // [input u8][dct precision]
+  int hash_ctas[2][3][2] = {};  // [input u8][dct precision][separable compress]
   int* d_err = nullptr;
   cudaStream_t stream = nullptr;       // compute stream of the blocking _host calls
   cudaStream_t copy_stream = nullptr;  // host->device copies that overlap that compute
@@ -40,6 +40,16 @@ ypdq_status fail(ypdq_status st, const char* fmt, ...);
 ypdq_status cuda_fail(cudaError_t e, const char* what);
 // Row and column sign masks of the dihedral derivation for a ypdq_dihedral_semantics.
 void semantics_masks(int sem, uint32_t* rm, uint32_t* cm);
+// Splits a dct_precision argument into the DCT variant (0..2) and the
+// YPDQ_COMPRESS_SEPARABLE flag; false if it holds anything else.
+inline bool parse_precision(int v, int* dct, int* separable) {
+  const int d = v & 0xFF;
+  if ((v & ~(0xFF | YPDQ_COMPRESS_SEPARABLE)) != 0 || d < YPDQ_DCT_FP32 || d > YPDQ_DCT_BF16X3)
+    return false;
+  *dct = d;
+  *separable = (v & YPDQ_COMPRESS_SEPARABLE) ? 1 : 0;
+  return true;
+}
 
 }  // namespace ypdq
 

@@ -169,6 +169,46 @@ __device__ __forceinline__ float compress_at(const Tin* st0, const Tin* st1, int
   return s;
 }
 
+// Separable compress (YPDQ_COMPRESS_SEPARABLE; not the reference's operation order). The
+// tent weights are W[di][dj] = c[di] c[dj] / 81 with c = (0, 1, 2, 3, 2, 1, 0) (the 128-bit
+// table also holds two subnormal residue taps, ~1e-40, which this form drops). So
+//   out[i][j] = S / 81,  S = sum_{r = 2..6} c[r] h(4i + r),  h(row) = sum_{k = 2..6} c[k] x[row][4j + k]
+// Each h row serves two output rows. For u8 input h and S are exact integers (two dp4a per
+// h), so the only rounding is the final scale.
+__device__ __forceinline__ float hsum(const uint8_t* row, int j) {
+  const uint32_t* r = reinterpret_cast<const uint32_t*>(row);
+  // bytes of r[j]: columns 4j .. 4j+3 (weights 0, 0, 1, 2); r[j+1]: 4j+4 .. 4j+7 (3, 2, 1, 0)
+  return static_cast<float>(__dp4a(r[j], 0x02010000u, __dp4a(r[j + 1], 0x00010203u, 0u)));
+}
+__device__ __forceinline__ float hsum(const float* row, int j) {
+  const float4* r = reinterpret_cast<const float4*>(row);
+  const float4 a = r[j], b = r[j + 1];  // columns 4j .. 4j+3 and 4j+4 .. 4j+7
+  return (a.z + b.z) + 2.0f * (a.w + b.y) + 3.0f * b.x;
+}
+// h of rows 1..3 of a 4-row stage (rows 4s+2 .. 4s+4), carried to the next output row.
+struct HCarry {
+  float h1, h2, h3;
+};
+template <typename Tin>
+__device__ __forceinline__ void hcarry_init(const Tin* st, int j, HCarry& c) {
+  constexpr int kRow = 512;
+  c.h1 = hsum(st + 1 * kRow, j);
+  c.h2 = hsum(st + 2 * kRow, j);
+  c.h3 = hsum(st + 3 * kRow, j);
+}
+// Output row i from the carried h of stage i and the new stage i+1 (rows 4i+5 .. 4i+8).
+template <typename Tin>
+__device__ __forceinline__ float compress_separable(const Tin* st1, int j, HCarry& c) {
+  constexpr int kRow = 512;
+  const float n0 = hsum(st1 + 0 * kRow, j), n1 = hsum(st1 + 1 * kRow, j);
+  const float n2 = hsum(st1 + 2 * kRow, j), n3 = hsum(st1 + 3 * kRow, j);
+  const float S = (c.h1 + n1) + 2.0f * (c.h2 + n0) + 3.0f * c.h3;
+  c.h1 = n1;
+  c.h2 = n2;
+  c.h3 = n3;
+  return S * (1.0f / 81.0f);
+}
+
 // ---------------------------------------------------------------- epilogue
 
 __device__ __forceinline__ uint32_t f32_key(float f) {
@@ -415,7 +455,7 @@ __device__ __forceinline__ void tmem_take16(uint32_t (&r)[16]) {
                  "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
 }
 
-template <typename Tin, int kDct>
+template <typename Tin, int kDct, bool kSep>
 __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kDct>()))
     hash_kernel(const HashLaunch prm) {
   constexpr int kRowBytes = InputTraits<Tin>::kRowBytes;
@@ -620,6 +660,9 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
       constexpr uint32_t kChunks = 128 / kR;
       const uint32_t gc0 = it * kChunks;
       if (!mbar_wait(&sm.full[g0 % kNumStages], (g0 / kNumStages) & 1u, abort_flag)) goto fail;
+      HCarry hc{};
+      if (kSep && active)
+        hcarry_init<Tin>(reinterpret_cast<const Tin*>(sm.ring[g0 % kNumStages]), j, hc);
       for (int i0 = 0; i0 < 128; i0 += 4) {
         float b[4];
 #pragma unroll
@@ -633,7 +676,7 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
             if (active) {
               const Tin* st0 = reinterpret_cast<const Tin*>(sm.ring[ga % kNumStages]);
               const Tin* st1 = reinterpret_cast<const Tin*>(sm.ring[gb % kNumStages]);
-              b[r] = compress_at<Tin>(st0, st1, j);
+              b[r] = kSep ? compress_separable<Tin>(st1, j, hc) : compress_at<Tin>(st0, st1, j);
               if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b[r];
             }
             __syncwarp();
@@ -690,6 +733,9 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
       for (int r = 0; r < 4; ++r) acc[k][r] = 0.0f;
 
     if (!mbar_wait(&sm.full[g0 % kNumStages], (g0 / kNumStages) & 1u, abort_flag)) goto fail;
+    HCarry hc{};
+    if (kSep && active)
+      hcarry_init<Tin>(reinterpret_cast<const Tin*>(sm.ring[g0 % kNumStages]), j, hc);
     for (int i0 = 0; i0 < 128; i0 += 4) {
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
@@ -702,7 +748,7 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
           if (active) {
             const Tin* st0 = reinterpret_cast<const Tin*>(sm.ring[ga % kNumStages]);
             const Tin* st1 = reinterpret_cast<const Tin*>(sm.ring[gb % kNumStages]);
-            b = compress_at<Tin>(st0, st1, j);
+            b = kSep ? compress_separable<Tin>(st1, j, hc) : compress_at<Tin>(st0, st1, j);
             if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b;
           }
           const float4* d4 = reinterpret_cast<const float4*>(&sm.dt[i][0]);
@@ -799,15 +845,20 @@ static size_t hash_smem_bytes() {
 
 // Dynamic shared memory size, and the largest shared-memory carveout so that the
 // occupancy query (and the grid) count the two CTAs per SM that fit.
-template <typename Tin, int kDct>
-static cudaError_t set_smem_attr() {
-  cudaError_t e = cudaFuncSetAttribute(hash_kernel<Tin, kDct>,
+template <typename Tin, int kDct, bool kSep>
+static cudaError_t set_smem_attr_one() {
+  cudaError_t e = cudaFuncSetAttribute(hash_kernel<Tin, kDct, kSep>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(hash_smem_bytes<Tin, kDct>()));
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(hash_kernel<Tin, kDct>,
+  return cudaFuncSetAttribute(hash_kernel<Tin, kDct, kSep>,
                               cudaFuncAttributePreferredSharedMemoryCarveout,
                               static_cast<int>(cudaSharedmemCarveoutMaxShared));
+}
+template <typename Tin, int kDct>
+static cudaError_t set_smem_attr() {
+  cudaError_t e = set_smem_attr_one<Tin, kDct, false>();
+  return e == cudaSuccess ? set_smem_attr_one<Tin, kDct, true>() : e;
 }
 
 cudaError_t upload_constants() {
@@ -829,15 +880,15 @@ cudaError_t upload_constants() {
 // Resident CTAs per SM. The runtime's occupancy query answers 1 for the tcgen05 variants
 // although their registers and shared memory admit 2 (ncu's occupancy section agrees on 2),
 // so the count is also derived from the per-SM limits and the larger answer is used.
-template <typename Tin, int kDct>
+template <typename Tin, int kDct, bool kSep>
 static cudaError_t occupancy_of(int* ctas) {
   int api = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &api, hash_kernel<Tin, kDct>, hash_threads<kDct>(), hash_smem_bytes<Tin, kDct>());
+      &api, hash_kernel<Tin, kDct, kSep>, hash_threads<kDct>(), hash_smem_bytes<Tin, kDct>());
   if (e != cudaSuccess) return e;
   cudaFuncAttributes fa{};
   int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0, threads_sm = 0;
-  e = cudaFuncGetAttributes(&fa, hash_kernel<Tin, kDct>);
+  e = cudaFuncGetAttributes(&fa, hash_kernel<Tin, kDct, kSep>);
   if (e == cudaSuccess) e = cudaGetDevice(&dev);
   if (e == cudaSuccess)
     e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
@@ -861,31 +912,50 @@ static cudaError_t occupancy_of(int* ctas) {
 }
 
 cudaError_t hash_occupancy(int input_u8, int* ctas_per_sm) {
-  return input_u8 ? occupancy_of<uint8_t, 0>(ctas_per_sm) : occupancy_of<float, 0>(ctas_per_sm);
+  return hash_occupancy_variant(input_u8, 0, 0, ctas_per_sm);
 }
 
-cudaError_t hash_occupancy_dct(int input_u8, int dct, int* ctas_per_sm) {
-  if (dct == 1) return input_u8 ? occupancy_of<uint8_t, 1>(ctas_per_sm) : occupancy_of<float, 1>(ctas_per_sm);
-  if (dct == 2) return input_u8 ? occupancy_of<uint8_t, 2>(ctas_per_sm) : occupancy_of<float, 2>(ctas_per_sm);
-  return hash_occupancy(input_u8, ctas_per_sm);
+cudaError_t hash_occupancy_variant(int input_u8, int dct, int separable, int* ctas_per_sm) {
+  switch ((dct * 2 + (input_u8 ? 1 : 0)) * 2 + (separable ? 1 : 0)) {
+    case 0: return occupancy_of<float, 0, false>(ctas_per_sm);
+    case 1: return occupancy_of<float, 0, true>(ctas_per_sm);
+    case 2: return occupancy_of<uint8_t, 0, false>(ctas_per_sm);
+    case 3: return occupancy_of<uint8_t, 0, true>(ctas_per_sm);
+    case 4: return occupancy_of<float, 1, false>(ctas_per_sm);
+    case 5: return occupancy_of<float, 1, true>(ctas_per_sm);
+    case 6: return occupancy_of<uint8_t, 1, false>(ctas_per_sm);
+    case 7: return occupancy_of<uint8_t, 1, true>(ctas_per_sm);
+    case 8: return occupancy_of<float, 2, false>(ctas_per_sm);
+    case 9: return occupancy_of<float, 2, true>(ctas_per_sm);
+    case 10: return occupancy_of<uint8_t, 2, false>(ctas_per_sm);
+    case 11: return occupancy_of<uint8_t, 2, true>(ctas_per_sm);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
-template <typename Tin, int kDct>
+template <typename Tin, int kDct, bool kSep>
 static void launch_one(const HashLaunch& p, int64_t grid, cudaStream_t s) {
-  hash_kernel<Tin, kDct><<<static_cast<int>(grid), hash_threads<kDct>(), hash_smem_bytes<Tin, kDct>(), s>>>(p);
+  hash_kernel<Tin, kDct, kSep><<<static_cast<int>(grid), hash_threads<kDct>(),
+                                 hash_smem_bytes<Tin, kDct>(), s>>>(p);
 }
 
 cudaError_t launch_hash(const HashLaunch& p, int num_sms, int ctas_per_sm, cudaStream_t s) {
   if (p.n <= 0) return cudaSuccess;
   int64_t grid = static_cast<int64_t>(num_sms) * (ctas_per_sm > 0 ? ctas_per_sm : 1);
   if (grid > p.n) grid = p.n;
-  switch (p.dct * 2 + (p.input_u8 ? 1 : 0)) {
-    case 0: launch_one<float, 0>(p, grid, s); break;
-    case 1: launch_one<uint8_t, 0>(p, grid, s); break;
-    case 2: launch_one<float, 1>(p, grid, s); break;
-    case 3: launch_one<uint8_t, 1>(p, grid, s); break;
-    case 4: launch_one<float, 2>(p, grid, s); break;
-    case 5: launch_one<uint8_t, 2>(p, grid, s); break;
+  switch ((p.dct * 2 + (p.input_u8 ? 1 : 0)) * 2 + (p.separable ? 1 : 0)) {
+    case 0: launch_one<float, 0, false>(p, grid, s); break;
+    case 1: launch_one<float, 0, true>(p, grid, s); break;
+    case 2: launch_one<uint8_t, 0, false>(p, grid, s); break;
+    case 3: launch_one<uint8_t, 0, true>(p, grid, s); break;
+    case 4: launch_one<float, 1, false>(p, grid, s); break;
+    case 5: launch_one<float, 1, true>(p, grid, s); break;
+    case 6: launch_one<uint8_t, 1, false>(p, grid, s); break;
+    case 7: launch_one<uint8_t, 1, true>(p, grid, s); break;
+    case 8: launch_one<float, 2, false>(p, grid, s); break;
+    case 9: launch_one<float, 2, true>(p, grid, s); break;
+    case 10: launch_one<uint8_t, 2, false>(p, grid, s); break;
+    case 11: launch_one<uint8_t, 2, true>(p, grid, s); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -142,7 +142,7 @@ ypdq_status capture_bucket(ypdq_server* S, Slot& sl, const Bucket& b, cudaGraphE
   hp.quality = sl.d_quality;
   hp.pdqf_slots = 1;
   hp.dev_err = &sl.d_hdr->err;
-  hp.dct = S->cfg.dct_precision;
+  parse_precision(S->cfg.dct_precision, &hp.dct, &hp.separable);
   ScanLaunch sp{};
   sp.rows = S->db->d_rows;
   sp.n_rows = S->db->n_rows;
@@ -160,7 +160,7 @@ ypdq_status capture_bucket(ypdq_server* S, Slot& sl, const Bucket& b, cudaGraphE
   cudaError_t e = cudaMemcpyAsync(sl.d_hdr, sl.h_hdr, 16, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(&sl.d_hdr->count, 0, 16, s);
   if (e == cudaSuccess)
-    e = launch_hash(hp, S->ctx->num_sms, S->ctx->hash_ctas[u8 ? 1 : 0][S->cfg.dct_precision], s);
+    e = launch_hash(hp, S->ctx->num_sms, S->ctx->hash_ctas[u8 ? 1 : 0][hp.dct][hp.separable], s);
   if (e == cudaSuccess) e = launch_scan(sp, b.algo, S->ctx->num_sms, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&sl.h_hdr->count, &sl.d_hdr->count, 16, cudaMemcpyDeviceToHost, s);
@@ -498,7 +498,8 @@ ypdq_status ypdq_server_create(ypdq_ctx* ctx, ypdq_db* db, const ypdq_server_con
   ypdq_server_config cfg = *cfg_in;
   if (cfg.input_kind != YPDQ_INPUT_F32 && cfg.input_kind != YPDQ_INPUT_U8)
     return fail(YPDQ_ERR_INVALID, "input_kind %d", cfg.input_kind);
-  if (cfg.dct_precision < YPDQ_DCT_FP32 || cfg.dct_precision > YPDQ_DCT_BF16X3)
+  int dct_v = 0, sep_v = 0;
+  if (!parse_precision(cfg.dct_precision, &dct_v, &sep_v))
     return fail(YPDQ_ERR_INVALID, "dct_precision %d", cfg.dct_precision);
   if (cfg.semantics < YPDQ_DIHEDRAL_EXACT || cfg.semantics > YPDQ_DIHEDRAL_SCALAR)
     return fail(YPDQ_ERR_INVALID, "semantics %d", cfg.semantics);

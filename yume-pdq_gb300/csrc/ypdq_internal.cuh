@@ -163,6 +163,8 @@ struct HashLaunch {
   float* buf1;
   int* dev_err;
   int dct;  // 0 FP32 SIMT (bit-exact), 1 TF32, 2 BF16x3 tensor cores
+  int separable;  // nonzero: separable compress (YPDQ_COMPRESS_SEPARABLE) instead of the
+                  // reference's tap order
   const int64_t* n_dev;  // if set, the image count is read from here (graph replay); n is the bound
 };
 
@@ -198,7 +200,7 @@ struct ScanLaunch {
 // hash.cu
 cudaError_t upload_constants();
 cudaError_t hash_occupancy(int input_u8, int* ctas_per_sm);
-cudaError_t hash_occupancy_dct(int input_u8, int dct, int* ctas_per_sm);
+cudaError_t hash_occupancy_variant(int input_u8, int dct, int separable, int* ctas_per_sm);
 cudaError_t launch_hash(const HashLaunch& p, int num_sms, int ctas_per_sm, cudaStream_t s);
 cudaError_t launch_dihedrals(const DihedralLaunch& p, cudaStream_t s);
 

@@ -25,6 +25,8 @@ def main(argv=None):
     h.add_argument("--input", choices=["f32", "u8"], default="f32")
     h.add_argument("--dct", type=int, choices=[0, 1, 2], default=0)
     h.add_argument("--images", type=int, default=4096)
+    h.add_argument("--separable", action="store_true",
+                   help="YPDQ_COMPRESS_SEPARABLE (not bit-exact with the reference)")
     s = sub.add_parser("scan")
     s.add_argument("--rows", type=int, default=10_000_000)
     s.add_argument("--queries", type=int, default=64)
@@ -47,12 +49,14 @@ def main(argv=None):
         reps = (a.images + 63) // 64
         d_img = ctx.to_device(np.concatenate([base] * reps)[: a.images])
         d_h, d_q = ctx.alloc(a.images * 256), ctx.alloc(a.images * 32)
+        prec = a.dct | (0x100 if a.separable else 0)
         c = ctypes.c_int()
-        yp._lib.check(ctx.lib.ypdq_hash_occupancy(ctx.handle, kind, a.dct, ctypes.byref(c)))
-        print("hash_kernel input %s dct %d: %d CTAs per SM" % (a.input, a.dct, c.value))
+        yp._lib.check(ctx.lib.ypdq_hash_occupancy(ctx.handle, kind, prec, ctypes.byref(c)))
+        print("hash_kernel input %s dct %d separable %d: %d CTAs per SM"
+              % (a.input, a.dct, a.separable, c.value))
         for _ in range(a.reps):
             ctx.record(e0, stream)
-            yp.core.hash_batch_device(ctx, d_img, a.images, kind, d_h, d_q, dct=a.dct,
+            yp.core.hash_batch_device(ctx, d_img, a.images, kind, d_h, d_q, dct=prec,
                                       stream=stream)
             ctx.record(e1, stream)
             ctx.sync(stream)
