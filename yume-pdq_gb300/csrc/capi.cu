@@ -361,18 +361,26 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
   if ((st = scratch(ctx, 3, sizeof(ypdq_hit) * (capacity > 0 ? capacity : 1), &d_hits))) return st;
   if ((st = scratch(ctx, 4, 64, &d_cnt))) return st;
   CK(cudaMemsetAsync(d_cnt, 0, sizeof(uint64_t), s), "clear count");
-  // Chunks of at least 128 images: the copy of chunk c+1 (copy stream) overlaps the hash
-  // and scan of chunk c (compute stream); every chunk's scan appends to one hit list.
-  const int nch = n >= 256 ? static_cast<int>(n / 128 < ypdq_ctx::kMaxChunks ? n / 128
-                                                                              : ypdq_ctx::kMaxChunks)
-                           : 1;
+  // Chunks that grow from 32 images (one 256-query scan pass) by doubling: the copy of
+  // chunk c+1 (copy stream) overlaps the hash and scan of chunk c (compute stream), and only
+  // the small first chunk's copy is exposed. Every chunk's scan appends to one hit list.
+  int64_t bounds[ypdq_ctx::kMaxChunks + 1];
+  int nch = 0;
+  bounds[0] = 0;
+  for (int64_t size = 32; bounds[nch] < n;) {
+    const int64_t rest = n - bounds[nch];
+    const int64_t take = (nch == ypdq_ctx::kMaxChunks - 1 || rest <= size + size / 2) ? rest : size;
+    bounds[nch + 1] = bounds[nch] + take;
+    ++nch;
+    if (size < 512) size *= 2;
+  }
   uint32_t rm, cm;
   semantics_masks(semantics, &rm, &cm);
   int dct = 0, sep = 0;
   if (!parse_precision(dct_precision, &dct, &sep))
     return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
   for (int c = 0; c < nch && n > 0; ++c) {
-    const int64_t i0 = n * c / nch, i1 = n * (c + 1) / nch;
+    const int64_t i0 = bounds[c], i1 = bounds[c + 1];
     const uint8_t* src = static_cast<const uint8_t*>(h_images) + i0 * img_bytes;
     uint8_t* dst = static_cast<uint8_t*>(d_img) + i0 * img_bytes;
     CK(cudaMemcpyAsync(dst, src, (i1 - i0) * img_bytes, cudaMemcpyHostToDevice, ctx->copy_stream),

@@ -218,20 +218,65 @@ __global__ void bitonic_step_kernel(ypdq_hit* h, uint64_t n, uint64_t k, uint64_
   }
 }
 
+// The steps of the same sort whose partners lie inside one 2,048-hit block, done in shared
+// memory in one launch. full != 0: every stage k = 2 .. k_last (<= 2,048), each its flip
+// step and then j = k/4 .. 1. full == 0: the steps j = 1,024 .. 1 of stage k_last (> 2,048),
+// whose wider steps ran as global launches. Positions past n hold a +infinity hit, which
+// compares above every real one exactly as the global kernel's skipped padding does.
+constexpr int kSortBlock = 2048;
+__global__ void __launch_bounds__(kSortBlock / 2)
+    bitonic_block_kernel(ypdq_hit* h, uint64_t n, uint64_t k_last, int full) {
+  __shared__ ypdq_hit sh[kSortBlock];
+  const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kSortBlock;
+  const int t = threadIdx.x;
+  ypdq_hit inf;
+  inf.index = ~0ull;
+  inf.query = ~0u;
+  inf.distance = ~0u;
+  for (int x = t; x < kSortBlock; x += kSortBlock / 2)
+    sh[x] = base + x < n ? h[base + x] : inf;
+  __syncthreads();
+  auto step = [&](uint32_t j, bool flip, uint32_t k) {
+    // thread t owns the pair whose lower position has bit j clear
+    const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+    const uint32_t l = flip ? (i ^ (k - 1)) : (i | j);
+    const ypdq_hit a = sh[i], b = sh[l];
+    if (hit_less(b, a)) {
+      sh[i] = b;
+      sh[l] = a;
+    }
+    __syncthreads();
+  };
+  if (full) {
+    for (uint32_t k = 2; k <= k_last; k <<= 1) {
+      step(k >> 1, true, k);
+      for (uint32_t j = k >> 2; j > 0; j >>= 1) step(j, false, k);
+    }
+  } else {
+    for (uint32_t j = kSortBlock / 2; j > 0; j >>= 1) step(j, false, 0);
+  }
+  for (int x = t; x < kSortBlock; x += kSortBlock / 2)
+    if (base + x < n) h[base + x] = sh[x];
+}
+
 cudaError_t launch_sort_hits(ypdq_hit* hits, uint64_t n, cudaStream_t s) {
   if (n < 2) return cudaSuccess;
   uint64_t padded = 1;
   while (padded < n) padded <<= 1;
   const unsigned threads = 256;
   const unsigned blocks = static_cast<unsigned>((n + threads - 1) / threads);
-  for (uint64_t k = 2; k <= padded; k <<= 1) {
+  const unsigned sblocks = static_cast<unsigned>((n + kSortBlock - 1) / kSortBlock);
+  const uint64_t first = padded < static_cast<uint64_t>(kSortBlock) ? padded : kSortBlock;
+  bitonic_block_kernel<<<sblocks, kSortBlock / 2, 0, s>>>(hits, n, first, 1);
+  for (uint64_t k = 2 * kSortBlock; k <= padded; k <<= 1) {
     bitonic_step_kernel<<<blocks, threads, 0, s>>>(hits, n, k, k >> 1, 1);
-    for (uint64_t j = k >> 2; j > 0; j >>= 1)
+    for (uint64_t j = k >> 2; j >= static_cast<uint64_t>(kSortBlock); j >>= 1)
       bitonic_step_kernel<<<blocks, threads, 0, s>>>(hits, n, k, j, 0);
+    bitonic_block_kernel<<<sblocks, kSortBlock / 2, 0, s>>>(hits, n, k, 0);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  return cudaSuccess;
+  return cudaGetLastError();
 }
 
 }  // namespace ypdq
