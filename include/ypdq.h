@@ -52,8 +52,19 @@ typedef enum {
   YPDQ_ERR_BUSY = 8       /* the server's request queue is full; submit again later */
 } ypdq_status;
 
-/* Input pixel format of 512x512 grayscale images, row-major, values 0..255. */
-typedef enum { YPDQ_INPUT_F32 = 0, YPDQ_INPUT_U8 = 1 } ypdq_input_kind;
+/*
+ * Input pixel format of 512x512 images, row-major, values 0..255. RGB8 (3 bytes per pixel)
+ * and RGBA8 (4 bytes; alpha ignored) are converted to luma inside the hash kernel exactly as
+ * yume-pdq's Kernel::cvt_rgb8_to_luma8f / cvt_rgba8_to_luma8f do (src/kernel/mod.rs:303-340,
+ * ITU-R BT.601, src/kernel/constants.rs:23), the conversion the CLI applies to rgb8/rgba8
+ * frames (src/main.rs:517-606).
+ */
+typedef enum {
+  YPDQ_INPUT_F32 = 0,
+  YPDQ_INPUT_U8 = 1,
+  YPDQ_INPUT_RGB8 = 2,
+  YPDQ_INPUT_RGBA8 = 3
+} ypdq_input_kind;
 
 /* DCT arithmetic. FP32 reproduces yume-pdq's scalar f32 kernel bit for bit. */
 typedef enum {

@@ -57,6 +57,7 @@ def lib():
             "ypdqo_count_all": (i64, [P, i64, P, i32, u32, i32]),
             "ypdqo_fm_sine_image": (None, [P]),
             "ypdqo_synth_rows": (None, [P, i64, ctypes.c_uint64, ctypes.c_uint64, i32]),
+            "ypdqo_luma": (None, [P, i64, i32, P]),
             "ypdqo_synth_clustered": (None, [P, i64, ctypes.c_uint64, ctypes.c_uint64,
                                              ctypes.c_uint32, ctypes.c_uint64, i32]),
         }
@@ -220,4 +221,12 @@ def synth_clustered(n, members, trials, seed, first=0, nthreads=None):
     out = np.empty((n, 32), np.uint8)
     lib().ypdqo_synth_clustered(_p(out), n, first, members, trials, seed,
                                 nthreads or os.cpu_count() or 1)
+    return out
+
+
+def luma(px):
+    """RGB8/RGBA8 pixels [..., 3 or 4] u8 -> f32 luma [...] in the reference's scalar order."""
+    px = np.ascontiguousarray(px, np.uint8)
+    out = np.empty(px.shape[:-1], np.float32)
+    lib().ypdqo_luma(_p(px), out.size, px.shape[-1], _p(out))
     return out

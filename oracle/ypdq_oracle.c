@@ -594,3 +594,20 @@ YPDQO_EXPORT void ypdqo_synth_clustered(uint8_t* out, int64_t n, uint64_t first,
   clustered_ctx c = {(uint64_t*)out, first, members, seed, trials};
   parallel_ranges(clustered_range, &c, n, nthreads);
 }
+
+/* ------------------------------------------------------ RGB8 / RGBA8 to luma */
+
+/* Kernel::cvt_rgb8_to_luma8f / cvt_rgba8_to_luma8f (src/kernel/mod.rs:303-340) with the
+ * ITU-R BT.601 table of src/kernel/constants.rs:23, the conversion the CLI applies to rgb8
+ * and rgba8 frames (src/main.rs:517-606): luma = (0.299 r + 0.587 g) + 0.114 b evaluated left
+ * to right in f32 (no contraction: this file builds with -ffp-contract=off). */
+YPDQO_EXPORT void ypdqo_luma(const uint8_t* px, int64_t n_pixels, int channels, float* out) {
+  const float kr = 0.299f, kg = 0.587f, kb = 0.114f;
+  for (int64_t i = 0; i < n_pixels; i++) {
+    const uint8_t* p = px + i * channels;
+    const float r = kr * (float)p[0];
+    const float g = kg * (float)p[1];
+    const float b = kb * (float)p[2];
+    out[i] = (r + g) + b;
+  }
+}

@@ -222,3 +222,34 @@ def test_invalid_arguments(ctx, yp):
     assert lib.ypdq_hash_batch(ctx.handle, d.ptr, -1, 0, 0, 0, None, None, None, None, 1, None, None) == yp._lib.ERR_INVALID
     assert lib.ypdq_hash_batch(ctx.handle, d.ptr, 0, 0, 0, 0, None, None, None, None, 1, None, None) == 0
     ctx.check_device_errors()
+
+
+@pytest.mark.parametrize("channels", [3, 4])
+def test_rgb_input_bit_exact(ctx, yp, oracle, channels):
+    """RGB8 / RGBA8 input: the kernel's fused BT.601 luma equals the reference's conversion
+    followed by its f32 pipeline, bit for bit (hashes, thresholds, qualities, PDQF, buffer)."""
+    imgs = yp.synth.color_images(10, seed=70 + channels, channels=channels)
+    got = yp.hash_batch(ctx, imgs, want_pdqf=True, want_buf1=True)
+    luma = oracle.luma(imgs)
+    h, q, t, p = oracle.hash_batch(luma, want_pdqf=True)
+    assert np.array_equal(got["hashes"], h)
+    assert np.array_equal(got["quality"], q)
+    assert np.array_equal(got["thresholds"], t)
+    assert np.array_equal(got["pdqf"][:, 0].view(np.uint32), p.view(np.uint32))
+    for n in (0, 9):
+        assert np.array_equal(got["buf1"][n].view(np.uint32), oracle.compress(luma[n]).view(np.uint32))
+
+
+@pytest.mark.parametrize("prec", [1, 2, 0x100, 0x102])
+def test_rgb_input_variants_match_luma_input(ctx, yp, oracle, prec):
+    """Every DCT / compress variant gives the same bits for RGB input as for the f32 luma
+    image (the conversion is the only RGB-specific step); RGBA equals RGB."""
+    rgba = yp.synth.color_images(6, seed=90, channels=4)
+    rgb = np.ascontiguousarray(rgba[..., :3])
+    luma = oracle.luma(rgb)
+    a = yp.hash_batch(ctx, rgb, dct=prec, want_pdqf=True)
+    b = yp.hash_batch(ctx, rgba, dct=prec, want_pdqf=True)
+    c = yp.hash_batch(ctx, luma, dct=prec, want_pdqf=True)
+    for k in ("hashes", "quality", "thresholds", "pdqf"):
+        assert np.array_equal(a[k], c[k]), k
+        assert np.array_equal(b[k], c[k]), k

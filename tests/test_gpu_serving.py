@@ -181,3 +181,14 @@ def test_pinned_images(ctx, yp, workload):
     assert np.array_equal(res[0].hits, yp.screen_host(ctx, db, imgs[:16], threshold=31))
     assert np.array_equal(res[1].hits, yp.screen_host(ctx, db, imgs[16:48], threshold=31))
     pin.free()
+
+
+def test_rgba_requests(ctx, yp, workload):
+    imgs, rows, db = workload
+    rgba = yp.synth.color_images(9, seed=77, channels=4)
+    with yp.Server(ctx, db, input_kind="rgba8", max_step_images=16) as srv:
+        srv.submit(rgba[:4], tag=0)
+        srv.submit(rgba[4:], tag=1)
+        res = {r.tag: r for r in srv.drain()}
+    assert np.array_equal(res[0].hits, yp.screen_host(ctx, db, rgba[:4], threshold=31))
+    assert np.array_equal(res[1].hits, yp.screen_host(ctx, db, rgba[4:], threshold=31))

@@ -185,3 +185,19 @@ def test_clustered_rows_twin(oracle):
     # rows are a pure function of the global row number
     again = oracle.synth_clustered(100, members, trials, seed, first=3_000_000 + 500)
     assert np.array_equal(again, rows[500:600])
+
+
+def test_luma_matches_reference_order(oracle):
+    """Kernel::cvt_rgb8_to_luma8f (src/kernel/mod.rs:303-340): (0.299 r + 0.587 g) + 0.114 b
+    in f32, left to right; the reference's own AVX2 test expects 0.299 * 255 for pure red
+    (src/kernel/x86.rs:1510-1540)."""
+    rng = np.random.default_rng(9)
+    px = rng.integers(0, 256, (4096, 4), dtype=np.uint8)
+    got3 = oracle.luma(px[:, :3])
+    got4 = oracle.luma(px)
+    r, g, b = (px[:, k].astype(np.float32) for k in range(3))
+    want = (np.float32(0.299) * r + np.float32(0.587) * g) + np.float32(0.114) * b
+    assert np.array_equal(got3.view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(got4, got3)  # alpha ignored
+    red = oracle.luma(np.array([[255, 0, 0]], np.uint8))[0]
+    assert red == np.float32(0.299) * np.float32(255.0)

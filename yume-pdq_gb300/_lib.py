@@ -21,7 +21,7 @@ STATUS_NAMES = {
     7: "UNSUPPORTED", 8: "BUSY",
 }
 
-INPUT_F32, INPUT_U8 = 0, 1
+INPUT_F32, INPUT_U8, INPUT_RGB8, INPUT_RGBA8 = 0, 1, 2, 3
 DCT_FP32, DCT_TF32, DCT_BF16X3 = 0, 1, 2
 DIHEDRAL_EXACT, DIHEDRAL_AVX2, DIHEDRAL_SCALAR = 0, 1, 2
 SEMANTICS = {"exact": DIHEDRAL_EXACT, "avx2": DIHEDRAL_AVX2, "scalar": DIHEDRAL_SCALAR}

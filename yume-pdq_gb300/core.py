@@ -131,20 +131,31 @@ def hash_batch_device(ctx, d_images, n, input_kind, d_hashes=None, d_quality=Non
                                   stream))
 
 
+def input_kind_of(images):
+    """(contiguous images, ypdq_input_kind) for host images: [n, 512, 512] f32 or u8, or
+    [n, 512, 512, 3 | 4] u8 (RGB8 / RGBA8)."""
+    imgs = np.ascontiguousarray(images)
+    if imgs.ndim == 4:
+        if imgs.dtype != np.uint8 or imgs.shape[1:3] != (512, 512) or imgs.shape[3] not in (3, 4):
+            raise ValueError("colour images must be [n, 512, 512, 3|4] u8, got %s %s"
+                             % (imgs.dtype, imgs.shape))
+        return imgs, (_lib.INPUT_RGB8 if imgs.shape[3] == 3 else _lib.INPUT_RGBA8)
+    if imgs.ndim != 3 or imgs.shape[1:] != (512, 512):
+        raise ValueError("images must be [n, 512, 512], got %s" % (imgs.shape,))
+    if imgs.dtype == np.uint8:
+        return imgs, _lib.INPUT_U8
+    return imgs.astype(np.float32, copy=False), _lib.INPUT_F32
+
+
 def hash_batch(ctx, images, semantics="exact", dct=_lib.DCT_FP32, want_pdqf=False,
                pdqf_slots=1, want_buf1=False):
-    """Hash host images [n, 512, 512] (f32 or u8) on the GPU.
+    """Hash host images on the GPU: [n, 512, 512] f32 or u8, or [n, 512, 512, 3|4] u8
+    (RGB8 / RGBA8, converted to BT.601 luma in the kernel).
 
     Returns a dict with hashes [n, 8, 32] u8, quality [n, 8], thresholds [n, 8] and,
     when asked, pdqf [n, slots, 16, 16] and buf1 [n, 127, 127].
     """
-    imgs = np.ascontiguousarray(images)
-    if imgs.dtype == np.uint8:
-        kind = _lib.INPUT_U8
-    else:
-        imgs = imgs.astype(np.float32, copy=False)
-        kind = _lib.INPUT_F32
-    assert imgs.shape[1:] == (512, 512), imgs.shape
+    imgs, kind = input_kind_of(images)
     n = imgs.shape[0]
     d_img = ctx.to_device(imgs)
     d_h = ctx.alloc(n * 256)
@@ -257,10 +268,7 @@ class Database:
 def screen_host(ctx, db, images, threshold=31, semantics="exact", dct=_lib.DCT_FP32,
                 capacity=1 << 16, want_hashes=False):
     """ypdq_screen_host: hash + 8 dihedrals + scan, from host images to sorted host hits."""
-    imgs = np.ascontiguousarray(images)
-    kind = _lib.INPUT_U8 if imgs.dtype == np.uint8 else _lib.INPUT_F32
-    if kind == _lib.INPUT_F32:
-        imgs = imgs.astype(np.float32, copy=False)
+    imgs, kind = input_kind_of(images)
     n = imgs.shape[0]
     while True:
         hits = np.zeros(max(capacity, 1), HIT_DTYPE)

@@ -118,7 +118,7 @@ ypdq_status ypdq_ctx_create(int device, ypdq_ctx** out) {
   if (e == cudaSuccess) e = scan_init();
   if (e == cudaSuccess) e = hash_occupancy(0, &ctx->hash_ctas_f32);
   if (e == cudaSuccess) e = hash_occupancy(1, &ctx->hash_ctas_u8);
-  for (int u = 0; u < 2 && e == cudaSuccess; ++u)
+  for (int u = 0; u < 4 && e == cudaSuccess; ++u)
     for (int d = 0; d < 3 && e == cudaSuccess; ++d)
       for (int sp = 0; sp < 2 && e == cudaSuccess; ++sp)
         e = hash_occupancy_variant(u, d, sp, &ctx->hash_ctas[u][d][sp]);
@@ -170,7 +170,7 @@ ypdq_status ypdq_hash_occupancy(ypdq_ctx* ctx, int input_kind, int dct_precision
   ypdq_status st = check_ctx(ctx);
   if (st) return st;
   if (!ctas_per_sm) return fail(YPDQ_ERR_INVALID, "ctas_per_sm is NULL");
-  if (input_kind != YPDQ_INPUT_F32 && input_kind != YPDQ_INPUT_U8)
+  if (image_bytes_of(input_kind) == 0)
     return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
   int dct = 0, sep = 0;
   if (!parse_precision(dct_precision, &dct, &sep))
@@ -202,7 +202,7 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
   if (st) return st;
   if (n < 0) return fail(YPDQ_ERR_INVALID, "n < 0");
   if (n > 0 && !d_images) return fail(YPDQ_ERR_INVALID, "d_images is NULL");
-  if (input_kind != YPDQ_INPUT_F32 && input_kind != YPDQ_INPUT_U8)
+  if (image_bytes_of(input_kind) == 0)
     return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
   if (semantics < YPDQ_DIHEDRAL_EXACT || semantics > YPDQ_DIHEDRAL_SCALAR)
     return fail(YPDQ_ERR_INVALID, "semantics %d", semantics);
@@ -216,7 +216,7 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
   HashLaunch p{};
   p.images = d_images;
   p.n = n;
-  p.input_u8 = input_kind == YPDQ_INPUT_U8;
+  p.input_kind = input_kind;
   semantics_masks(semantics, &p.row_mask, &p.col_mask);
   p.hashes = d_hashes;
   p.quality = d_quality;
@@ -227,7 +227,7 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
   p.dev_err = ctx->d_err;
   p.dct = dct;
   p.separable = sep;
-  CK(launch_hash(p, ctx->num_sms, ctx->hash_ctas[p.input_u8][dct][sep],
+  CK(launch_hash(p, ctx->num_sms, ctx->hash_ctas[p.input_kind][dct][sep],
                  reinterpret_cast<cudaStream_t>(stream)),
      "hash kernel launch");
   return YPDQ_OK;
@@ -348,12 +348,12 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
   if (!db || !n_hits || (n > 0 && !h_images) || (capacity > 0 && !h_hits))
     return fail(YPDQ_ERR_INVALID, "NULL argument");
   if (n < 0 || n * 8 > 0xffffffffll) return fail(YPDQ_ERR_INVALID, "n out of range");
-  if (input_kind != YPDQ_INPUT_F32 && input_kind != YPDQ_INPUT_U8)
+  if (image_bytes_of(input_kind) == 0)
     return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
   if (threshold > 256) return fail(YPDQ_ERR_INVALID, "threshold %u > 256", threshold);
   std::lock_guard<std::mutex> lock(ctx->mu);
   cudaStream_t s = ctx->stream;
-  const size_t img_bytes = (input_kind == YPDQ_INPUT_U8 ? 1u : 4u) * 512u * 512u;
+  const size_t img_bytes = image_bytes_of(input_kind);
   void *d_img, *d_hash, *d_q, *d_hits, *d_cnt;
   if ((st = scratch(ctx, 0, img_bytes * (n > 0 ? n : 1), &d_img))) return st;
   if ((st = scratch(ctx, 1, 256 * (n > 0 ? n : 1), &d_hash))) return st;
@@ -390,7 +390,7 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
     HashLaunch hp{};
     hp.images = dst;
     hp.n = i1 - i0;
-    hp.input_u8 = input_kind == YPDQ_INPUT_U8;
+    hp.input_kind = input_kind;
     hp.row_mask = rm;
     hp.col_mask = cm;
     hp.hashes = static_cast<uint8_t*>(d_hash) + i0 * 256;
@@ -399,7 +399,7 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
     hp.dev_err = ctx->d_err;
     hp.dct = dct;
     hp.separable = sep;
-    CK(launch_hash(hp, ctx->num_sms, ctx->hash_ctas[hp.input_u8][dct][sep], s),
+    CK(launch_hash(hp, ctx->num_sms, ctx->hash_ctas[hp.input_kind][dct][sep], s),
        "hash launch");
     ScanLaunch sp{};
     sp.rows = db->d_rows;
@@ -618,7 +618,7 @@ ypdq_status dropin_hash(ypdq_ctx* ctx, const float* input, float* threshold, uin
   HashLaunch p{};
   p.images = d_img;
   p.n = 1;
-  p.input_u8 = 0;
+  p.input_kind = YPDQ_INPUT_F32;
   semantics_masks(g_dropin_semantics, &p.row_mask, &p.col_mask);
   p.hashes = d_hash;
   p.quality = d_q;

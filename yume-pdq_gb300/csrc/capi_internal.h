@@ -14,7 +14,7 @@ struct ypdq_ctx {
   int num_sms = 0;
   int hash_ctas_f32 = 1;
   int hash_ctas_u8 = 1;
-  int hash_ctas[2][3][2] = {};  // [input u8][dct precision][separable compress]
+  int hash_ctas[4][3][2] = {};  // [input kind][dct precision][separable compress]
   int* d_err = nullptr;
   cudaStream_t stream = nullptr;       // compute stream of the blocking _host calls
   cudaStream_t copy_stream = nullptr;  // host->device copies that overlap that compute
@@ -33,6 +33,17 @@ struct ypdq_db {
 };
 
 namespace ypdq {
+
+// Bytes of one 512x512 image of an input kind, 0 for an unknown kind.
+inline size_t image_bytes_of(int kind) {
+  switch (kind) {
+    case YPDQ_INPUT_F32: return 4u * 512u * 512u;
+    case YPDQ_INPUT_U8: return 512u * 512u;
+    case YPDQ_INPUT_RGB8: return 3u * 512u * 512u;
+    case YPDQ_INPUT_RGBA8: return 4u * 512u * 512u;
+    default: return 0;
+  }
+}
 
 // Record a formatted message for ypdq_last_error() on the calling thread; returns st.
 ypdq_status fail(ypdq_status st, const char* fmt, ...);

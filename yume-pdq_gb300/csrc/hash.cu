@@ -29,6 +29,8 @@
 
 #include <cstring>
 
+#include <type_traits>
+
 #include "ypdq_internal.cuh"
 #include "ypdq_tables.h"
 
@@ -43,6 +45,18 @@ constexpr int kEpilogueWarp = 5;
 constexpr int kMmaWarpHash = 6;   // tensor-core DCT only: allocates TMEM, issues the MMAs
 template <int kDct>
 constexpr int hash_threads() { return kDct == 0 ? 192 : 224; }
+// RGB8 / RGBA8 pixels, converted to f32 luma once per stage (see convert_stage).
+struct rgb8_t {
+  uint8_t c[3];
+};
+struct rgba8_t {
+  uint8_t c[4];
+};
+template <typename Tin>
+constexpr bool is_rgb() {
+  return std::is_same<Tin, rgb8_t>::value || std::is_same<Tin, rgba8_t>::value;
+}
+
 // Depth of the input ring (4-row stages). The tensor-core variants with f32 input use 6
 // stages so that two CTAs fit on an SM next to their operand buffers.
 #ifndef YPDQ_RING_U8
@@ -56,8 +70,12 @@ constexpr int hash_threads() { return kDct == 0 ? 192 : 224; }
 #endif
 template <typename Tin, int kDct>
 constexpr int ring_stages() {
-  return sizeof(Tin) == 4 ? (kDct != 0 ? 6 : 8) : (kDct != 0 ? YPDQ_RING_U8_TC : YPDQ_RING_U8);
+  return is_rgb<Tin>() ? (kDct != 0 ? 4 : 6)
+                       : (sizeof(Tin) == 4 ? (kDct != 0 ? 6 : 8)
+                                           : (kDct != 0 ? YPDQ_RING_U8_TC : YPDQ_RING_U8));
 }
+template <typename Tin>
+constexpr int conv_slots() { return is_rgb<Tin>() ? 3 : 0; }
 // The tensor-core variants need no DCT accumulators in registers: with u8 input (issue-
 // bound, not HBM-bound) they run 3 CTAs per SM.
 template <typename Tin, int kDct>
@@ -91,8 +109,10 @@ struct DctTraits<2> {  // BF16x3: 32 rows x 2 B (64-byte swizzle), hi at +0 and 
   static constexpr int kALo = 8192, kDLo = 4096;  // byte offsets of the lo operands
 };
 
-template <int kStageBytes, int kNumStages, int kDct>
+template <int kStageBytes, int kNumStages, int kDct, int kConvSlots>
 struct HashSmem {
+  // RGB input only: f32 luma of the last 3 stages, shared by the compute threads
+  alignas(16) float conv[kConvSlots > 0 ? kConvSlots : 1][kConvSlots > 0 ? 4 * 512 : 4];
   alignas(1024) uint8_t ops[2][DctTraits<kDct>::kBufBytes];  // A operand, double-buffered
   alignas(1024) uint8_t dops[DctTraits<kDct>::kDBytes];      // B operand (DCT matrix)
   alignas(128) unsigned char ring[kNumStages][kStageBytes];
@@ -119,6 +139,75 @@ template <>
 struct InputTraits<uint8_t> {
   static constexpr int kRowBytes = 512;
 };
+template <>
+struct InputTraits<rgb8_t> {
+  static constexpr int kRowBytes = 512 * 3;
+};
+template <>
+struct InputTraits<rgba8_t> {
+  static constexpr int kRowBytes = 512 * 4;
+};
+// The element type the compress reads: the input itself, or f32 luma for RGB input.
+template <typename Tin, bool kRgb = is_rgb<Tin>()>
+struct CompressIn {
+  using T = Tin;
+};
+template <typename Tin>
+struct CompressIn<Tin, true> {
+  using T = float;
+};
+
+// ITU-R BT.601 luma in the reference's scalar order (Kernel::cvt_rgb8_to_luma8f,
+// src/kernel/mod.rs:303-340, coefficients src/kernel/constants.rs:23):
+// (0.299 r + 0.587 g) + 0.114 b, each product and sum rounded to f32, no fused multiply-add.
+__device__ __forceinline__ float luma_bt601(uint32_t r, uint32_t g, uint32_t b) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(0.299f, static_cast<float>(r)),
+                             __fmul_rn(0.587f, static_cast<float>(g))),
+                   __fmul_rn(0.114f, static_cast<float>(b)));
+}
+// One 4-row stage (2,048 pixels) to f32 luma: compute thread t converts pixels 16t .. 16t+15.
+__device__ __forceinline__ void convert_stage(const unsigned char* raw, float* out, int t,
+                                              rgba8_t) {
+  const uint4* src = reinterpret_cast<const uint4*>(raw) + 4 * t;
+  float4* dst = reinterpret_cast<float4*>(out) + 4 * t;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const uint4 v = src[q];
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    float l[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      l[k] = luma_bt601(w[k] & 0xFFu, (w[k] >> 8) & 0xFFu, (w[k] >> 16) & 0xFFu);
+    dst[q] = make_float4(l[0], l[1], l[2], l[3]);
+  }
+}
+__device__ __forceinline__ void convert_stage(const unsigned char* raw, float* out, int t,
+                                              rgb8_t) {
+  const uint4* src = reinterpret_cast<const uint4*>(raw + 48 * t);
+  float4* dst = reinterpret_cast<float4*>(out) + 4 * t;
+  uint32_t w[12];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const uint4 v = src[q];
+    w[4 * q] = v.x;
+    w[4 * q + 1] = v.y;
+    w[4 * q + 2] = v.z;
+    w[4 * q + 3] = v.w;
+  }
+  float l[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int b0 = 3 * k;  // byte index of the pixel's red channel
+    const uint32_t r = (w[b0 >> 2] >> (8 * (b0 & 3))) & 0xFFu;
+    const uint32_t g = (w[(b0 + 1) >> 2] >> (8 * ((b0 + 1) & 3))) & 0xFFu;
+    const uint32_t b = (w[(b0 + 2) >> 2] >> (8 * ((b0 + 2) & 3))) & 0xFFu;
+    l[k] = luma_bt601(r, g, b);
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) dst[q] = make_float4(l[4 * q], l[4 * q + 1], l[4 * q + 2], l[4 * q + 3]);
+}
+template <typename Tin>
+__device__ __forceinline__ void convert_stage(const unsigned char*, float*, int, Tin) {}
 
 // Columns 4j .. 4j+7 of one input row held in shared memory.
 __device__ __forceinline__ void load_row8(const float* row, int j, float x[8]) {
@@ -455,6 +544,13 @@ __device__ __forceinline__ void tmem_take16(uint32_t (&r)[16]) {
                  "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
 }
 
+// The compress input of global stage g: the ring slot itself, or (RGB) its luma slot.
+template <typename Tin, typename CT, int kNumStages, typename Smem>
+__device__ __forceinline__ const CT* stage_ptr(Smem& sm, uint32_t g) {
+  if constexpr (is_rgb<Tin>()) return sm.conv[g % 3];
+  else return reinterpret_cast<const CT*>(sm.ring[g % kNumStages]);
+}
+
 template <typename Tin, int kDct, bool kSep>
 __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kDct>()))
     hash_kernel(const HashLaunch prm) {
@@ -462,7 +558,9 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
   constexpr int kStageBytes = 4 * kRowBytes;
   constexpr int kNumStages = ring_stages<Tin, kDct>();
   constexpr int kThreads = hash_threads<kDct>();
-  using Smem = HashSmem<kStageBytes, kNumStages, kDct>;
+  using Smem = HashSmem<kStageBytes, kNumStages, kDct, conv_slots<Tin>()>;
+  constexpr bool kRgb = is_rgb<Tin>();
+  using CT = typename CompressIn<Tin>::T;
   extern __shared__ unsigned char smem_raw[];
   // Align by offsetting the shared array itself so the compiler keeps the shared address
   // space (an integer round trip would turn every access into a generic one).
@@ -660,9 +758,17 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
       constexpr uint32_t kChunks = 128 / kR;
       const uint32_t gc0 = it * kChunks;
       if (!mbar_wait(&sm.full[g0 % kNumStages], (g0 / kNumStages) & 1u, abort_flag)) goto fail;
+      if constexpr (kRgb) {
+        // the first stage to luma; the barrier also orders this image's slot writes after
+        // every thread's last read of the previous image
+        convert_stage(sm.ring[g0 % kNumStages], sm.conv[g0 % 3], tid, Tin{});
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.empty[g0 % kNumStages]);
+        named_bar_sync(kComputeBarrier, kComputeThreads);
+      }
       HCarry hc{};
       if (kSep && active)
-        hcarry_init<Tin>(reinterpret_cast<const Tin*>(sm.ring[g0 % kNumStages]), j, hc);
+        hcarry_init<CT>(stage_ptr<Tin, CT, kNumStages>(sm, g0), j, hc);
       for (int i0 = 0; i0 < 128; i0 += 4) {
         float b[4];
 #pragma unroll
@@ -673,14 +779,22 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
             const uint32_t ga = g0 + i, gb = ga + 1;
             if (!mbar_wait(&sm.full[gb % kNumStages], (gb / kNumStages) & 1u, abort_flag))
               goto fail;
+            if constexpr (kRgb) {
+              convert_stage(sm.ring[gb % kNumStages], sm.conv[gb % 3], tid, Tin{});
+              __syncwarp();
+              if (lane == 0) mbar_arrive(&sm.empty[gb % kNumStages]);
+              named_bar_sync(kComputeBarrier, kComputeThreads);
+            }
             if (active) {
-              const Tin* st0 = reinterpret_cast<const Tin*>(sm.ring[ga % kNumStages]);
-              const Tin* st1 = reinterpret_cast<const Tin*>(sm.ring[gb % kNumStages]);
-              b[r] = kSep ? compress_separable<Tin>(st1, j, hc) : compress_at<Tin>(st0, st1, j);
+              const CT* st0 = stage_ptr<Tin, CT, kNumStages>(sm, ga);
+              const CT* st1 = stage_ptr<Tin, CT, kNumStages>(sm, gb);
+              b[r] = kSep ? compress_separable<CT>(st1, j, hc) : compress_at<CT>(st0, st1, j);
               if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b[r];
             }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&sm.empty[ga % kNumStages]);
+            if constexpr (!kRgb) {
+              __syncwarp();
+              if (lane == 0) mbar_arrive(&sm.empty[ga % kNumStages]);
+            }
           }
         }
         const uint32_t within = static_cast<uint32_t>(i0 % kR);
@@ -706,8 +820,10 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
           if (lane == 0) mbar_arrive(&sm.a_full[buf]);
         }
       }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&sm.empty[(g0 + 127) % kNumStages]);
+      if constexpr (!kRgb) {
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.empty[(g0 + 127) % kNumStages]);
+      }
       {
         const uint32_t acc = it & 1;
         if (!mbar_wait(&sm.acc_full[acc], (it >> 1) & 1u, abort_flag)) goto fail;
@@ -733,9 +849,15 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
       for (int r = 0; r < 4; ++r) acc[k][r] = 0.0f;
 
     if (!mbar_wait(&sm.full[g0 % kNumStages], (g0 / kNumStages) & 1u, abort_flag)) goto fail;
+    if constexpr (kRgb) {
+      convert_stage(sm.ring[g0 % kNumStages], sm.conv[g0 % 3], tid, Tin{});
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.empty[g0 % kNumStages]);
+      named_bar_sync(kComputeBarrier, kComputeThreads);
+    }
     HCarry hc{};
     if (kSep && active)
-      hcarry_init<Tin>(reinterpret_cast<const Tin*>(sm.ring[g0 % kNumStages]), j, hc);
+      hcarry_init<CT>(stage_ptr<Tin, CT, kNumStages>(sm, g0), j, hc);
     for (int i0 = 0; i0 < 128; i0 += 4) {
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
@@ -744,11 +866,17 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
           const uint32_t ga = g0 + i, gb = ga + 1;
           if (!mbar_wait(&sm.full[gb % kNumStages], (gb / kNumStages) & 1u, abort_flag))
             goto fail;
+          if constexpr (kRgb) {
+            convert_stage(sm.ring[gb % kNumStages], sm.conv[gb % 3], tid, Tin{});
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sm.empty[gb % kNumStages]);
+            named_bar_sync(kComputeBarrier, kComputeThreads);
+          }
           float b = 0.0f;
           if (active) {
-            const Tin* st0 = reinterpret_cast<const Tin*>(sm.ring[ga % kNumStages]);
-            const Tin* st1 = reinterpret_cast<const Tin*>(sm.ring[gb % kNumStages]);
-            b = kSep ? compress_separable<Tin>(st1, j, hc) : compress_at<Tin>(st0, st1, j);
+            const CT* st0 = stage_ptr<Tin, CT, kNumStages>(sm, ga);
+            const CT* st1 = stage_ptr<Tin, CT, kNumStages>(sm, gb);
+            b = kSep ? compress_separable<CT>(st1, j, hc) : compress_at<CT>(st0, st1, j);
             if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b;
           }
           const float4* d4 = reinterpret_cast<const float4*>(&sm.dt[i][0]);
@@ -757,13 +885,17 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
                                dc.x, dc.y, dc.z, dc.w, dd.x, dd.y, dd.z, dd.w};
 #pragma unroll
           for (int k = 0; k < 16; ++k) acc[k][r] = __fadd_rn(acc[k][r], __fmul_rn(d[k], b));
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&sm.empty[ga % kNumStages]);
+          if constexpr (!kRgb) {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sm.empty[ga % kNumStages]);
+          }
         }
       }
     }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&sm.empty[(g0 + 127) % kNumStages]);
+    if constexpr (!kRgb) {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.empty[(g0 + 127) % kNumStages]);
+    }
 
     if (active) {
 #pragma unroll
@@ -839,7 +971,8 @@ __global__ void __launch_bounds__(128) dihedral_kernel(const DihedralLaunch prm)
 
 template <typename Tin, int kDct>
 static size_t hash_smem_bytes() {
-  return sizeof(HashSmem<4 * InputTraits<Tin>::kRowBytes, ring_stages<Tin, kDct>(), kDct>) +
+  return sizeof(HashSmem<4 * InputTraits<Tin>::kRowBytes, ring_stages<Tin, kDct>(), kDct,
+                         conv_slots<Tin>()>) +
          1024;  // + base alignment
 }
 
@@ -855,27 +988,8 @@ static cudaError_t set_smem_attr_one() {
                               cudaFuncAttributePreferredSharedMemoryCarveout,
                               static_cast<int>(cudaSharedmemCarveoutMaxShared));
 }
-template <typename Tin, int kDct>
-static cudaError_t set_smem_attr() {
-  cudaError_t e = set_smem_attr_one<Tin, kDct, false>();
-  return e == cudaSuccess ? set_smem_attr_one<Tin, kDct, true>() : e;
-}
 
-cudaError_t upload_constants() {
-  float d[16 * 127];
-  for (int i = 0; i < 16 * 127; ++i) {
-    uint32_t b = YPDQ_DCT_F32_BITS[i];
-    memcpy(&d[i], &b, 4);
-  }
-  cudaError_t e = cudaMemcpyToSymbol(g_dct, d, sizeof(d));
-  if (e == cudaSuccess) e = set_smem_attr<float, 0>();
-  if (e == cudaSuccess) e = set_smem_attr<uint8_t, 0>();
-  if (e == cudaSuccess) e = set_smem_attr<float, 1>();
-  if (e == cudaSuccess) e = set_smem_attr<uint8_t, 1>();
-  if (e == cudaSuccess) e = set_smem_attr<float, 2>();
-  if (e == cudaSuccess) e = set_smem_attr<uint8_t, 2>();
-  return e;
-}
+
 
 // Resident CTAs per SM. The runtime's occupancy query answers 1 for the tcgen05 variants
 // although their registers and shared memory admit 2 (ncu's occupancy section agrees on 2),
@@ -911,54 +1025,73 @@ static cudaError_t occupancy_of(int* ctas) {
   return cudaSuccess;
 }
 
-cudaError_t hash_occupancy(int input_u8, int* ctas_per_sm) {
-  return hash_occupancy_variant(input_u8, 0, 0, ctas_per_sm);
+cudaError_t hash_occupancy(int input_kind, int* ctas_per_sm) {
+  return hash_occupancy_variant(input_kind, 0, 0, ctas_per_sm);
 }
 
-cudaError_t hash_occupancy_variant(int input_u8, int dct, int separable, int* ctas_per_sm) {
-  switch ((dct * 2 + (input_u8 ? 1 : 0)) * 2 + (separable ? 1 : 0)) {
-    case 0: return occupancy_of<float, 0, false>(ctas_per_sm);
-    case 1: return occupancy_of<float, 0, true>(ctas_per_sm);
-    case 2: return occupancy_of<uint8_t, 0, false>(ctas_per_sm);
-    case 3: return occupancy_of<uint8_t, 0, true>(ctas_per_sm);
-    case 4: return occupancy_of<float, 1, false>(ctas_per_sm);
-    case 5: return occupancy_of<float, 1, true>(ctas_per_sm);
-    case 6: return occupancy_of<uint8_t, 1, false>(ctas_per_sm);
-    case 7: return occupancy_of<uint8_t, 1, true>(ctas_per_sm);
-    case 8: return occupancy_of<float, 2, false>(ctas_per_sm);
-    case 9: return occupancy_of<float, 2, true>(ctas_per_sm);
-    case 10: return occupancy_of<uint8_t, 2, false>(ctas_per_sm);
-    case 11: return occupancy_of<uint8_t, 2, true>(ctas_per_sm);
+// Calls F<Tin, kDct, kSep>::run(args...) for the runtime (input kind, DCT, separable).
+template <template <typename, int, bool> class F, typename... A>
+static cudaError_t dispatch(int kind, int dct, int sep, A&&... args) {
+#define YPDQ_CASE(K, T)                                                        \
+  case K:                                                                      \
+    switch (dct * 2 + (sep ? 1 : 0)) {                                         \
+      case 0: return F<T, 0, false>::run(args...);                             \
+      case 1: return F<T, 0, true>::run(args...);                              \
+      case 2: return F<T, 1, false>::run(args...);                             \
+      case 3: return F<T, 1, true>::run(args...);                              \
+      case 4: return F<T, 2, false>::run(args...);                             \
+      case 5: return F<T, 2, true>::run(args...);                              \
+      default: return cudaErrorInvalidValue;                                   \
+    }
+  switch (kind) {
+    YPDQ_CASE(YPDQ_INPUT_F32, float)
+    YPDQ_CASE(YPDQ_INPUT_U8, uint8_t)
+    YPDQ_CASE(YPDQ_INPUT_RGB8, rgb8_t)
+    YPDQ_CASE(YPDQ_INPUT_RGBA8, rgba8_t)
     default: return cudaErrorInvalidValue;
   }
+#undef YPDQ_CASE
 }
 
 template <typename Tin, int kDct, bool kSep>
-static void launch_one(const HashLaunch& p, int64_t grid, cudaStream_t s) {
-  hash_kernel<Tin, kDct, kSep><<<static_cast<int>(grid), hash_threads<kDct>(),
-                                 hash_smem_bytes<Tin, kDct>(), s>>>(p);
+struct OccupancyOf {
+  static cudaError_t run(int* ctas) { return occupancy_of<Tin, kDct, kSep>(ctas); }
+};
+template <typename Tin, int kDct, bool kSep>
+struct SetSmemAttr {
+  static cudaError_t run() { return set_smem_attr_one<Tin, kDct, kSep>(); }
+};
+template <typename Tin, int kDct, bool kSep>
+struct LaunchOne {
+  static cudaError_t run(const HashLaunch& p, int64_t grid, cudaStream_t s) {
+    hash_kernel<Tin, kDct, kSep><<<static_cast<int>(grid), hash_threads<kDct>(),
+                                   hash_smem_bytes<Tin, kDct>(), s>>>(p);
+    return cudaGetLastError();
+  }
+};
+
+cudaError_t hash_occupancy_variant(int input_kind, int dct, int separable, int* ctas_per_sm) {
+  return dispatch<OccupancyOf>(input_kind, dct, separable, ctas_per_sm);
 }
 
 cudaError_t launch_hash(const HashLaunch& p, int num_sms, int ctas_per_sm, cudaStream_t s) {
   if (p.n <= 0) return cudaSuccess;
   int64_t grid = static_cast<int64_t>(num_sms) * (ctas_per_sm > 0 ? ctas_per_sm : 1);
   if (grid > p.n) grid = p.n;
-  switch ((p.dct * 2 + (p.input_u8 ? 1 : 0)) * 2 + (p.separable ? 1 : 0)) {
-    case 0: launch_one<float, 0, false>(p, grid, s); break;
-    case 1: launch_one<float, 0, true>(p, grid, s); break;
-    case 2: launch_one<uint8_t, 0, false>(p, grid, s); break;
-    case 3: launch_one<uint8_t, 0, true>(p, grid, s); break;
-    case 4: launch_one<float, 1, false>(p, grid, s); break;
-    case 5: launch_one<float, 1, true>(p, grid, s); break;
-    case 6: launch_one<uint8_t, 1, false>(p, grid, s); break;
-    case 7: launch_one<uint8_t, 1, true>(p, grid, s); break;
-    case 8: launch_one<float, 2, false>(p, grid, s); break;
-    case 9: launch_one<float, 2, true>(p, grid, s); break;
-    case 10: launch_one<uint8_t, 2, false>(p, grid, s); break;
-    case 11: launch_one<uint8_t, 2, true>(p, grid, s); break;
-    default: return cudaErrorInvalidValue;
+  return dispatch<LaunchOne>(p.input_kind, p.dct, p.separable, p, grid, s);
+}
+
+cudaError_t upload_constants() {
+  float d[16 * 127];
+  for (int i = 0; i < 16 * 127; ++i) {
+    uint32_t b = YPDQ_DCT_F32_BITS[i];
+    memcpy(&d[i], &b, 4);
   }
-  return cudaGetLastError();
+  cudaError_t e = cudaMemcpyToSymbol(g_dct, d, sizeof(d));
+  for (int kind = 0; kind < 4 && e == cudaSuccess; ++kind)
+    for (int dct = 0; dct < 3 && e == cudaSuccess; ++dct)
+      for (int sep = 0; sep < 2 && e == cudaSuccess; ++sep) e = dispatch<SetSmemAttr>(kind, dct, sep);
+  return e;
 }
 
 cudaError_t launch_dihedrals(const DihedralLaunch& p, cudaStream_t s) {

@@ -121,13 +121,13 @@ extern "C" ypdq_status ypdq_screen_noalloc(const void* d_images, int64_t n, int 
     HashLaunch hp{};
     hp.images = d_images;
     hp.n = n;
-    hp.input_u8 = input_kind == YPDQ_INPUT_U8;
+    hp.input_kind = input_kind;
     hp.row_mask = semantics == YPDQ_DIHEDRAL_SCALAR ? 0xAAAAu : 0x5555u;
     hp.col_mask = semantics == YPDQ_DIHEDRAL_AVX2 ? 0x0055u : 0x5555u;
     hp.hashes = s->hashes;
     hp.pdqf_slots = 1;
     hp.dev_err = s->err;
-    e = launch_hash(hp, s->num_sms, hp.input_u8 ? s->ctas_u8 : s->ctas_f32, cs);
+    e = launch_hash(hp, s->num_sms, input_kind == YPDQ_INPUT_U8 ? s->ctas_u8 : s->ctas_f32, cs);
   }
   if (e == cudaSuccess) {
     ScanLaunch sp{};

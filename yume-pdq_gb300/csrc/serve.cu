@@ -129,13 +129,13 @@ namespace {
 ypdq_status capture_bucket(ypdq_server* S, Slot& sl, const Bucket& b, cudaGraphExec_t* out) {
   cudaStream_t s = sl.stream;
   const uint32_t nb = b.images;
-  const bool u8 = S->cfg.input_kind == YPDQ_INPUT_U8;
+  const int kind = S->cfg.input_kind;
   CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
   HashLaunch hp{};
   hp.images = sl.d_images;
   hp.n = nb;
   hp.n_dev = &sl.d_hdr->n_images;
-  hp.input_u8 = u8;
+  hp.input_kind = kind;
   hp.row_mask = S->row_mask;
   hp.col_mask = S->col_mask;
   hp.hashes = sl.d_hashes;
@@ -160,7 +160,7 @@ ypdq_status capture_bucket(ypdq_server* S, Slot& sl, const Bucket& b, cudaGraphE
   cudaError_t e = cudaMemcpyAsync(sl.d_hdr, sl.h_hdr, 16, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(&sl.d_hdr->count, 0, 16, s);
   if (e == cudaSuccess)
-    e = launch_hash(hp, S->ctx->num_sms, S->ctx->hash_ctas[u8 ? 1 : 0][hp.dct][hp.separable], s);
+    e = launch_hash(hp, S->ctx->num_sms, S->ctx->hash_ctas[kind][hp.dct][hp.separable], s);
   if (e == cudaSuccess) e = launch_scan(sp, b.algo, S->ctx->num_sms, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&sl.h_hdr->count, &sl.d_hdr->count, 16, cudaMemcpyDeviceToHost, s);
@@ -496,7 +496,7 @@ ypdq_status ypdq_server_create(ypdq_ctx* ctx, ypdq_db* db, const ypdq_server_con
   if (!ctx || !db || !cfg_in || !out) return fail(YPDQ_ERR_INVALID, "NULL argument");
   *out = nullptr;
   ypdq_server_config cfg = *cfg_in;
-  if (cfg.input_kind != YPDQ_INPUT_F32 && cfg.input_kind != YPDQ_INPUT_U8)
+  if (image_bytes_of(cfg.input_kind) == 0)
     return fail(YPDQ_ERR_INVALID, "input_kind %d", cfg.input_kind);
   int dct_v = 0, sep_v = 0;
   if (!parse_precision(cfg.dct_precision, &dct_v, &sep_v))
@@ -518,7 +518,7 @@ ypdq_status ypdq_server_create(ypdq_ctx* ctx, ypdq_db* db, const ypdq_server_con
   S->ctx = ctx;
   S->db = db;
   S->cfg = cfg;
-  S->image_bytes = (cfg.input_kind == YPDQ_INPUT_U8 ? 1u : 4u) * 512u * 512u;
+  S->image_bytes = image_bytes_of(cfg.input_kind);
   semantics_masks(cfg.semantics, &S->row_mask, &S->col_mask);
   for (uint32_t b = 1; b <= cfg.max_step_images; b *= 2) {
     Bucket k;

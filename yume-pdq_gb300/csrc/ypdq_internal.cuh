@@ -153,7 +153,7 @@ __device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
 struct HashLaunch {
   const void* images;
   int64_t n;
-  int input_u8;
+  int input_kind;  // ypdq_input_kind: 0 f32, 1 u8, 2 RGB8, 3 RGBA8
   uint32_t row_mask, col_mask;
   uint8_t* hashes;
   float* quality;
@@ -199,8 +199,8 @@ struct ScanLaunch {
 
 // hash.cu
 cudaError_t upload_constants();
-cudaError_t hash_occupancy(int input_u8, int* ctas_per_sm);
-cudaError_t hash_occupancy_variant(int input_u8, int dct, int separable, int* ctas_per_sm);
+cudaError_t hash_occupancy(int input_kind, int* ctas_per_sm);
+cudaError_t hash_occupancy_variant(int input_kind, int dct, int separable, int* ctas_per_sm);
 cudaError_t launch_hash(const HashLaunch& p, int num_sms, int ctas_per_sm, cudaStream_t s);
 cudaError_t launch_dihedrals(const DihedralLaunch& p, cudaStream_t s);
 

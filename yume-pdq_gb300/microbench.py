@@ -22,7 +22,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="what", required=True)
     h = sub.add_parser("hash")
-    h.add_argument("--input", choices=["f32", "u8"], default="f32")
+    h.add_argument("--input", choices=["f32", "u8", "rgb8", "rgba8"], default="f32")
     h.add_argument("--dct", type=int, choices=[0, 1, 2], default=0)
     h.add_argument("--images", type=int, default=4096)
     h.add_argument("--separable", action="store_true",
@@ -42,10 +42,15 @@ def main(argv=None):
     stream = ctx.stream()
     e0, e1 = ctx.event(), ctx.event()
     if a.what == "hash":
-        kind = yp._lib.INPUT_U8 if a.input == "u8" else yp._lib.INPUT_F32
-        base = yp.synth.blob_images(64, seed=3)
-        if kind == yp._lib.INPUT_U8:
-            base = yp.synth.to_u8(base)
+        kind = {"f32": yp._lib.INPUT_F32, "u8": yp._lib.INPUT_U8, "rgb8": yp._lib.INPUT_RGB8,
+                "rgba8": yp._lib.INPUT_RGBA8}[a.input]
+        if kind in (yp._lib.INPUT_RGB8, yp._lib.INPUT_RGBA8):
+            base = yp.synth.color_images(16, seed=3, channels=3 if kind == yp._lib.INPUT_RGB8 else 4)
+            base = np.concatenate([base] * 4)
+        else:
+            base = yp.synth.blob_images(64, seed=3)
+            if kind == yp._lib.INPUT_U8:
+                base = yp.synth.to_u8(base)
         reps = (a.images + 63) // 64
         d_img = ctx.to_device(np.concatenate([base] * reps)[: a.images])
         d_h, d_q = ctx.alloc(a.images * 256), ctx.alloc(a.images * 32)

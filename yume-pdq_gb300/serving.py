@@ -17,7 +17,10 @@ import numpy as np
 from . import _lib
 from ._lib import HIT_DTYPE, YpdqError, check, ptr
 
-_KINDS = {"f32": _lib.INPUT_F32, "u8": _lib.INPUT_U8}
+_KINDS = {"f32": _lib.INPUT_F32, "u8": _lib.INPUT_U8, "rgb8": _lib.INPUT_RGB8,
+          "rgba8": _lib.INPUT_RGBA8}
+_SHAPES = {_lib.INPUT_F32: ((512, 512), np.float32), _lib.INPUT_U8: ((512, 512), np.uint8),
+           _lib.INPUT_RGB8: ((512, 512, 3), np.uint8), _lib.INPUT_RGBA8: ((512, 512, 4), np.uint8)}
 
 
 class PinnedArray:
@@ -92,9 +95,10 @@ class Server:
         self._comp = (_lib.Completion * 256)()
 
     def _check_images(self, images):
-        want = np.uint8 if self.input_kind == _lib.INPUT_U8 else np.float32
-        if images.dtype != want or images.ndim != 3 or images.shape[1:] != (512, 512):
-            raise ValueError("images must be (n, 512, 512) %s" % np.dtype(want).name)
+        shape, want = _SHAPES[self.input_kind]
+        if images.dtype != want or images.shape[1:] != shape:
+            raise ValueError("images must be (n, %s) %s"
+                             % (", ".join(map(str, shape)), np.dtype(want).name))
         if not images.flags.c_contiguous:
             raise ValueError("images must be C-contiguous")
 

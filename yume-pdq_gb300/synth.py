@@ -60,6 +60,20 @@ def mixed_images(n, seed=0, noise_frac=0.25, const_frac=0.05):
     return imgs, kind
 
 
+def color_images(n, seed=0, channels=3):
+    """n RGB8 (channels 3) or RGBA8 (channels 4) images [n, 512, 512, channels] u8: each
+    colour channel an independent blob image; alpha (if any) uniform noise, which the
+    luma conversion ignores."""
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, IMG, IMG, channels), np.uint8)
+    for i in range(n):
+        for c in range(3):
+            out[i, :, :, c] = np.clip(np.rint(blob_image(rng)), 0, 255).astype(np.uint8)
+        if channels == 4:
+            out[i, :, :, 3] = rng.integers(0, 256, (IMG, IMG), dtype=np.uint8)
+    return out
+
+
 def to_u8(imgs):
     return np.clip(np.rint(imgs), 0, 255).astype(np.uint8)
 
