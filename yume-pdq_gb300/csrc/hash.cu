@@ -70,7 +70,7 @@ constexpr bool is_rgb() {
 #endif
 template <typename Tin, int kDct>
 constexpr int ring_stages() {
-  return is_rgb<Tin>() ? (kDct != 0 ? 4 : 6)
+  return is_rgb<Tin>() ? (kDct != 0 ? 3 : 6)
                        : (sizeof(Tin) == 4 ? (kDct != 0 ? 6 : 8)
                                            : (kDct != 0 ? YPDQ_RING_U8_TC : YPDQ_RING_U8));
 }
@@ -81,6 +81,7 @@ constexpr int conv_slots() { return is_rgb<Tin>() ? 3 : 0; }
 template <typename Tin, int kDct>
 constexpr int hash_min_blocks() { return (kDct != 0 && sizeof(Tin) == 1) ? YPDQ_U8_TC_CTAS : 2; }
 constexpr int kComputeBarrier = 1;  // named barrier id used by the 128 compute threads
+constexpr int kConvRow = 136;       // floats per row of an RGB luma staging (128 + 4, padded)
 
 // Stage 1 of the DCT on tensor cores (kDct = 1: TF32, 2: BF16x3). The compressed values
 // are written, chunk by chunk of compressed rows, into a 128-byte-swizzled K-major operand
@@ -111,8 +112,9 @@ struct DctTraits<2> {  // BF16x3: 32 rows x 2 B (64-byte swizzle), hi at +0 and 
 
 template <int kStageBytes, int kNumStages, int kDct, int kConvSlots>
 struct HashSmem {
-  // RGB input only: f32 luma of the last 3 stages, shared by the compute threads
-  alignas(16) float conv[kConvSlots > 0 ? kConvSlots : 1][kConvSlots > 0 ? 4 * 512 : 4];
+  // RGB input only: per compute warp, f32 luma of its columns of the last 3 stages
+  alignas(16) float conv[kConvSlots > 0 ? 4 : 1][kConvSlots > 0 ? kConvSlots : 1]
+                        [kConvSlots > 0 ? 4 * kConvRow : 4];
   alignas(1024) uint8_t ops[2][DctTraits<kDct>::kBufBytes];  // A operand, double-buffered
   alignas(1024) uint8_t dops[DctTraits<kDct>::kDBytes];      // B operand (DCT matrix)
   alignas(128) unsigned char ring[kNumStages][kStageBytes];
@@ -160,54 +162,56 @@ struct CompressIn<Tin, true> {
 // ITU-R BT.601 luma in the reference's scalar order (Kernel::cvt_rgb8_to_luma8f,
 // src/kernel/mod.rs:303-340, coefficients src/kernel/constants.rs:23):
 // (0.299 r + 0.587 g) + 0.114 b, each product and sum rounded to f32, no fused multiply-add.
-__device__ __forceinline__ float luma_bt601(uint32_t r, uint32_t g, uint32_t b) {
-  return __fadd_rn(__fadd_rn(__fmul_rn(0.299f, static_cast<float>(r)),
-                             __fmul_rn(0.587f, static_cast<float>(g))),
-                   __fmul_rn(0.114f, static_cast<float>(b)));
+__device__ __forceinline__ float luma_bt601(float r, float g, float b) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g)), __fmul_rn(0.114f, b));
 }
-// One 4-row stage (2,048 pixels) to f32 luma: compute thread t converts pixels 16t .. 16t+15.
-__device__ __forceinline__ void convert_stage(const unsigned char* raw, float* out, int t,
-                                              rgba8_t) {
-  const uint4* src = reinterpret_cast<const uint4*>(raw) + 4 * t;
-  float4* dst = reinterpret_cast<float4*>(out) + 4 * t;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const uint4 v = src[q];
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-    float l[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      l[k] = luma_bt601(w[k] & 0xFFu, (w[k] >> 8) & 0xFFu, (w[k] >> 16) & 0xFFu);
-    dst[q] = make_float4(l[0], l[1], l[2], l[3]);
-  }
+// Byte k (0..3) of w as an exact float: the byte placed in the mantissa of 2^23 by a byte
+// permute, then 2^23 subtracted (keeps the conversion off the quarter-rate I2F path).
+template <int k>
+__device__ __forceinline__ float byte_f(uint32_t w) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650 | k)) - 8388608.0f;
 }
-__device__ __forceinline__ void convert_stage(const unsigned char* raw, float* out, int t,
-                                              rgb8_t) {
-  const uint4* src = reinterpret_cast<const uint4*>(raw + 48 * t);
-  float4* dst = reinterpret_cast<float4*>(out) + 4 * t;
-  uint32_t w[12];
-#pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    const uint4 v = src[q];
-    w[4 * q] = v.x;
-    w[4 * q + 1] = v.y;
-    w[4 * q + 2] = v.z;
-    w[4 * q + 3] = v.w;
-  }
-  float l[16];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const int b0 = 3 * k;  // byte index of the pixel's red channel
-    const uint32_t r = (w[b0 >> 2] >> (8 * (b0 & 3))) & 0xFFu;
-    const uint32_t g = (w[(b0 + 1) >> 2] >> (8 * ((b0 + 1) & 3))) & 0xFFu;
-    const uint32_t b = (w[(b0 + 2) >> 2] >> (8 * ((b0 + 2) & 3))) & 0xFFu;
-    l[k] = luma_bt601(r, g, b);
-  }
-#pragma unroll
-  for (int q = 0; q < 4; ++q) dst[q] = make_float4(l[4 * q], l[4 * q + 1], l[4 * q + 2], l[4 * q + 3]);
+// Luma staging of one 4-row stage for one compute warp: warp w reads input columns
+// 128w .. 128w+131 (its 32 compressed columns need 4j .. 4j+7), stored as 4 rows of
+// kConvRow floats from column 128w on. Lane l converts columns 128w+4l .. +3 of each row;
+// lanes 0..15 also convert the 4 columns past the warp's 128 (row l/4), 0 past the image.
+__device__ __forceinline__ uint32_t rgb_word(const unsigned char* p) {  // 4-byte aligned
+  return *reinterpret_cast<const uint32_t*>(p);
 }
 template <typename Tin>
-__device__ __forceinline__ void convert_stage(const unsigned char*, float*, int, Tin) {}
+__device__ __forceinline__ void convert_stage_warp(const unsigned char* raw, float* out, int w,
+                                                   int lane) {
+  constexpr int kRowBytes = InputTraits<Tin>::kRowBytes;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int c0 = 128 * w + 4 * lane;
+    const unsigned char* row = raw + r * kRowBytes;
+    float l[4];
+    if constexpr (sizeof(Tin) == 4) {
+      const uint4 v = *reinterpret_cast<const uint4*>(row + 4 * c0);
+      const uint32_t px[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) l[k] = luma_bt601(byte_f<0>(px[k]), byte_f<1>(px[k]), byte_f<2>(px[k]));
+    } else {
+      const unsigned char* p = row + 3 * c0;  // 12 bytes: r g b r | g b r g | b r g b
+      const uint32_t a = rgb_word(p), b = rgb_word(p + 4), c = rgb_word(p + 8);
+      l[0] = luma_bt601(byte_f<0>(a), byte_f<1>(a), byte_f<2>(a));
+      l[1] = luma_bt601(byte_f<3>(a), byte_f<0>(b), byte_f<1>(b));
+      l[2] = luma_bt601(byte_f<2>(b), byte_f<3>(b), byte_f<0>(c));
+      l[3] = luma_bt601(byte_f<1>(c), byte_f<2>(c), byte_f<3>(c));
+    }
+    *reinterpret_cast<float4*>(out + r * kConvRow + 4 * lane) = make_float4(l[0], l[1], l[2], l[3]);
+  }
+  if (lane < 16) {
+    const int r = lane >> 2, c = 128 * w + 128 + (lane & 3);
+    float v = 0.0f;
+    if (c < 512) {
+      const unsigned char* p = raw + r * kRowBytes + c * static_cast<int>(sizeof(Tin));
+      v = luma_bt601(static_cast<float>(p[0]), static_cast<float>(p[1]), static_cast<float>(p[2]));
+    }
+    out[r * kConvRow + 128 + (lane & 3)] = v;
+  }
+}
 
 // Columns 4j .. 4j+7 of one input row held in shared memory.
 __device__ __forceinline__ void load_row8(const float* row, int j, float x[8]) {
@@ -237,9 +241,8 @@ __device__ __forceinline__ void load_row8(const uint8_t* row, int j, float x[8])
 
 // Compressed value (i, j): rows 4i+1 .. 4i+6 come from stage i (rows 0..3) and stage i+1
 // (rows 0..1); tap (di, dj) reads input column 4j+1+dj, which is x[1+dj].
-template <typename Tin>
+template <typename Tin, int kRow = 512>  // kRow: elements between consecutive rows
 __device__ __forceinline__ float compress_at(const Tin* st0, const Tin* st1, int j) {
-  constexpr int kRow = 512;  // elements per row
   float x[8];
   float s = 0.0f;
   load_row8(st0 + 0 * kRow, j, x);  // row 4i+1: only the two residue taps are nonzero
@@ -278,17 +281,15 @@ __device__ __forceinline__ float hsum(const float* row, int j) {
 struct HCarry {
   float h1, h2, h3;
 };
-template <typename Tin>
+template <typename Tin, int kRow = 512>
 __device__ __forceinline__ void hcarry_init(const Tin* st, int j, HCarry& c) {
-  constexpr int kRow = 512;
   c.h1 = hsum(st + 1 * kRow, j);
   c.h2 = hsum(st + 2 * kRow, j);
   c.h3 = hsum(st + 3 * kRow, j);
 }
 // Output row i from the carried h of stage i and the new stage i+1 (rows 4i+5 .. 4i+8).
-template <typename Tin>
+template <typename Tin, int kRow = 512>
 __device__ __forceinline__ float compress_separable(const Tin* st1, int j, HCarry& c) {
-  constexpr int kRow = 512;
   const float n0 = hsum(st1 + 0 * kRow, j), n1 = hsum(st1 + 1 * kRow, j);
   const float n2 = hsum(st1 + 2 * kRow, j), n3 = hsum(st1 + 3 * kRow, j);
   const float S = (c.h1 + n1) + 2.0f * (c.h2 + n0) + 3.0f * c.h3;
@@ -545,9 +546,11 @@ __device__ __forceinline__ void tmem_take16(uint32_t (&r)[16]) {
 }
 
 // The compress input of global stage g: the ring slot itself, or (RGB) its luma slot.
+// (for RGB: the calling warp's staging, which starts at input column 128 * warp, so the
+// compress reads it at column index j - 32 * warp with rows kConvRow apart)
 template <typename Tin, typename CT, int kNumStages, typename Smem>
-__device__ __forceinline__ const CT* stage_ptr(Smem& sm, uint32_t g) {
-  if constexpr (is_rgb<Tin>()) return sm.conv[g % 3];
+__device__ __forceinline__ const CT* stage_ptr(Smem& sm, uint32_t g, int warp) {
+  if constexpr (is_rgb<Tin>()) return sm.conv[warp][g % 3];
   else return reinterpret_cast<const CT*>(sm.ring[g % kNumStages]);
 }
 
@@ -749,6 +752,9 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
   // ---- compute warps: thread j <-> compressed column j
   const int j = tid;
   const bool active = j < 127;
+  // column index and row stride the compress reads with (RGB: the warp's own staging)
+  const int jc = kRgb ? lane : j;
+  constexpr int kCRow = kRgb ? kConvRow : 512;
   uint32_t it = 0;
   for (int64_t n = blockIdx.x; n < n_images; n += gridDim.x, ++it) {
     const uint32_t g0 = it * kStagesPerImage;
@@ -761,14 +767,13 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
       if constexpr (kRgb) {
         // the first stage to luma; the barrier also orders this image's slot writes after
         // every thread's last read of the previous image
-        convert_stage(sm.ring[g0 % kNumStages], sm.conv[g0 % 3], tid, Tin{});
+        convert_stage_warp<Tin>(sm.ring[g0 % kNumStages], sm.conv[warp][g0 % 3], warp, lane);
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[g0 % kNumStages]);
-        named_bar_sync(kComputeBarrier, kComputeThreads);
       }
       HCarry hc{};
       if (kSep && active)
-        hcarry_init<CT>(stage_ptr<Tin, CT, kNumStages>(sm, g0), j, hc);
+        hcarry_init<CT, kCRow>(stage_ptr<Tin, CT, kNumStages>(sm, g0, warp), jc, hc);
       for (int i0 = 0; i0 < 128; i0 += 4) {
         float b[4];
 #pragma unroll
@@ -780,15 +785,15 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
             if (!mbar_wait(&sm.full[gb % kNumStages], (gb / kNumStages) & 1u, abort_flag))
               goto fail;
             if constexpr (kRgb) {
-              convert_stage(sm.ring[gb % kNumStages], sm.conv[gb % 3], tid, Tin{});
+              convert_stage_warp<Tin>(sm.ring[gb % kNumStages], sm.conv[warp][gb % 3], warp, lane);
               __syncwarp();
               if (lane == 0) mbar_arrive(&sm.empty[gb % kNumStages]);
-              named_bar_sync(kComputeBarrier, kComputeThreads);
             }
             if (active) {
-              const CT* st0 = stage_ptr<Tin, CT, kNumStages>(sm, ga);
-              const CT* st1 = stage_ptr<Tin, CT, kNumStages>(sm, gb);
-              b[r] = kSep ? compress_separable<CT>(st1, j, hc) : compress_at<CT>(st0, st1, j);
+              const CT* st0 = stage_ptr<Tin, CT, kNumStages>(sm, ga, warp);
+              const CT* st1 = stage_ptr<Tin, CT, kNumStages>(sm, gb, warp);
+              b[r] = kSep ? compress_separable<CT, kCRow>(st1, jc, hc)
+                          : compress_at<CT, kCRow>(st0, st1, jc);
               if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b[r];
             }
             if constexpr (!kRgb) {
@@ -850,14 +855,13 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
 
     if (!mbar_wait(&sm.full[g0 % kNumStages], (g0 / kNumStages) & 1u, abort_flag)) goto fail;
     if constexpr (kRgb) {
-      convert_stage(sm.ring[g0 % kNumStages], sm.conv[g0 % 3], tid, Tin{});
+      convert_stage_warp<Tin>(sm.ring[g0 % kNumStages], sm.conv[warp][g0 % 3], warp, lane);
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.empty[g0 % kNumStages]);
-      named_bar_sync(kComputeBarrier, kComputeThreads);
     }
     HCarry hc{};
     if (kSep && active)
-      hcarry_init<CT>(stage_ptr<Tin, CT, kNumStages>(sm, g0), j, hc);
+      hcarry_init<CT, kCRow>(stage_ptr<Tin, CT, kNumStages>(sm, g0, warp), jc, hc);
     for (int i0 = 0; i0 < 128; i0 += 4) {
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
@@ -867,16 +871,16 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
           if (!mbar_wait(&sm.full[gb % kNumStages], (gb / kNumStages) & 1u, abort_flag))
             goto fail;
           if constexpr (kRgb) {
-            convert_stage(sm.ring[gb % kNumStages], sm.conv[gb % 3], tid, Tin{});
+            convert_stage_warp<Tin>(sm.ring[gb % kNumStages], sm.conv[warp][gb % 3], warp, lane);
             __syncwarp();
             if (lane == 0) mbar_arrive(&sm.empty[gb % kNumStages]);
-            named_bar_sync(kComputeBarrier, kComputeThreads);
           }
           float b = 0.0f;
           if (active) {
-            const CT* st0 = stage_ptr<Tin, CT, kNumStages>(sm, ga);
-            const CT* st1 = stage_ptr<Tin, CT, kNumStages>(sm, gb);
-            b = kSep ? compress_separable<CT>(st1, j, hc) : compress_at<CT>(st0, st1, j);
+            const CT* st0 = stage_ptr<Tin, CT, kNumStages>(sm, ga, warp);
+            const CT* st1 = stage_ptr<Tin, CT, kNumStages>(sm, gb, warp);
+            b = kSep ? compress_separable<CT, kCRow>(st1, jc, hc)
+                     : compress_at<CT, kCRow>(st0, st1, jc);
             if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b;
           }
           const float4* d4 = reinterpret_cast<const float4*>(&sm.dt[i][0]);
