@@ -196,6 +196,17 @@ ypdq_status ypdq_db_create(ypdq_ctx *ctx, const uint8_t *h_rows, uint64_t n_rows
 ypdq_status ypdq_db_wrap(ypdq_ctx *ctx, const uint8_t *d_rows, uint64_t n_rows, ypdq_db **out);
 ypdq_status ypdq_db_destroy(ypdq_db *db);
 ypdq_status ypdq_db_info(ypdq_db *db, const uint8_t **d_rows, uint64_t *n_rows);
+/*
+ * Database files: consecutive 32-byte rows, no header (yume-pdq's in-memory layout; its CPU
+ * matcher's files pad the last 2,048-row batch by repeating the final row,
+ * examples/end_to_end.rs:52-53, and load as-is). Any size, streamed through two pinned
+ * staging buffers of chunk_bytes (0 -> 64 MiB) so that reading and copying overlap. The
+ * load creates an owned database; YPDQ_ERR_INVALID if the file cannot be read or its size
+ * is not a multiple of 32. Blocking.
+ */
+ypdq_status ypdq_db_load_file(ypdq_ctx *ctx, const char *path, uint64_t chunk_bytes,
+                              ypdq_db **out);
+ypdq_status ypdq_db_save_file(ypdq_db *db, const char *path, uint64_t chunk_bytes);
 
 /*
  * Screen n host images against db: hash, derive 8 dihedrals, scan all 8n hashes at

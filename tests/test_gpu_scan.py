@@ -178,3 +178,38 @@ def test_screen_host_chunked(ctx, yp, oracle):
     hu, _, _, _ = oracle.hash_batch(u8)
     hits_u8 = yp.screen_host(ctx, db, u8, threshold=31)
     assert np.array_equal(as_tuples(hits_u8), as_tuples(oracle.find_all(rows, hu.reshape(-1, 32), 31)))
+
+
+def test_db_file_round_trip_and_scan(ctx, yp, oracle, tmp_path):
+    """ypdq_db_load_file / ypdq_db_save_file: a flat row file, padded the reference's way to
+    whole 2,048-row batches by repeating the last row, loads in chunks (a chunk size that
+    does not divide the file) and scans exactly like the same rows from memory."""
+    rows = yp.synth.rows_128(70_001, seed=31)
+    q = yp.synth.rows_128(24, seed=32)
+    yp.synth.plant(rows, q, 500, 0, 31, seed=33)
+    pad = (-len(rows)) % 2048
+    padded = np.concatenate([rows, np.repeat(rows[-1:], pad, axis=0)])
+    path = tmp_path / "db.bin"
+    padded.tofile(path)
+    db = yp.Database.from_file(ctx, path, chunk_bytes=32 * 5000)
+    assert db.n_rows == len(padded)
+    d_rows, n = db.device_rows()
+    d_q, d_hits, d_cnt = ctx.to_device(q), ctx.alloc(16 << 16), ctx.alloc(8)
+    yp.core.scan_device(ctx, d_rows, n, d_q, len(q), 31, d_hits, 1 << 16, d_cnt)
+    ctx.sync()
+    total = int(d_cnt.download((1,), np.uint64)[0])
+    yp.core.sort_hits_device(ctx, d_hits, total)
+    ctx.sync()
+    hits = d_hits.download((total,), yp.HIT_DTYPE)
+    want = oracle.find_all(padded, q, 31)
+    assert np.array_equal(hits[["index", "query", "distance"]], want[["index", "query", "distance"]])
+    out = tmp_path / "db2.bin"
+    db.save(out, chunk_bytes=32 * 7777)
+    assert np.array_equal(np.fromfile(out, np.uint8).reshape(-1, 32), padded)
+    db.close()
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(b"x" * 33)
+    with pytest.raises(yp.YpdqError):
+        yp.Database.from_file(ctx, bad)
+    with pytest.raises(yp.YpdqError):
+        yp.Database.from_file(ctx, tmp_path / "missing.bin")

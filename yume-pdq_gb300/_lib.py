@@ -95,6 +95,8 @@ SIGNATURES = {
     "ypdq_db_wrap": (i32, [P, P, u64, PP]),
     "ypdq_db_destroy": (i32, [P]),
     "ypdq_db_info": (i32, [P, P, P]),
+    "ypdq_db_load_file": (i32, [P, ctypes.c_char_p, u64, PP]),
+    "ypdq_db_save_file": (i32, [P, ctypes.c_char_p, u64]),
     "ypdq_screen_host": (i32, [P, P, P, i64, i32, i32, i32, u32, P, u64, P, P, P]),
     "ypdq_malloc_device": (i32, [P, sz, PP]),
     "ypdq_free_device": (i32, [P, P]),

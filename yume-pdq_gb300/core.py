@@ -1,5 +1,6 @@
 """Host-side objects over the C ABI: context, device buffers, batched hash and scan."""
 import ctypes
+import os
 
 import numpy as np
 
@@ -246,6 +247,22 @@ class Database:
             check(ctx.lib.ypdq_db_create(ctx.handle, ptr(r), r.shape[0], ctypes.byref(h)))
             self.n_rows = r.shape[0]
         self.handle = h
+
+    @classmethod
+    def from_file(cls, ctx, path, chunk_bytes=0):
+        """ypdq_db_load_file: a flat file of 32-byte rows onto the device."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        check(ctx.lib.ypdq_db_load_file(ctx.handle, os.fsencode(path), int(chunk_bytes),
+                                        ctypes.byref(h)))
+        self.handle = h
+        self.n_rows = self.device_rows()[1]
+        return self
+
+    def save(self, path, chunk_bytes=0):
+        """ypdq_db_save_file: the device rows to a flat file."""
+        check(self.ctx.lib.ypdq_db_save_file(self.handle, os.fsencode(path), int(chunk_bytes)))
 
     def device_rows(self):
         p = ctypes.c_void_p()
