@@ -83,6 +83,16 @@ typedef enum {
 #define YPDQ_COMPRESS_SEPARABLE 0x100
 
 /*
+ * Passed as the whole dct_precision of ypdq_hash_batch: yume-pdq's ReferenceKernel<f32>, the
+ * pdqhash-faithful kernel (src/kernel/mod.rs:690-820, src/kernel/ref.rs). Its compress runs
+ * the full Jarosz filter (two box passes of window 3 along rows and columns of the whole
+ * 512x512 image, running sums in f32) and samples it; its DCT sums each output in one
+ * sequential accumulator. Bit-exact with that kernel for finite inputs. Slower (six passes
+ * over the image); ypdq_hash_batch only.
+ */
+#define YPDQ_COMPRESS_JAROSZ 0x200
+
+/*
  * Sign conventions of the dihedral derivation. yume-pdq's kernels disagree:
  *   EXACT  = Avx512F32Kernel: negate rows 0,2,..,14 and columns 0,2,..,14, which is the
  *            sign pattern of a real flip/flop of the image (src/kernel/x86.rs:989-1079).

@@ -58,6 +58,10 @@ def lib():
             "ypdqo_fm_sine_image": (None, [P]),
             "ypdqo_synth_rows": (None, [P, i64, ctypes.c_uint64, ctypes.c_uint64, i32]),
             "ypdqo_luma": (None, [P, i64, i32, P]),
+            "ypdqo_jarosz_compress": (None, [P, P]),
+            "ypdqo_dct2d_reference": (None, [P, P]),
+            "ypdqo_hash_batch_reference": (None, [P, i64, i32, ctypes.c_uint32, ctypes.c_uint32,
+                                                  P, P, P, P, P, i32]),
             "ypdqo_synth_clustered": (None, [P, i64, ctypes.c_uint64, ctypes.c_uint64,
                                              ctypes.c_uint32, ctypes.c_uint64, i32]),
         }
@@ -230,3 +234,30 @@ def luma(px):
     out = np.empty(px.shape[:-1], np.float32)
     lib().ypdqo_luma(_p(px), out.size, px.shape[-1], _p(out))
     return out
+
+
+def jarosz_compress(img):
+    """ReferenceKernel<f32>::jarosz_compress: full Jarosz filter + sampling -> [127, 127]."""
+    img = np.ascontiguousarray(img, np.float32)
+    out = np.empty((127, 127), np.float32)
+    lib().ypdqo_jarosz_compress(_p(img), _p(out))
+    return out
+
+
+def hash_batch_reference(imgs, semantics="scalar", nthreads=None):
+    """ReferenceKernel<f32> over n images (f32 or u8 [n, 512, 512]) with dihedrals; returns
+    hashes [n,8,32], quality [n,8], thresholds [n,8], pdqf [n,16,16], buf127 [n,127,127]."""
+    rm, cm = SEMANTICS[semantics]
+    imgs = np.ascontiguousarray(imgs)
+    is_u8 = imgs.dtype == np.uint8
+    if not is_u8:
+        imgs = imgs.astype(np.float32, copy=False)
+    n = imgs.shape[0]
+    h = np.zeros((n, 8, 32), np.uint8)
+    q = np.zeros((n, 8), np.float32)
+    t = np.zeros((n, 8), np.float32)
+    p = np.zeros((n, 16, 16), np.float32)
+    b = np.zeros((n, 127, 127), np.float32)
+    lib().ypdqo_hash_batch_reference(_p(imgs), n, int(is_u8), rm, cm, _p(h), _p(q), _p(t), _p(p),
+                                     _p(b), nthreads or os.cpu_count() or 1)
+    return h, q, t, p, b

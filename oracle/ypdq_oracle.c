@@ -611,3 +611,129 @@ YPDQO_EXPORT void ypdqo_luma(const uint8_t* px, int64_t n_pixels, int channels, 
     out[i] = (r + g) + b;
   }
 }
+
+/* ------------------------------------- ReferenceKernel<f32>: full Jarosz compress */
+
+/* compute_jarosz_filter_window_size (src/kernel/ref.rs): ceil(old / (2 new)); 3 for 512 -> 127. */
+static int jarosz_window(int old_dim, int new_dim) {
+  return (old_dim + 2 * new_dim - 1) / (2 * new_dim);
+}
+
+/* box_one_d_float (src/kernel/ref.rs): a running-sum box filter of one line in four phases
+ * (fill, grow, slide, shrink), all in f32 with true divisions by the current window size. */
+static void box_one_d(const float* in, int64_t start, float* out, int len, int64_t stride,
+                      int w) {
+  const int half = (w + 2) / 2;
+  const int64_t oi_off = (int64_t)(half - 1) * stride, li_off = (int64_t)(w - half + 1) * stride;
+  float sum = 0.0f, cws = 0.0f;
+  const int64_t p1_end = oi_off + start;
+  for (int64_t ri = start; ri < p1_end; ri += stride) {
+    sum += in[ri];
+    cws += 1.0f;
+  }
+  const int64_t p2_end = (int64_t)w * stride + start;
+  for (int64_t ri = p1_end; ri < p2_end; ri += stride) {
+    sum += in[ri];
+    cws += 1.0f;
+    out[ri - oi_off] = sum / cws;
+  }
+  const int64_t p3_end = (int64_t)len * stride + start;
+  for (int64_t ri = p2_end; ri < p3_end; ri += stride) {
+    const int64_t oi = ri - oi_off;
+    sum += in[ri];
+    sum -= in[oi - li_off];
+    out[oi] = sum / cws;
+  }
+  const int64_t p4_start = (int64_t)(len - half + 1) * stride + start;
+  for (int64_t oi = p4_start; oi < p3_end; oi += stride) {
+    sum -= in[oi - li_off];
+    cws += -1.0f;
+    out[oi] = sum / cws;
+  }
+}
+
+/* ReferenceKernel<f32>::jarosz_compress (src/kernel/mod.rs:790-820): jarosz_filter_float
+ * (two repetitions of a box filter along rows then along columns, src/kernel/ref.rs) on the
+ * whole 512x512 image, then samples ((2 o + 1) 512) / 254 in each dimension. */
+YPDQO_EXPORT void ypdqo_jarosz_compress(const float* img, float* out /* 127*127 */) {
+  const int w = jarosz_window(512, 127);
+  float* buf = (float*)malloc(512 * 512 * sizeof(float));
+  float* tmp = (float*)malloc(512 * 512 * sizeof(float));
+  memcpy(buf, img, 512 * 512 * sizeof(float));
+  for (int rep = 0; rep < 2; rep++) {
+    for (int i = 0; i < 512; i++) box_one_d(buf, (int64_t)i * 512, tmp, 512, 1, w);
+    for (int j = 0; j < 512; j++) box_one_d(tmp, j, buf, 512, 512, w);
+  }
+  for (int oi = 0; oi < 127; oi++) {
+    const int ini = ((oi * 2 + 1) * 512) / (127 * 2);
+    for (int oj = 0; oj < 127; oj++) {
+      const int inj = ((oj * 2 + 1) * 512) / (127 * 2);
+      out[oi * 127 + oj] = buf[ini * 512 + inj];
+    }
+  }
+  free(tmp);
+  free(buf);
+}
+
+/* ReferenceKernel<f32>::dct2d (src/kernel/mod.rs:711-735): one sequential accumulator per
+ * output, row pass then column pass. */
+YPDQO_EXPORT void ypdqo_dct2d_reference(const float* buf /* 127*127 */, float* pdqf /* 256 */) {
+  init_constants();
+  float tmp[127];
+  for (int i = 0; i < 16; i++) {
+    for (int j = 0; j < 127; j++) {
+      float s = 0.0f;
+      for (int k = 0; k < 127; k++) s += DCT32[i * 127 + k] * buf[k * 127 + j];
+      tmp[j] = s;
+    }
+    for (int j = 0; j < 16; j++) {
+      float s = 0.0f;
+      for (int k = 0; k < 127; k++) s += tmp[k] * DCT32[j * 127 + k];
+      pdqf[i * 16 + j] = s;
+    }
+  }
+}
+
+typedef struct {
+  const void* imgs;
+  int is_u8;
+  uint32_t row_mask, col_mask;
+  uint8_t* hashes;
+  float *quality, *thresholds, *pdqf, *buf127;
+} ref_batch_ctx;
+
+static void ref_batch_range(void* vctx, int64_t b, int64_t e) {
+  ref_batch_ctx* c = (ref_batch_ctx*)vctx;
+  float* img = (float*)malloc(512 * 512 * sizeof(float));
+  float* bb = (float*)malloc(127 * 127 * sizeof(float));
+  for (int64_t n = b; n < e; n++) {
+    if (c->is_u8) {
+      const uint8_t* u = (const uint8_t*)c->imgs + n * 512 * 512;
+      for (int i = 0; i < 512 * 512; i++) img[i] = (float)u[i];
+    } else {
+      memcpy(img, (const float*)c->imgs + n * 512 * 512, 512 * 512 * sizeof(float));
+    }
+    float p[256], t;
+    ypdqo_jarosz_compress(img, bb);
+    ypdqo_dct2d_reference(bb, p);
+    c->quality[n * 8] = ypdqo_adjust_quality(ypdqo_sum_of_gradients(p));
+    ypdqo_quantize(p, &t, c->hashes + n * 256);
+    c->thresholds[n * 8] = t;
+    if (c->pdqf) memcpy(c->pdqf + n * 256, p, sizeof(p));
+    if (c->buf127) memcpy(c->buf127 + n * 127 * 127, bb, 127 * 127 * sizeof(float));
+    ypdqo_dihedrals(p, t, c->row_mask, c->col_mask, c->hashes + n * 256 + 32,
+                    c->thresholds + n * 8 + 1, c->quality + n * 8 + 1, NULL);
+  }
+  free(bb);
+  free(img);
+}
+
+/* ReferenceKernel<f32> (the pdqhash-faithful kernel) over n images, with the dihedrals. */
+YPDQO_EXPORT void ypdqo_hash_batch_reference(const void* imgs, int64_t n, int is_u8,
+                                             uint32_t row_mask, uint32_t col_mask,
+                                             uint8_t* hashes, float* quality, float* thresholds,
+                                             float* pdqf, float* buf127, int nthreads) {
+  init_constants();
+  ref_batch_ctx c = {imgs, is_u8, row_mask, col_mask, hashes, quality, thresholds, pdqf, buf127};
+  parallel_ranges(ref_batch_range, &c, n, nthreads);
+}

@@ -253,3 +253,33 @@ def test_rgb_input_variants_match_luma_input(ctx, yp, oracle, prec):
     for k in ("hashes", "quality", "thresholds", "pdqf"):
         assert np.array_equal(a[k], c[k]), k
         assert np.array_equal(b[k], c[k]), k
+
+
+JAROSZ = 0x200  # YPDQ_COMPRESS_JAROSZ
+
+
+@pytest.mark.parametrize("u8", [False, True])
+def test_reference_kernel_bit_exact(ctx, yp, oracle, u8):
+    """YPDQ_COMPRESS_JAROSZ = ReferenceKernel<f32>: full Jarosz filter, sequential DCT, the
+    trait-default (scalar) dihedrals; bit-exact with the oracle, across the 512-image chunk
+    boundary of the filter's scratch."""
+    base, kind = yp.synth.mixed_images(13, seed=801)
+    imgs = np.concatenate([base] * 40)  # 520 images
+    if u8:
+        imgs = yp.synth.to_u8(imgs)
+    got = yp.hash_batch(ctx, imgs, dct=JAROSZ, semantics="scalar", want_pdqf=True, want_buf1=True)
+    h, q, t, p, b = oracle.hash_batch_reference(imgs[:13], semantics="scalar")
+    for k in (0, 21, 39):  # repeats of the 13 distinct images, incl. the second chunk
+        sl = slice(13 * k, 13 * k + 13)
+        assert np.array_equal(got["hashes"][sl], h)
+        assert np.array_equal(got["quality"][sl], q)
+        assert np.array_equal(got["thresholds"][sl], t)
+        assert np.array_equal(got["pdqf"][sl, 0].view(np.uint32), p.view(np.uint32))
+        assert np.array_equal(got["buf1"][sl].view(np.uint32), b.view(np.uint32))
+
+
+def test_reference_kernel_rgba(ctx, yp, oracle):
+    rgba = yp.synth.color_images(3, seed=802, channels=4)
+    got = yp.hash_batch(ctx, rgba, dct=JAROSZ, semantics="scalar")
+    h, q, t, p, b = oracle.hash_batch_reference(oracle.luma(rgba), semantics="scalar")
+    assert np.array_equal(got["hashes"], h) and np.array_equal(got["quality"], q)

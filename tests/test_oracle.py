@@ -201,3 +201,26 @@ def test_luma_matches_reference_order(oracle):
     assert np.array_equal(got4, got3)  # alpha ignored
     red = oracle.luma(np.array([[255, 0, 0]], np.uint8))[0]
     assert red == np.float32(0.299) * np.float32(255.0)
+
+
+def test_jarosz_compress_semantics(oracle, yp):
+    """ReferenceKernel<f32>::jarosz_compress (src/kernel/ref.rs): two passes of a box filter of
+    window ceil(512/254) = 3 along rows then columns, windows shrinking to 2 at the edges,
+    sampled at ((2 o + 1) 512) / 254. The oracle's f32 running sums agree with a direct FP64
+    evaluation of that definition to f32 rounding."""
+    img = yp.synth.blob_images(1, seed=12)[0]
+
+    def box(a, axis):
+        a = np.moveaxis(a, axis, -1)
+        out = np.empty_like(a)
+        for i in range(a.shape[-1]):
+            out[..., i] = a[..., max(0, i - 1):i + 2].mean(-1)
+        return np.moveaxis(out, -1, axis)
+
+    y = img.astype(np.float64)
+    for _ in range(2):
+        y = box(box(y, 1), 0)
+    idx = ((2 * np.arange(127) + 1) * 512) // 254
+    want = y[np.ix_(idx, idx)]
+    got = oracle.jarosz_compress(img)
+    assert np.abs(got - want).max() / np.abs(want).max() < 1e-5

@@ -116,6 +116,7 @@ ypdq_status ypdq_ctx_create(int device, ypdq_ctx** out) {
   cudaError_t e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = upload_constants();
   if (e == cudaSuccess) e = scan_init();
+  if (e == cudaSuccess) e = jarosz_init();
   if (e == cudaSuccess) e = hash_occupancy(0, &ctx->hash_ctas_f32);
   if (e == cudaSuccess) e = hash_occupancy(1, &ctx->hash_ctas_u8);
   for (int u = 0; u < 4 && e == cudaSuccess; ++u)
@@ -126,6 +127,7 @@ ypdq_status ypdq_ctx_create(int device, ypdq_ctx** out) {
   if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->jarosz_done, cudaEventDisableTiming);
   for (int i = 0; i < ypdq_ctx::kMaxChunks && e == cudaSuccess; ++i)
     e = cudaEventCreateWithFlags(&ctx->chunk_copied[i], cudaEventDisableTiming);
   if (e != cudaSuccess) {
@@ -149,6 +151,8 @@ ypdq_status ypdq_ctx_destroy(ypdq_ctx* ctx) {
   cudaDeviceSynchronize();
   for (int i = 0; i < 8; ++i)
     if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
+  if (ctx->jarosz_scratch) cudaFree(ctx->jarosz_scratch);
+  if (ctx->jarosz_done) cudaEventDestroy(ctx->jarosz_done);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
@@ -206,8 +210,9 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
     return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
   if (semantics < YPDQ_DIHEDRAL_EXACT || semantics > YPDQ_DIHEDRAL_SCALAR)
     return fail(YPDQ_ERR_INVALID, "semantics %d", semantics);
+  const bool jarosz = dct_precision == YPDQ_COMPRESS_JAROSZ;
   int dct = 0, sep = 0;
-  if (!parse_precision(dct_precision, &dct, &sep))
+  if (!jarosz && !parse_precision(dct_precision, &dct, &sep))
     return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
   if (d_pdqf && pdqf_slots != 1 && pdqf_slots != 8)
     return fail(YPDQ_ERR_INVALID, "pdqf_slots must be 1 or 8");
@@ -227,6 +232,27 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
   p.dev_err = ctx->d_err;
   p.dct = dct;
   p.separable = sep;
+  if (jarosz) {
+    // The filter passes need two f32 planes per image in flight: a context-owned scratch
+    // for chunks of up to 512 images (1 GiB; each pass then runs 512 threads per image, one
+    // per line, enough to fill the GPU). Calls on different streams take turns on it: each
+    // waits for the previous user's completion event and records its own.
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int64_t chunk = n < 512 ? (n > 0 ? n : 1) : 512;
+    const size_t need = jarosz_scratch_bytes(chunk);
+    if (ctx->jarosz_bytes < need) {
+      if (ctx->jarosz_scratch) CK(cudaFree(ctx->jarosz_scratch), "cudaFree(jarosz scratch)");
+      ctx->jarosz_scratch = nullptr;
+      ctx->jarosz_bytes = 0;
+      CK(cudaMalloc(&ctx->jarosz_scratch, need), "cudaMalloc(jarosz scratch)");
+      ctx->jarosz_bytes = need;
+    }
+    CK(cudaStreamWaitEvent(s, ctx->jarosz_done, 0), "wait jarosz scratch");
+    CK(launch_hash_jarosz(p, ctx->jarosz_scratch, chunk, s), "jarosz launch");
+    CK(cudaEventRecord(ctx->jarosz_done, s), "record jarosz scratch");
+    return YPDQ_OK;
+  }
   CK(launch_hash(p, ctx->num_sms, ctx->hash_ctas[p.input_kind][dct][sep],
                  reinterpret_cast<cudaStream_t>(stream)),
      "hash kernel launch");

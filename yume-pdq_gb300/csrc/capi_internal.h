@@ -23,6 +23,9 @@ struct ypdq_ctx {
   std::mutex mu;                  // guards the scratch buffers below
   void* scratch[8] = {};
   size_t scratch_bytes[8] = {};
+  void* jarosz_scratch = nullptr;  // YPDQ_COMPRESS_JAROSZ filter planes
+  size_t jarosz_bytes = 0;
+  cudaEvent_t jarosz_done = nullptr;  // recorded after the last work that used it
 };
 
 struct ypdq_db {

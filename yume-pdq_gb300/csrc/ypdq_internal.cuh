@@ -204,6 +204,12 @@ cudaError_t hash_occupancy_variant(int input_kind, int dct, int separable, int* 
 cudaError_t launch_hash(const HashLaunch& p, int num_sms, int ctas_per_sm, cudaStream_t s);
 cudaError_t launch_dihedrals(const DihedralLaunch& p, cudaStream_t s);
 
+// jarosz.cu: ReferenceKernel<f32> (full Jarosz compress, sequential DCT) over p.n images in
+// chunks of `chunk`, using `scratch` (jarosz_scratch_bytes(chunk) bytes).
+cudaError_t jarosz_init();
+size_t jarosz_scratch_bytes(int64_t chunk);
+cudaError_t launch_hash_jarosz(const HashLaunch& p, void* scratch, int64_t chunk, cudaStream_t s);
+
 // scan.cu
 cudaError_t scan_init();
 cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t s);
