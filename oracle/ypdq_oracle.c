@@ -456,14 +456,34 @@ typedef struct {
   int64_t* counts;
 } count_ctx;
 
+/* The scalar CpuMatcher's inner loop (src/matching/mod.rs:231-257): each database row is
+ * loaded once and compared with the needles in fixed blocks of 8 (the matcher's batch of
+ * needles, unrolled at compile time there as here), counting without branches. */
+static inline int64_t count_block8(uint64_t a0, uint64_t a1, uint64_t a2, uint64_t a3,
+                                   const uint64_t* n, uint32_t t) {
+  int64_t c = 0;
+  for (int k = 0; k < 8; k++) {
+    const uint32_t d = (uint32_t)(__builtin_popcountll(a0 ^ n[4 * k]) +
+                                  __builtin_popcountll(a1 ^ n[4 * k + 1]) +
+                                  __builtin_popcountll(a2 ^ n[4 * k + 2]) +
+                                  __builtin_popcountll(a3 ^ n[4 * k + 3]));
+    c += d <= t;
+  }
+  return c;
+}
+
 static void count_range(void* vctx, int64_t b, int64_t e) {
   count_ctx* c = (count_ctx*)vctx;
+  const int full = c->n_needles / 8 * 8;
   for (int64_t t = b; t < e; t++) {
     int64_t r0 = c->n_rows * t / c->nthreads, r1 = c->n_rows * (t + 1) / c->nthreads;
     int64_t cnt = 0;
     for (int64_t r = r0; r < r1; r++) {
       const uint64_t* row = c->db + r * 4;
-      for (int q = 0; q < c->n_needles; q++)
+      const uint64_t a0 = row[0], a1 = row[1], a2 = row[2], a3 = row[3];
+      for (int q = 0; q < full; q += 8)
+        cnt += count_block8(a0, a1, a2, a3, c->needles + q * 4, c->threshold);
+      for (int q = full; q < c->n_needles; q++)
         cnt += dist256(row, c->needles + q * 4) <= c->threshold;
     }
     c->counts[t] = cnt;
