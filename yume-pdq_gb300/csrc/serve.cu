@@ -262,6 +262,11 @@ void finish_step(ypdq_server* S, Slot& sl, cudaError_t q) {
       for (uint32_t i = 0; i < sl.reqs[r].n; ++i) img_req[o + i] = static_cast<uint32_t>(r);
       o += sl.reqs[r].n;
     }
+    // every hit names one of this step's 8 n queries; anything else is a device fault
+    for (uint64_t h = 0; h < total; ++h)
+      if (hits[h].query >= 8u * sl.n_images) st = YPDQ_ERR_CUDA;
+  }
+  if (st == YPDQ_OK) {
     for (uint64_t h = 0; h < total; ++h) ++counts[img_req[hits[h].query >> 3]];
     std::vector<uint64_t> pos(nr + 1, 0);
     for (size_t r = 0; r < nr; ++r) pos[r + 1] = pos[r] + counts[r];
