@@ -419,9 +419,11 @@ def run_ours(args):
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_value = world * B / e2e_s
     ctx.lib.ypdq_free_host(ctx.handle, h_img)
-    serve = serving(yp, ctx, db, batch, args)
-    large = large_db(yp, ctx, args)
-    dctv = dct_variants(yp, ctx, args) if args.dct_variants else None
+    # the serving sweep, the heavy-hit database and the precision variants describe one GPU:
+    # rank 0 runs them (the other replicas wait at the final barrier)
+    serve = serving(yp, ctx, db, batch, args) if rank == 0 else None
+    large = large_db(yp, ctx, args) if rank == 0 else None
+    dctv = dct_variants(yp, ctx, args) if args.dct_variants and rank == 0 else None
 
     hbm_peak, bf16_peak, peak_kind = measured_peaks()
     hash_avg = statistics.mean(hash_ms)
@@ -495,6 +497,8 @@ def run_ours(args):
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline(args, sample=args.cpu_sample)
         print(json.dumps(out))
+    if pg:
+        pg.barrier()
     ctx.close()
 
 
