@@ -258,18 +258,18 @@ def test_rgb_input_variants_match_luma_input(ctx, yp, oracle, prec):
 JAROSZ = 0x200  # YPDQ_COMPRESS_JAROSZ
 
 
-@pytest.mark.parametrize("u8", [False, True])
-def test_reference_kernel_bit_exact(ctx, yp, oracle, u8):
+@pytest.mark.parametrize("u8,reps", [(False, 40), (True, 160)])
+def test_reference_kernel_bit_exact(ctx, yp, oracle, u8, reps):
     """YPDQ_COMPRESS_JAROSZ = ReferenceKernel<f32>: full Jarosz filter, sequential DCT, the
-    trait-default (scalar) dihedrals; bit-exact with the oracle, across the 512-image chunk
-    boundary of the filter's scratch."""
+    trait-default (scalar) dihedrals; bit-exact with the oracle. The u8 case (2,080 images)
+    crosses the 2,048-image chunk boundary of the filter's scratch."""
     base, kind = yp.synth.mixed_images(13, seed=801)
-    imgs = np.concatenate([base] * 40)  # 520 images
     if u8:
-        imgs = yp.synth.to_u8(imgs)
+        base = yp.synth.to_u8(base)
+    imgs = np.concatenate([base] * reps)
     got = yp.hash_batch(ctx, imgs, dct=JAROSZ, semantics="scalar", want_pdqf=True, want_buf1=True)
-    h, q, t, p, b = oracle.hash_batch_reference(imgs[:13], semantics="scalar")
-    for k in (0, 21, 39):  # repeats of the 13 distinct images, incl. the second chunk
+    h, q, t, p, b = oracle.hash_batch_reference(base, semantics="scalar")
+    for k in (0, reps // 2 + 1, reps - 1):  # repeats of the 13 distinct images
         sl = slice(13 * k, 13 * k + 13)
         assert np.array_equal(got["hashes"][sl], h)
         assert np.array_equal(got["quality"][sl], q)
@@ -278,8 +278,11 @@ def test_reference_kernel_bit_exact(ctx, yp, oracle, u8):
         assert np.array_equal(got["buf1"][sl].view(np.uint32), b.view(np.uint32))
 
 
-def test_reference_kernel_rgba(ctx, yp, oracle):
-    rgba = yp.synth.color_images(3, seed=802, channels=4)
-    got = yp.hash_batch(ctx, rgba, dct=JAROSZ, semantics="scalar")
-    h, q, t, p, b = oracle.hash_batch_reference(oracle.luma(rgba), semantics="scalar")
+@pytest.mark.parametrize("channels", [3, 4])
+def test_reference_kernel_color(ctx, yp, oracle, channels):
+    """RGB8 / RGBA8 through the Jarosz path: BT.601 luma on load, then the f32 filter."""
+    rgb = yp.synth.color_images(3, seed=802, channels=channels)
+    got = yp.hash_batch(ctx, rgb, dct=JAROSZ, semantics="scalar", want_pdqf=True)
+    h, q, t, p, b = oracle.hash_batch_reference(oracle.luma(rgb), semantics="scalar")
     assert np.array_equal(got["hashes"], h) and np.array_equal(got["quality"], q)
+    assert np.array_equal(got["pdqf"][:, 0].view(np.uint32), p.view(np.uint32))

@@ -234,12 +234,13 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
   p.separable = sep;
   if (jarosz) {
     // The filter passes need two f32 planes per image in flight: a context-owned scratch
-    // for chunks of up to 512 images (1 GiB; each pass then runs 512 threads per image, one
-    // per line, enough to fill the GPU). Calls on different streams take turns on it: each
+    // for chunks of up to 2,048 images (4 GiB). Each pass runs one thread per line, 512 per
+    // image, so a chunk is about nine rounds of the GPU's resident warps and the last,
+    // partly filled round costs little. Calls on different streams take turns on it: each
     // waits for the previous user's completion event and records its own.
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    const int64_t chunk = n < 512 ? (n > 0 ? n : 1) : 512;
+    const int64_t chunk = n < 2048 ? (n > 0 ? n : 1) : 2048;
     const size_t need = jarosz_scratch_bytes(chunk);
     if (ctx->jarosz_bytes < need) {
       if (ctx->jarosz_scratch) CK(cudaFree(ctx->jarosz_scratch), "cudaFree(jarosz scratch)");

@@ -1,6 +1,7 @@
 """Time one kernel configuration of the library with CUDA events (a tuning aid).
 
     python yume-pdq_gb300/microbench.py hash --input u8 --dct 2 --images 4096
+    python yume-pdq_gb300/microbench.py hash --input u8 --jarosz --images 2048
     python yume-pdq_gb300/microbench.py scan --rows 10000000 --queries 2048 --algo 3
 
 `hash` times ypdq_hash_batch on device-resident seeded blob images (64 distinct images
@@ -27,6 +28,8 @@ def main(argv=None):
     h.add_argument("--images", type=int, default=4096)
     h.add_argument("--separable", action="store_true",
                    help="YPDQ_COMPRESS_SEPARABLE (not bit-exact with the reference)")
+    h.add_argument("--jarosz", action="store_true",
+                   help="YPDQ_COMPRESS_JAROSZ (ReferenceKernel<f32>; --dct is ignored)")
     s = sub.add_parser("scan")
     s.add_argument("--rows", type=int, default=10_000_000)
     s.add_argument("--queries", type=int, default=64)
@@ -55,10 +58,14 @@ def main(argv=None):
         d_img = ctx.to_device(np.concatenate([base] * reps)[: a.images])
         d_h, d_q = ctx.alloc(a.images * 256), ctx.alloc(a.images * 32)
         prec = a.dct | (0x100 if a.separable else 0)
-        c = ctypes.c_int()
-        yp._lib.check(ctx.lib.ypdq_hash_occupancy(ctx.handle, kind, prec, ctypes.byref(c)))
-        print("hash_kernel input %s dct %d separable %d: %d CTAs per SM"
-              % (a.input, a.dct, a.separable, c.value))
+        if a.jarosz:
+            prec = 0x200
+            print("jarosz input %s" % a.input)
+        else:
+            c = ctypes.c_int()
+            yp._lib.check(ctx.lib.ypdq_hash_occupancy(ctx.handle, kind, prec, ctypes.byref(c)))
+            print("hash_kernel input %s dct %d separable %d: %d CTAs per SM"
+                  % (a.input, a.dct, a.separable, c.value))
         for _ in range(a.reps):
             ctx.record(e0, stream)
             yp.core.hash_batch_device(ctx, d_img, a.images, kind, d_h, d_q, dct=prec,
