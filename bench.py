@@ -141,10 +141,10 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-def scan_algo_used(algo, nq):
-    """The algorithm ypdq_scan runs for YPDQ_SCAN_AUTO (mirrors launch_scan's choice)."""
+def scan_algo_used(algo, nq, threshold):
+    """The algorithm ypdq_scan runs for YPDQ_SCAN_AUTO (mirrors auto_scan_algo in scan.cu)."""
     if algo == 0:
-        return 1 if nq <= 2 else 3
+        return 1 if nq <= (40 if threshold <= 34 else 28 if threshold <= 62 else 16) else 3
     return algo
 
 
@@ -284,11 +284,49 @@ def large_db(yp, ctx, args, members=1000, trials=40, n_queries=1024):
             "db_bytes": n * 32, "points": points}
 
 
+def scan_sweep(yp, ctx, d_rows, n, d_hash, args, qs=(1, 8, 64, 256, 1024), reps=6):
+    """Scan only against the bench database: query batches of 1, 8, 64, 256 and 1,024 hashes
+    (the step's own dihedral hashes, whose near-duplicates are planted in the database) at
+    the bench threshold, through the SIMT scan, the tensor-core scan and YPDQ_SCAN_AUTO:
+    launch time (median of reps - 1 after one warm launch), database stream rate and its
+    fraction of the measured HBM copy rate. Every launch reads the whole database (larger
+    than L2)."""
+    hbm_peak, _, peak_kind = measured_peaks()
+    stream = ctx.stream()
+    e0, e1 = ctx.event(), ctx.event()
+    cap = 1 << 20
+    d_hits, d_cnt = ctx.alloc(cap * 16), ctx.alloc(8)
+    out = {"db_rows": n, "threshold": args.threshold, "hbm_peak_gbs": hbm_peak,
+           "peak_source": peak_kind, "points": []}
+    for q in qs:
+        pt = {"queries": q, "auto_algo": {1: "simt", 3: "tc"}[scan_algo_used(0, q, args.threshold)]}
+        for name, algo in (("simt", 1), ("tc", 3), ("auto", 0)):
+            ms = []
+            for rep in range(reps):
+                ctx.record(e0, stream)
+                yp.core.scan_device(ctx, d_rows, n, d_hash, q, args.threshold, d_hits, cap, d_cnt,
+                                    algo, stream)
+                ctx.record(e1, stream)
+                ctx.sync(stream)
+                if rep:
+                    ms.append(ctx.elapsed_ms(e0, e1))
+            t = statistics.median(ms)
+            gbs = n * 32 / (t / 1e3) / 1e9
+            pt[name] = {"ms": t, "db_GB_s": gbs, "frac_hbm": gbs / hbm_peak,
+                        "Gpairs_s": n * q / (t / 1e3) / 1e9}
+        pt["hits"] = int(d_cnt.download((1,), np.uint64)[0])
+        out["points"].append(pt)
+    d_hits.free()
+    d_cnt.free()
+    return out
+
+
 def dct_variants(yp, ctx, args, n_distinct=512, n_launch=4096):
     """4,096 images per launch (blob images with 25 % noise and 5 % constant ones), f32 and
     u8 input, DCT stage 1 in FP32 SIMT / TF32 / BF16x3, each with the reference-order and the
-    separable compress: launch throughput, coefficient error against an FP64 DCT of the
-    variant's own compressed images, hash-bit disagreement with the exact FP32 kernel."""
+    separable compress, and the ReferenceKernel (full Jarosz filter, sequential DCT): launch
+    throughput, coefficient error against an FP64 DCT of the variant's own compressed
+    images, hash-bit disagreement with the exact FP32 kernel."""
     import ctypes
     imgs, kind = yp.synth.mixed_images(n_distinct, seed=args.seed + 11)
     live = kind != 2  # constant images: PDQF is rounding noise, bits carry no information
@@ -304,7 +342,8 @@ def dct_variants(yp, ctx, args, n_distinct=512, n_launch=4096):
         d_img = ctx.to_device(np.concatenate([data] * (n_launch // n_distinct)))
         d_h, d_q = ctx.alloc(n_launch * 256), ctx.alloc(n_launch * 32)
         ref = yp.hash_batch(ctx, data, dct=0)
-        for dct in (0, 1, 2, 0x100, 0x101, 0x102):  # 0x100: YPDQ_COMPRESS_SEPARABLE
+        # 0x100: YPDQ_COMPRESS_SEPARABLE; 0x200: YPDQ_COMPRESS_JAROSZ (ReferenceKernel<f32>)
+        for dct in (0, 1, 2, 0x100, 0x101, 0x102, 0x200):
             ms = []
             for rep in range(6):
                 ctx.record(e0, stream)
@@ -315,11 +354,16 @@ def dct_variants(yp, ctx, args, n_distinct=512, n_launch=4096):
                 if rep:
                     ms.append(ctx.elapsed_ms(e0, e1))
             t = statistics.median(ms)
-            c = ctypes.c_int()
-            yp._lib.check(ctx.lib.ypdq_hash_occupancy(ctx.handle, ik, dct, ctypes.byref(c)))
-            v = {"input": name, "dct": ("fp32", "tf32", "bf16x3")[dct & 0xFF],
-                 "compress": "separable" if dct & 0x100 else "reference order", "ms": t,
-                 "images_s": n_launch / (t / 1e3), "ctas_per_sm": c.value,
+            ctas = None
+            if dct != 0x200:
+                c = ctypes.c_int()
+                yp._lib.check(ctx.lib.ypdq_hash_occupancy(ctx.handle, ik, dct, ctypes.byref(c)))
+                ctas = c.value
+            v = {"input": name,
+                 "dct": "fp32 sequential" if dct == 0x200 else ("fp32", "tf32", "bf16x3")[dct & 0xFF],
+                 "compress": ("jarosz filter (ReferenceKernel)" if dct == 0x200 else
+                              "separable" if dct & 0x100 else "reference order"), "ms": t,
+                 "images_s": n_launch / (t / 1e3), "ctas_per_sm": ctas,
                  "input_GB_s": n_launch * data[0].nbytes / (t / 1e3) / 1e9}
             got = yp.hash_batch(ctx, data, dct=dct, want_pdqf=True, want_buf1=True)
             b = got["buf1"][live].astype(np.float64)
@@ -423,12 +467,13 @@ def run_ours(args):
     # rank 0 runs them (the other replicas wait at the final barrier)
     serve = serving(yp, ctx, db, batch, args) if rank == 0 else None
     large = large_db(yp, ctx, args) if rank == 0 else None
+    sweep = scan_sweep(yp, ctx, d_rows, n, d_hash, args) if rank == 0 else None
     dctv = dct_variants(yp, ctx, args) if args.dct_variants and rank == 0 else None
 
     hbm_peak, bf16_peak, peak_kind = measured_peaks()
     hash_avg = statistics.mean(hash_ms)
     scan_avg = statistics.mean(scan_ms)
-    algo = scan_algo_used(args.algo, nq)
+    algo = scan_algo_used(args.algo, nq, args.threshold)
     scan_launches = 1 if algo == 3 else (nq + 2047) // 2048
     if scan_avg >= hash_avg and algo == 3:
         # tensor-core scan: 2 * 256 FP8 flops per (row, query) pair, one launch per step;
@@ -485,6 +530,7 @@ def run_ours(args):
                              "p99": 1000 * float(np.percentile(lat, 99)),
                              "at": "ypdq_screen_host of %d images" % B},
         "serving": serve,
+        "scan_sweep": sweep,
         "large_db": large,
         "dct_variants": dctv,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": B * 512 * 512 * 4,

@@ -14,6 +14,9 @@
 namespace ypdq {
 
 constexpr int kScanThreads = 256;
+// resident SIMT-scan blocks per SM (register-bound: two rows per thread in flight); its
+// grid-stride grid is exactly this many blocks per SM so that no block starts late
+constexpr int kSimtBlocksPerSm = 6;
 constexpr uint32_t kMaxSmemQueries = 2048;  // queries per launch (64 KiB of shared memory)
 
 // Hit emission from lanes that found a hit in the same converged step: one atomic per warp.
@@ -49,7 +52,45 @@ __device__ __forceinline__ uint4 ld_stream(const uint4* p) {
 
 // ------------------------------------------------------------------- SIMT
 
-__global__ void __launch_bounds__(kScanThreads)
+// Popcounts of several words through carry-save adders: a full adder turns three words into
+// a sum word and a carry word with x0 + x1 + x2 = s + 2 c bit by bit, so fewer popcounts
+// (the scarce pipe) are needed; the adders are single three-input logic ops.
+__device__ __forceinline__ void csa(uint32_t a, uint32_t b, uint32_t c, uint32_t& s, uint32_t& cy) {
+  s = a ^ b ^ c;
+  cy = (a & b) | (c & (a ^ b));
+}
+__device__ __forceinline__ uint32_t popc3(uint32_t x0, uint32_t x1, uint32_t x2) {
+  uint32_t s, c;
+  csa(x0, x1, x2, s, c);
+  return __popc(s) + 2 * __popc(c);
+}
+__device__ __forceinline__ uint32_t popc5(uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3,
+                                          uint32_t x4) {
+  uint32_t s1, c1, s2, c2;
+  csa(x0, x1, x2, s1, c1);
+  csa(s1, x3, x4, s2, c2);
+  return __popc(s2) + 2 * (__popc(c1) + __popc(c2));
+}
+__device__ __forceinline__ uint32_t popc8(uint4 x, uint4 y) {
+  uint32_t s1, c1, s2, c2, s3, c3, t1, f1;
+  csa(x.x, x.y, x.z, s1, c1);
+  csa(x.w, y.x, y.y, s2, c2);
+  csa(s1, s2, y.z, s3, c3);
+  const uint32_t ones = s3 ^ y.w, c4 = s3 & y.w;
+  csa(c1, c2, c3, t1, f1);
+  const uint32_t twos = t1 ^ c4, f2 = t1 & c4;
+  const uint32_t fours = f1 ^ f2, eights = f1 & f2;
+  return __popc(ones) + 2 * __popc(twos) + 4 * __popc(fours) + 8 * __popc(eights);
+}
+
+// kPrefix words (3, 5 or 8 of 8) are counted first. Their popcount is a lower bound of the
+// distance, so once it exceeds t in every lane of the warp no pair of this query can be a
+// hit; rows that pass are finished exactly, so hits and distances do not change. The host
+// picks kPrefix by threshold: a random row is 48 +- 5 bits from a query in 96 bits and
+// 80 +- 6 in 160, so for t <= 34 (or <= 62) nearly every warp stops after 2 (or 3) of the
+// 8 popcounts that a plain count needs; above that the whole row is counted with 4.
+template <int kPrefix>
+__global__ void __launch_bounds__(kScanThreads, kSimtBlocksPerSm)
     scan_simt_kernel(const uint4* __restrict__ rows, uint64_t n_rows,
                      const uint4* __restrict__ queries, uint32_t nq, uint32_t q_base,
                      uint32_t t, ypdq_hit* hits, uint64_t cap, unsigned long long* count,
@@ -62,20 +103,41 @@ __global__ void __launch_bounds__(kScanThreads)
   // Every lane of a warp runs the same number of iterations so the ballots stay converged.
   const uint64_t first = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t warp_first = first & ~31ull;
+  // the next row's loads are in flight while the queries run over the current one
+  uint4 na = make_uint4(0, 0, 0, 0), nb = make_uint4(0, 0, 0, 0);
+  const uint64_t r_first = warp_first + (threadIdx.x & 31);
+  if (r_first < n_rows) {
+    na = ld_stream(rows + 2 * r_first);
+    nb = ld_stream(rows + 2 * r_first + 1);
+  }
   for (uint64_t base = warp_first; base < n_rows; base += stride) {
     const uint64_t r = base + (threadIdx.x & 31);
     const bool valid = r < n_rows;
-    uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
-    if (valid) {
-      a = ld_stream(rows + 2 * r);
-      b = ld_stream(rows + 2 * r + 1);
+    const uint4 a = na, b = nb;
+    const uint64_t rn = r + stride;
+    if (rn < n_rows) {
+      na = ld_stream(rows + 2 * rn);
+      nb = ld_stream(rows + 2 * rn + 1);
     }
 #pragma unroll 4
     for (uint32_t q = 0; q < nq; ++q) {
-      const uint4 qa = sq[2 * q], qb = sq[2 * q + 1];
-      const uint32_t d = __popc(a.x ^ qa.x) + __popc(a.y ^ qa.y) + __popc(a.z ^ qa.z) +
-                         __popc(a.w ^ qa.w) + __popc(b.x ^ qb.x) + __popc(b.y ^ qb.y) +
-                         __popc(b.z ^ qb.z) + __popc(b.w ^ qb.w);
+      const uint4 qa = sq[2 * q];
+      uint32_t d;
+      if constexpr (kPrefix == 3) {
+        d = popc3(a.x ^ qa.x, a.y ^ qa.y, a.z ^ qa.z);
+        if (!__any_sync(0xffffffffu, d <= t)) continue;
+        const uint4 qb = sq[2 * q + 1];
+        d += popc5(a.w ^ qa.w, b.x ^ qb.x, b.y ^ qb.y, b.z ^ qb.z, b.w ^ qb.w);
+      } else if constexpr (kPrefix == 5) {
+        const uint4 qb = sq[2 * q + 1];
+        d = popc5(a.x ^ qa.x, a.y ^ qa.y, a.z ^ qa.z, a.w ^ qa.w, b.x ^ qb.x);
+        if (!__any_sync(0xffffffffu, d <= t)) continue;
+        d += popc3(b.y ^ qb.y, b.z ^ qb.z, b.w ^ qb.w);
+      } else {
+        const uint4 qb = sq[2 * q + 1];
+        d = popc8(make_uint4(a.x ^ qa.x, a.y ^ qa.y, a.z ^ qa.z, a.w ^ qa.w),
+                  make_uint4(b.x ^ qb.x, b.y ^ qb.y, b.z ^ qb.z, b.w ^ qb.w));
+      }
       const bool hit = valid && d <= t;
       if (__any_sync(0xffffffffu, hit)) emit_hits_ballot(hit, r, q_base + q, d, hits, cap, count);
     }
@@ -146,18 +208,31 @@ __global__ void __launch_bounds__(kScanThreads)
 
 cudaError_t scan_init() {
   const int smem = static_cast<int>(kMaxSmemQueries * 32);
-  cudaError_t e = cudaFuncSetAttribute(scan_simt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
+  cudaError_t e = cudaSuccess;
+  for (const void* f : {reinterpret_cast<const void*>(scan_simt_kernel<3>),
+                        reinterpret_cast<const void*>(scan_simt_kernel<5>),
+                        reinterpret_cast<const void*>(scan_simt_kernel<8>)}) {
+    e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+  }
   e = cudaFuncSetAttribute(scan_b1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   return scan_tc_init();
 }
 
+// SIMT is HBM-bound up to a few queries; past that it is bound by its popcount and logic
+// pipes, at 2, 3 or 4 popcounts per pair depending on the threshold (the prefix bound in
+// scan_simt_kernel), and the tensor-core pipeline's fixed cost per pass (about the time of
+// 40, 28 or 16 SIMT queries over the same rows) takes over.
+int auto_scan_algo(uint32_t n_queries, uint32_t threshold) {
+  const uint32_t simt_max = threshold <= 34 ? 40 : threshold <= 62 ? 28 : 16;
+  return n_queries <= simt_max ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;
+}
+
 cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t s) {
   cudaError_t e = p.append ? cudaSuccess : cudaMemsetAsync(p.count, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess || p.n_rows == 0 || p.n_queries == 0) return e;
-  // SIMT is HBM-bound up to a few queries and beats the tensor-core pipeline up to ~16.
-  if (algo == YPDQ_SCAN_AUTO) algo = p.n_queries <= 16 ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;
+  if (algo == YPDQ_SCAN_AUTO) algo = auto_scan_algo(p.n_queries, p.threshold);
   if (algo == YPDQ_SCAN_TC) return launch_scan_tc(p, num_sms, s);
   // a device-side query count needs the whole query set in one launch
   if (p.nq_dev && (algo != YPDQ_SCAN_SIMT || p.n_queries > kMaxSmemQueries))
@@ -175,11 +250,17 @@ cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t
           reinterpret_cast<const uint2*>(p.rows), p.n_rows, reinterpret_cast<const uint2*>(qptr),
           nq, p.query_base + q0, p.threshold, p.hits, p.capacity, p.count);
     } else {
-      uint64_t blocks = (p.n_rows + kScanThreads - 1) / kScanThreads;
-      const uint64_t cap_blocks = static_cast<uint64_t>(num_sms) * 8;
-      if (blocks > cap_blocks) blocks = cap_blocks;
       const size_t smem = static_cast<size_t>(nq) * 32;
-      scan_simt_kernel<<<static_cast<unsigned>(blocks), kScanThreads, smem, s>>>(
+      // blocks per SM: registers allow kSimtBlocksPerSm; the queries' shared memory (plus
+      // the 1 KiB the runtime reserves per block, of 228 KiB per SM) may allow fewer
+      const uint64_t fit = (228u << 10) / (smem + 1024);
+      uint64_t blocks = (p.n_rows + kScanThreads - 1) / kScanThreads;
+      const uint64_t cap_blocks =
+          static_cast<uint64_t>(num_sms) * (fit < kSimtBlocksPerSm ? fit : kSimtBlocksPerSm);
+      if (blocks > cap_blocks) blocks = cap_blocks;
+      auto kern = p.threshold <= 34 ? scan_simt_kernel<3>
+                  : p.threshold <= 62 ? scan_simt_kernel<5> : scan_simt_kernel<8>;
+      kern<<<static_cast<unsigned>(blocks), kScanThreads, smem, s>>>(
           reinterpret_cast<const uint4*>(p.rows), p.n_rows, reinterpret_cast<const uint4*>(qptr),
           nq, p.query_base + q0, p.threshold, p.hits, p.capacity, p.count, p.nq_dev);
     }

@@ -528,7 +528,7 @@ ypdq_status ypdq_server_create(ypdq_ctx* ctx, ypdq_db* db, const ypdq_server_con
   for (uint32_t b = 1; b <= cfg.max_step_images; b *= 2) {
     Bucket k;
     k.images = b;
-    k.algo = 8 * b <= 16 ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;  // the ypdq_scan AUTO rule
+    k.algo = auto_scan_algo(8 * b, cfg.threshold);  // the ypdq_scan AUTO rule
     S->buckets.push_back(k);
   }
   S->max_step = cfg.max_step_images;

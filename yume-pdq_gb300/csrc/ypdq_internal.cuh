@@ -213,6 +213,8 @@ cudaError_t launch_hash_jarosz(const HashLaunch& p, void* scratch, int64_t chunk
 // scan.cu
 cudaError_t scan_init();
 cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t s);
+// the algorithm YPDQ_SCAN_AUTO runs for n_queries queries at threshold t
+int auto_scan_algo(uint32_t n_queries, uint32_t threshold);
 cudaError_t launch_sort_hits(ypdq_hit* hits, uint64_t n, cudaStream_t s);
 
 // scan_tc.cu
