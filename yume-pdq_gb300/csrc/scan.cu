@@ -14,9 +14,6 @@
 namespace ypdq {
 
 constexpr int kScanThreads = 256;
-// resident SIMT-scan blocks per SM (register-bound: two rows per thread in flight); its
-// grid-stride grid is exactly this many blocks per SM so that no block starts late
-constexpr int kSimtBlocksPerSm = 6;
 constexpr uint32_t kMaxSmemQueries = 2048;  // queries per launch (64 KiB of shared memory)
 
 // Hit emission from lanes that found a hit in the same converged step: one atomic per warp.
@@ -89,57 +86,101 @@ __device__ __forceinline__ uint32_t popc8(uint4 x, uint4 y) {
 // picks kPrefix by threshold: a random row is 48 +- 5 bits from a query in 96 bits and
 // 80 +- 6 in 160, so for t <= 34 (or <= 62) nearly every warp stops after 2 (or 3) of the
 // 8 popcounts that a plain count needs; above that the whole row is counted with 4.
+// Rows per thread and resident blocks per SM of each variant (register-bound). With a
+// prefix bound a thread takes two rows, so each query's shared load, vote and loop step
+// serve both; the full count (4 popcounts per pair) runs out of registers first and keeps
+// one row at higher occupancy. The grid-stride grid is exactly this many blocks per SM so
+// that no block starts late.
+__host__ __device__ constexpr int simt_rows(int prefix) { return prefix == 8 ? 1 : 2; }
+__host__ __device__ constexpr int simt_blocks_per_sm(int prefix) { return prefix == 8 ? 6 : 4; }
+
 template <int kPrefix>
-__global__ void __launch_bounds__(kScanThreads, kSimtBlocksPerSm)
+__global__ void __launch_bounds__(kScanThreads, simt_blocks_per_sm(kPrefix))
     scan_simt_kernel(const uint4* __restrict__ rows, uint64_t n_rows,
                      const uint4* __restrict__ queries, uint32_t nq, uint32_t q_base,
                      uint32_t t, ypdq_hit* hits, uint64_t cap, unsigned long long* count,
                      const uint32_t* nq_dev) {
+  constexpr int R = simt_rows(kPrefix);
   extern __shared__ uint4 sq[];
   if (nq_dev) nq = min(*nq_dev, nq);
   for (uint32_t i = threadIdx.x; i < 2 * nq; i += blockDim.x) sq[i] = queries[i];
   __syncthreads();
-  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-  // Every lane of a warp runs the same number of iterations so the ballots stay converged.
-  const uint64_t first = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const uint64_t warp_first = first & ~31ull;
-  // the next row's loads are in flight while the queries run over the current one
-  uint4 na = make_uint4(0, 0, 0, 0), nb = make_uint4(0, 0, 0, 0);
-  const uint64_t r_first = warp_first + (threadIdx.x & 31);
-  if (r_first < n_rows) {
-    na = ld_stream(rows + 2 * r_first);
-    nb = ld_stream(rows + 2 * r_first + 1);
+  // A warp owns 32 R consecutive rows per step, lane l rows l + 32 i. Every lane of a warp
+  // runs the same number of steps so the ballots stay converged.
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = static_cast<uint64_t>(R) * gridDim.x * blockDim.x;
+  const uint64_t warp_first =
+      ((static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * (32 * R);
+  // the next step's rows are in flight while the queries run over the current ones
+  uint4 na[R], nb[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const uint64_t r = warp_first + lane + 32 * i;
+    na[i] = nb[i] = make_uint4(0, 0, 0, 0);
+    if (r < n_rows) {
+      na[i] = ld_stream(rows + 2 * r);
+      nb[i] = ld_stream(rows + 2 * r + 1);
+    }
   }
   for (uint64_t base = warp_first; base < n_rows; base += stride) {
-    const uint64_t r = base + (threadIdx.x & 31);
-    const bool valid = r < n_rows;
-    const uint4 a = na, b = nb;
-    const uint64_t rn = r + stride;
-    if (rn < n_rows) {
-      na = ld_stream(rows + 2 * rn);
-      nb = ld_stream(rows + 2 * rn + 1);
+    uint64_t r[R];
+    bool v[R];
+    uint4 a[R], b[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      r[i] = base + lane + 32 * i;
+      v[i] = r[i] < n_rows;
+      a[i] = na[i];
+      b[i] = nb[i];
+      if (r[i] + stride < n_rows) {
+        na[i] = ld_stream(rows + 2 * (r[i] + stride));
+        nb[i] = ld_stream(rows + 2 * (r[i] + stride) + 1);
+      }
     }
-#pragma unroll 4
+#pragma unroll(R == 1 ? 4 : 2)
     for (uint32_t q = 0; q < nq; ++q) {
       const uint4 qa = sq[2 * q];
-      uint32_t d;
+      uint32_t d[R];
       if constexpr (kPrefix == 3) {
-        d = popc3(a.x ^ qa.x, a.y ^ qa.y, a.z ^ qa.z);
-        if (!__any_sync(0xffffffffu, d <= t)) continue;
+        bool near = false;
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          d[i] = popc3(a[i].x ^ qa.x, a[i].y ^ qa.y, a[i].z ^ qa.z);
+          near |= d[i] <= t;
+        }
+        if (!__any_sync(0xffffffffu, near)) continue;
         const uint4 qb = sq[2 * q + 1];
-        d += popc5(a.w ^ qa.w, b.x ^ qb.x, b.y ^ qb.y, b.z ^ qb.z, b.w ^ qb.w);
+#pragma unroll
+        for (int i = 0; i < R; ++i)
+          d[i] += popc5(a[i].w ^ qa.w, b[i].x ^ qb.x, b[i].y ^ qb.y, b[i].z ^ qb.z, b[i].w ^ qb.w);
       } else if constexpr (kPrefix == 5) {
         const uint4 qb = sq[2 * q + 1];
-        d = popc5(a.x ^ qa.x, a.y ^ qa.y, a.z ^ qa.z, a.w ^ qa.w, b.x ^ qb.x);
-        if (!__any_sync(0xffffffffu, d <= t)) continue;
-        d += popc3(b.y ^ qb.y, b.z ^ qb.z, b.w ^ qb.w);
+        bool near = false;
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          d[i] = popc5(a[i].x ^ qa.x, a[i].y ^ qa.y, a[i].z ^ qa.z, a[i].w ^ qa.w, b[i].x ^ qb.x);
+          near |= d[i] <= t;
+        }
+        if (!__any_sync(0xffffffffu, near)) continue;
+#pragma unroll
+        for (int i = 0; i < R; ++i) d[i] += popc3(b[i].y ^ qb.y, b[i].z ^ qb.z, b[i].w ^ qb.w);
       } else {
         const uint4 qb = sq[2 * q + 1];
-        d = popc8(make_uint4(a.x ^ qa.x, a.y ^ qa.y, a.z ^ qa.z, a.w ^ qa.w),
-                  make_uint4(b.x ^ qb.x, b.y ^ qb.y, b.z ^ qb.z, b.w ^ qb.w));
+#pragma unroll
+        for (int i = 0; i < R; ++i)
+          d[i] = popc8(make_uint4(a[i].x ^ qa.x, a[i].y ^ qa.y, a[i].z ^ qa.z, a[i].w ^ qa.w),
+                       make_uint4(b[i].x ^ qb.x, b[i].y ^ qb.y, b[i].z ^ qb.z, b[i].w ^ qb.w));
       }
-      const bool hit = valid && d <= t;
-      if (__any_sync(0xffffffffu, hit)) emit_hits_ballot(hit, r, q_base + q, d, hits, cap, count);
+      bool h[R], any_hit = false;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        h[i] = v[i] && d[i] <= t;
+        any_hit |= h[i];
+      }
+      if (__any_sync(0xffffffffu, any_hit)) {
+#pragma unroll
+        for (int i = 0; i < R; ++i) emit_hits_ballot(h[i], r[i], q_base + q, d[i], hits, cap, count);
+      }
     }
   }
 }
@@ -251,15 +292,17 @@ cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t
           nq, p.query_base + q0, p.threshold, p.hits, p.capacity, p.count);
     } else {
       const size_t smem = static_cast<size_t>(nq) * 32;
-      // blocks per SM: registers allow kSimtBlocksPerSm; the queries' shared memory (plus
+      const int prefix = p.threshold <= 34 ? 3 : p.threshold <= 62 ? 5 : 8;
+      auto kern = prefix == 3 ? scan_simt_kernel<3> : prefix == 5 ? scan_simt_kernel<5>
+                                                                  : scan_simt_kernel<8>;
+      // blocks per SM: registers allow simt_blocks_per_sm; the queries' shared memory (plus
       // the 1 KiB the runtime reserves per block, of 228 KiB per SM) may allow fewer
       const uint64_t fit = (228u << 10) / (smem + 1024);
-      uint64_t blocks = (p.n_rows + kScanThreads - 1) / kScanThreads;
-      const uint64_t cap_blocks =
-          static_cast<uint64_t>(num_sms) * (fit < kSimtBlocksPerSm ? fit : kSimtBlocksPerSm);
+      const uint64_t bps = static_cast<uint64_t>(simt_blocks_per_sm(prefix));
+      const uint64_t rows_per_block = static_cast<uint64_t>(kScanThreads) * simt_rows(prefix);
+      uint64_t blocks = (p.n_rows + rows_per_block - 1) / rows_per_block;
+      const uint64_t cap_blocks = static_cast<uint64_t>(num_sms) * (fit < bps ? fit : bps);
       if (blocks > cap_blocks) blocks = cap_blocks;
-      auto kern = p.threshold <= 34 ? scan_simt_kernel<3>
-                  : p.threshold <= 62 ? scan_simt_kernel<5> : scan_simt_kernel<8>;
       kern<<<static_cast<unsigned>(blocks), kScanThreads, smem, s>>>(
           reinterpret_cast<const uint4*>(p.rows), p.n_rows, reinterpret_cast<const uint4*>(qptr),
           nq, p.query_base + q0, p.threshold, p.hits, p.capacity, p.count, p.nq_dev);
