@@ -220,14 +220,13 @@ __device__ __forceinline__ void load_row8(const float* row, int j, float x[8]) {
   x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
   x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
 }
+// u8 columns as exact floats through a byte permute and one add (byte_f), which keeps the
+// 27 conversions per compressed value off the quarter-rate conversion pipe.
 __device__ __forceinline__ void load_row8(const uint8_t* row, int j, float x[8]) {
   const uint32_t* r = reinterpret_cast<const uint32_t*>(row);
   uint32_t a = r[j], b = r[j + 1];
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    x[e] = static_cast<float>((a >> (8 * e)) & 0xffu);
-    x[4 + e] = static_cast<float>((b >> (8 * e)) & 0xffu);
-  }
+  x[0] = byte_f<0>(a); x[1] = byte_f<1>(a); x[2] = byte_f<2>(a); x[3] = byte_f<3>(a);
+  x[4] = byte_f<0>(b); x[5] = byte_f<1>(b); x[6] = byte_f<2>(b); x[7] = byte_f<3>(b);
 }
 
 #define YPDQ_W(di, dj) __uint_as_float(YPDQ_TENT_BITS_##di##_##dj)
