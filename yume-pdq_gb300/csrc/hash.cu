@@ -238,25 +238,48 @@ __device__ __forceinline__ void load_row8(const uint8_t* row, int j, float x[8])
   YPDQ_TAP(acc, di, 4, x[5]);         \
   YPDQ_TAP(acc, di, 5, x[6])
 
-// Compressed value (i, j): rows 4i+1 .. 4i+6 come from stage i (rows 0..3) and stage i+1
-// (rows 0..1); tap (di, dj) reads input column 4j+1+dj, which is x[1+dj].
-template <typename Tin, int kRow = 512>  // kRow: elements between consecutive rows
-__device__ __forceinline__ float compress_at(const Tin* st0, const Tin* st1, int j) {
+// Compressed value (i, j) in the reference's tap order: rows 4i+1 .. 4i+6 come from stage i
+// (rows 0..3) and stage i+1 (rows 0..1); tap (di, dj) reads input column 4j+1+dj, which is
+// x[1+dj]; row 4i+1 holds only the two residue taps. Called for consecutive output rows of
+// one column: the first two input rows of output row i + 1 (4i + 5, 4i + 6) are the last
+// two of row i, so their converted values (x[5], x[6] of the first; x[2..6] of the second)
+// stay in registers instead of being read and converted twice.
+struct CompressCarry {
+  float a5, a6;   // row 4i + 1: the residue taps' inputs
+  float b[5];     // row 4i + 2: x[2..6]
+};
+template <typename Tin, int kRow = 512>
+__device__ __forceinline__ float compress_next(const Tin* st0, const Tin* st1, int j, bool first,
+                                               CompressCarry& c) {
   float x[8];
   float s = 0.0f;
-  load_row8(st0 + 0 * kRow, j, x);  // row 4i+1: only the two residue taps are nonzero
-  YPDQ_TAP(s, 0, 4, x[5]);
-  YPDQ_TAP(s, 0, 5, x[6]);
-  load_row8(st0 + 1 * kRow, j, x);
-  YPDQ_ROW_TAPS(s, 1, x);
+  if (first) {
+    load_row8(st0 + 0 * kRow, j, x);
+    c.a5 = x[5];
+    c.a6 = x[6];
+    load_row8(st0 + 1 * kRow, j, x);
+#pragma unroll
+    for (int e = 0; e < 5; ++e) c.b[e] = x[2 + e];
+  }
+  YPDQ_TAP(s, 0, 4, c.a5);
+  YPDQ_TAP(s, 0, 5, c.a6);
+  YPDQ_TAP(s, 1, 1, c.b[0]);
+  YPDQ_TAP(s, 1, 2, c.b[1]);
+  YPDQ_TAP(s, 1, 3, c.b[2]);
+  YPDQ_TAP(s, 1, 4, c.b[3]);
+  YPDQ_TAP(s, 1, 5, c.b[4]);
   load_row8(st0 + 2 * kRow, j, x);
   YPDQ_ROW_TAPS(s, 2, x);
   load_row8(st0 + 3 * kRow, j, x);
   YPDQ_ROW_TAPS(s, 3, x);
   load_row8(st1 + 0 * kRow, j, x);
   YPDQ_ROW_TAPS(s, 4, x);
+  c.a5 = x[5];
+  c.a6 = x[6];
   load_row8(st1 + 1 * kRow, j, x);
   YPDQ_ROW_TAPS(s, 5, x);
+#pragma unroll
+  for (int e = 0; e < 5; ++e) c.b[e] = x[2 + e];
   return s;
 }
 
@@ -771,6 +794,7 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
         if (lane == 0) mbar_arrive(&sm.empty[g0 % kNumStages]);
       }
       HCarry hc{};
+      CompressCarry cc{};
       if (kSep && active)
         hcarry_init<CT, kCRow>(stage_ptr<Tin, CT, kNumStages>(sm, g0, warp), jc, hc);
       for (int i0 = 0; i0 < 128; i0 += 4) {
@@ -792,7 +816,7 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
               const CT* st0 = stage_ptr<Tin, CT, kNumStages>(sm, ga, warp);
               const CT* st1 = stage_ptr<Tin, CT, kNumStages>(sm, gb, warp);
               b[r] = kSep ? compress_separable<CT, kCRow>(st1, jc, hc)
-                          : compress_at<CT, kCRow>(st0, st1, jc);
+                          : compress_next<CT, kCRow>(st0, st1, jc, i == 0, cc);
               if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b[r];
             }
             if constexpr (!kRgb) {
@@ -859,6 +883,7 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
       if (lane == 0) mbar_arrive(&sm.empty[g0 % kNumStages]);
     }
     HCarry hc{};
+    CompressCarry cc{};
     if (kSep && active)
       hcarry_init<CT, kCRow>(stage_ptr<Tin, CT, kNumStages>(sm, g0, warp), jc, hc);
     for (int i0 = 0; i0 < 128; i0 += 4) {
@@ -879,7 +904,7 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
             const CT* st0 = stage_ptr<Tin, CT, kNumStages>(sm, ga, warp);
             const CT* st1 = stage_ptr<Tin, CT, kNumStages>(sm, gb, warp);
             b = kSep ? compress_separable<CT, kCRow>(st1, jc, hc)
-                     : compress_at<CT, kCRow>(st0, st1, jc);
+                     : compress_next<CT, kCRow>(st0, st1, jc, i == 0, cc);
             if (prm.buf1) prm.buf1[(n * 127 + i) * 128 + j] = b;
           }
           const float4* d4 = reinterpret_cast<const float4*>(&sm.dt[i][0]);
