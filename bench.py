@@ -54,6 +54,8 @@ def parse():
                     help="arrival window per serving rate (and for the saturation run)")
     ap.add_argument("--large-rows", type=int, default=100_000_000,
                     help="rows of the clustered heavy-hit database (0 skips it)")
+    ap.add_argument("--scan-sweep", type=int, default=1,
+                    help="1: report the 1/8/64/256/1024-query scan sweep (0 skips the section)")
     ap.add_argument("--dct-variants", type=int, default=1,
                     help="1: time and check the FP32 / TF32 / BF16x3 hash variants")
     return ap.parse_args()
@@ -467,7 +469,7 @@ def run_ours(args):
     # rank 0 runs them (the other replicas wait at the final barrier)
     serve = serving(yp, ctx, db, batch, args) if rank == 0 else None
     large = large_db(yp, ctx, args) if rank == 0 else None
-    sweep = scan_sweep(yp, ctx, d_rows, n, d_hash, args) if rank == 0 else None
+    sweep = scan_sweep(yp, ctx, d_rows, n, d_hash, args) if args.scan_sweep and rank == 0 else None
     dctv = dct_variants(yp, ctx, args) if args.dct_variants and rank == 0 else None
 
     hbm_peak, bf16_peak, peak_kind = measured_peaks()

@@ -87,8 +87,9 @@ typedef enum {
  * pdqhash-faithful kernel (src/kernel/mod.rs:690-820, src/kernel/ref.rs). Its compress runs
  * the full Jarosz filter (two box passes of window 3 along rows and columns of the whole
  * 512x512 image, running sums in f32) and samples it; its DCT sums each output in one
- * sequential accumulator. Bit-exact with that kernel for finite inputs. Slower (six passes
- * over the image); ypdq_hash_batch only.
+ * sequential accumulator. Bit-exact with that kernel for finite inputs. Slower (four passes
+ * over the image through two f32 planes per image; the context keeps up to 4 GiB of
+ * scratch for chunks of 2,048 images); ypdq_hash_batch only.
  */
 #define YPDQ_COMPRESS_JAROSZ 0x200
 
