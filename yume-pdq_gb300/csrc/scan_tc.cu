@@ -15,8 +15,14 @@
 //               accumulator out of TMEM is the scan's limit (one f16 per (row, query) pair
 //               against 256 MACs), so it gets twice the warps of the other roles.
 //   warp 8      producer: one lane bulk-copies packed tiles (128 rows x 32 B) into a ring.
-//   warp 9      MMA: allocates TMEM; one lane issues 8 x tcgen05.mma (M=128, N, K=32) per
-//               tile into a double-buffered accumulator and commits to mbarriers.
+//   warps 9, 14 MMA: one lane issues 8 x tcgen05.mma (M=128, N, K=32) per tile into a
+//               double-buffered accumulator and commits to mbarriers (tcgen05.commit tracks
+//               the issuing thread's own MMAs). Issuing and its barrier handoffs keep one
+//               thread busy ~1,100 clk per tile, longer than the MMAs of a pass of <= 128
+//               queries take on the tensor core; there the two warps take alternate tiles
+//               (one accumulator stage each; kDual), 7-14 % faster. Wider passes are
+//               tensor-bound and launch without warp 14. Warp 9 also allocates and frees
+//               TMEM.
 //   warps 10-13 expanders: packed bits -> FP8 +-1 in the 128B-swizzled K-major layout that
 //               the MMA descriptors describe (database tiles, and the queries once per pass).
 // Queries are processed in passes of N <= 256; the database streams once per pass. The
@@ -33,7 +39,8 @@ constexpr int kEpilogueWarps = 8;  // warps 0..7
 constexpr int kProducerWarp = 8;
 constexpr int kMmaWarp = 9;
 constexpr int kExpandWarp0 = 10;   // warps 10..13
-constexpr int kThreads = 14 * 32;
+constexpr int kMmaWarp2 = 14;      // the second MMA issuer (kDual only)
+__host__ __device__ constexpr int threads_of(bool dual) { return (dual ? 15 : 14) * 32; }
 constexpr int kTileRows = 128;
 constexpr int kMaxN = 256;
 constexpr int kMaxPackStages = 16;
@@ -171,7 +178,8 @@ __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
   atomicOr(dev_err, kDevErrTimeout);
 }
 
-__global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) {
+template <bool kDual>
+__global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Params prm) {
   extern __shared__ uint8_t smem_raw[];
   // Align by offsetting the shared array itself so the compiler keeps the shared address
   // space (an integer round trip would turn every access into a generic one).
@@ -205,9 +213,9 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
       mbar_init(&sm.acc_empty[s], kEpilogueWarps);
     }
     mbar_init(&sm.b_full, 4);
-    mbar_init(&sm.b_empty, 1);
+    mbar_init(&sm.b_empty, kDual ? 2 : 1);   // one commit per MMA issuer
     mbar_init(&sm.epi_exit, kEpilogueWarps);
-    mbar_init(&sm.mma_done, 1);
+    mbar_init(&sm.mma_done, kDual ? 2 : 1);
     sm.abort_flag = 0;
     fence_mbar_init();
   }
@@ -265,7 +273,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
     return;
   }
 
-  if (warp >= kExpandWarp0) {
+  if (warp >= kExpandWarp0 && warp < kExpandWarp0 + 4) {
     const int e = tid - kExpandWarp0 * 32;  // 0..127: tile row / query row
     uint32_t slot = 0, phase = 0, ga = 0;
     for (uint32_t p = 0; p < n_passes; ++p) {
@@ -312,8 +320,9 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
     return;
   }
 
-  if (warp == kMmaWarp) {
+  if (warp == kMmaWarp || (kDual && warp == kMmaWarp2)) {
     const uint32_t idesc = idesc_f8(N);
+    const uint32_t issuer = warp == kMmaWarp ? 0u : 1u;  // kDual: takes the tiles ga % 2 == issuer
     uint32_t ga = 0;
     bool ok = true;
     if (lane == 0) {
@@ -325,6 +334,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
         tc_fence_after();
         const uint32_t b0 = smem_u32(bchunk0), b1 = smem_u32(bchunk1);
         for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
+          if (kDual && (ga & 1u) != issuer) continue;
           const uint32_t as = ga % kAStages, ac = ga % kAccStages;
           if (!mbar_wait(&sm.a_full[as], (ga / kAStages) & 1u, abort_flag) ||
               !mbar_wait(&sm.acc_empty[ac], ((ga / kAccStages) & 1u) ^ 1u, abort_flag)) {
@@ -347,13 +357,14 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
         if (ok) mma_commit(&sm.b_empty);
       }
       if (!ok) raise_abort(sm, prm.dev_err);
-      // every MMA issued so far has completed once this commit arrives
+      // every MMA of both issuers has completed once both commits arrive
       mma_commit(&sm.mma_done);
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(&sm.mma_done, 0))
         if (globaltimer_ns() - t0 > kWaitLimitNs) break;
     }
     __syncwarp();
+    if (kDual && warp == kMmaWarp2) return;
     // the epilogue warps arrive on epi_exit when they stop reading TMEM
     {
       const uint64_t t0 = globaltimer_ns();
@@ -423,7 +434,12 @@ __global__ void __launch_bounds__(kThreads, 1) scan_tc_kernel(const Params prm) 
 }  // namespace tc
 
 cudaError_t scan_tc_init() {
-  return cudaFuncSetAttribute(tc::scan_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(tc::scan_tc_kernel<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(tc::kSmemLimit));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(tc::scan_tc_kernel<false>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                               static_cast<int>(tc::kSmemLimit));
 }
 
@@ -459,7 +475,11 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   const size_t smem = b_end + stages * tc::kPackBytes + 1024;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
-  tc::scan_tc_kernel<<<static_cast<unsigned>(grid), tc::kThreads, smem, s>>>(prm);
+  // passes of <= 128 queries: two MMA issuers (the pass is issue-bound, not tensor-bound)
+  if (prm.n_tile <= 128)
+    tc::scan_tc_kernel<true><<<static_cast<unsigned>(grid), tc::threads_of(true), smem, s>>>(prm);
+  else
+    tc::scan_tc_kernel<false><<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
   return cudaGetLastError();
 }
 
