@@ -23,8 +23,14 @@
 //               (one accumulator stage each; kDual), 7-14 % faster. Wider passes are
 //               tensor-bound and launch without warp 14. Warp 9 also allocates and frees
 //               TMEM.
-//   warps 10-13 expanders: packed bits -> FP8 +-1 in the 128B-swizzled K-major layout that
-//               the MMA descriptors describe (database tiles, and the queries once per pass).
+//   warps 10-13 expanders: packed bits -> FP8 +-1. The queries (B, once per pass) go to
+//               shared memory in the 128B-swizzled K-major layout that the MMA descriptors
+//               describe. The database tiles (A) go there too for passes of 256 queries;
+//               for <= 128 (kDual) they go straight into tensor memory with tcgen05.st (row
+//               r = TMEM lane r, K in column order) and the MMA reads A from there: a narrow
+//               pass is otherwise bound by shared-memory traffic (expansion stores plus the
+//               MMA's operand reads), and the columns the accumulators leave free hold 4-6
+//               tiles in flight.
 // Queries are processed in passes of N <= 256; the database streams once per pass. The
 // shared memory left after the operands holds as many packed tiles in flight as fit.
 #include <cuda_fp16.h>
@@ -44,24 +50,26 @@ __host__ __device__ constexpr int threads_of(bool dual) { return (dual ? 15 : 14
 constexpr int kTileRows = 128;
 constexpr int kMaxN = 256;
 constexpr int kMaxPackStages = 16;
-constexpr int kAStages = 4;
+constexpr int kAStages = 4;       // A tiles in shared memory (32 KiB each)
+constexpr int kMaxAStages = 6;    // A tiles in tensor memory (kDual; 64 columns each)
 constexpr int kAccStages = 2;
+constexpr int kTmemCols = 512;
 constexpr int kChunkBytes = kTileRows * 128;  // one 128-byte K-chunk of a 128-row tile
 constexpr int kPackBytes = kTileRows * 32;
 constexpr size_t kSmemLimit = 227 * 1024;
 
-// Fixed part of shared memory; the expanded queries (2 K-chunks of N x 128 B) and the
+// Fixed part of shared memory; the expanded tiles (shared-memory A only: kAStages x 2
+// K-chunks of 128 rows x 128 B), the expanded queries (2 K-chunks of N x 128 B) and the
 // packed ring follow it at 1024-byte aligned offsets computed per launch.
 struct Smem {
-  uint8_t a[kAStages][2][kChunkBytes];    // expanded tiles: 2 K-chunks of 128 rows x 128 B
   uint64_t pk_full[kMaxPackStages], pk_empty[kMaxPackStages];
-  uint64_t a_full[kAStages], a_empty[kAStages];
+  uint64_t a_full[kMaxAStages], a_empty[kMaxAStages];
   uint64_t acc_full[kAccStages], acc_empty[kAccStages];
-  uint64_t b_full, b_empty, epi_exit, mma_done;
+  uint64_t b_full, b_empty, epi_exit, exp_exit, mma_done;
   uint32_t tmem_base;
   int abort_flag;
 };
-constexpr size_t kBOffset = (sizeof(Smem) + 1023) & ~static_cast<size_t>(1023);
+constexpr size_t kFixedBytes = (sizeof(Smem) + 1023) & ~static_cast<size_t>(1023);
 
 __device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                        uint32_t idesc, uint32_t accumulate) {
@@ -72,6 +80,27 @@ __device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+// The same with A read from tensor memory (128 lanes = rows, K along the columns).
+__device__ __forceinline__ void mma_f8_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// Store 32 consecutive 32-bit columns of this warp's 32 TMEM lanes (one row per lane).
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 // Issue a load of 32 consecutive columns of this warp's 32 TMEM lanes. The registers are
 // written asynchronously: read them only through tmem_take() after tmem_ld_wait().
 __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
@@ -133,6 +162,25 @@ __device__ __forceinline__ void expand_row(const uint4 w0, const uint4 w1, uint8
   }
 }
 
+// The expansion of expand_row as 64 column words of one TMEM lane: K element 4 c + i is
+// byte i of column c. Output word (p, m) of expand_row holds K elements 32 p + 4 m .. + 3,
+// so it is column 8 p + m, and rows and queries keep the same bijection.
+__device__ __forceinline__ void expand_row_tmem(const uint4 w0, const uint4 w1,
+                                                uint32_t taddr) {
+  const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    uint32_t r[32];
+#pragma unroll
+    for (int pp = 0; pp < 4; ++pp) {
+      const uint32_t w = words[4 * half + pp];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) r[8 * pp + m] = ((w << m) & 0x80808080u) | 0x38383838u;
+    }
+    tmem_st32(taddr + 32 * half, r);
+  }
+}
+
 struct Params {
   const uint8_t* rows;
   uint64_t n_rows;
@@ -148,6 +196,8 @@ struct Params {
   const uint32_t* nq_dev; // device-side query count (graph replay), bounded by n_queries
   uint32_t pack_stages;   // packed tiles in flight (<= kMaxPackStages)
   uint32_t pack_offset;   // byte offset of the packed ring in shared memory
+  uint32_t a_stages;      // expanded tiles in flight
+  uint32_t b_offset;      // byte offset of the expanded queries
 };
 
 // Compact one column of hits across the warp (one atomic per warp with a hit).
@@ -189,7 +239,9 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
   const uint32_t N = prm.n_tile;
   const uint32_t n_pack = prm.pack_stages;
   const uint32_t n_queries = prm.nq_dev ? min(*prm.nq_dev, prm.n_queries) : prm.n_queries;
-  uint8_t* const bchunk0 = smem_base + kBOffset;      // N rows x 128 B (K 0..127)
+  const uint32_t n_a = kDual ? prm.a_stages : static_cast<uint32_t>(kAStages);
+  uint8_t* const a_smem = smem_base + kFixedBytes;    // [kAStages][2][kChunkBytes] (!kDual)
+  uint8_t* const bchunk0 = smem_base + prm.b_offset;  // N rows x 128 B (K 0..127)
   uint8_t* const bchunk1 = bchunk0 + N * 128;         // N rows x 128 B (K 128..255)
   uint8_t* const packed = smem_base + prm.pack_offset;
   const uint64_t n_tiles = (prm.n_rows + kTileRows - 1) / kTileRows;
@@ -204,22 +256,28 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
       mbar_init(&sm.pk_full[s], 1);
       mbar_init(&sm.pk_empty[s], 4);
     }
-    for (int s = 0; s < kAStages; ++s) {
+    for (uint32_t s = 0; s < n_a; ++s) {
       mbar_init(&sm.a_full[s], 4);
       mbar_init(&sm.a_empty[s], 1);
     }
     for (int s = 0; s < kAccStages; ++s) {
       mbar_init(&sm.acc_full[s], 1);
-      mbar_init(&sm.acc_empty[s], kEpilogueWarps);
+      // kDual with N = 64: each epilogue group drains one accumulator stage (alternate tiles)
+      mbar_init(&sm.acc_empty[s], kDual && N <= 64 ? kEpilogueWarps / 2 : kEpilogueWarps);
     }
     mbar_init(&sm.b_full, 4);
     mbar_init(&sm.b_empty, kDual ? 2 : 1);   // one commit per MMA issuer
     mbar_init(&sm.epi_exit, kEpilogueWarps);
+    mbar_init(&sm.exp_exit, 4);
     mbar_init(&sm.mma_done, kDual ? 2 : 1);
     sm.abort_flag = 0;
     fence_mbar_init();
   }
-  const uint32_t tmem_cols = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : (2 * N <= 256 ? 256 : 512)));
+  // columns: kAccStages accumulators of N, then (kDual) n_a A tiles of 64 columns
+  const uint32_t tmem_cols =
+      kDual ? static_cast<uint32_t>(kTmemCols)
+            : (2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : (2 * N <= 256 ? 256 : 512))));
+  const uint32_t a_col0 = kAccStages * N;
   if (warp == kMmaWarp) {
     tmem_alloc(&sm.tmem_base, tmem_cols);
     tmem_relinquish();
@@ -274,8 +332,11 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
   }
 
   if (warp >= kExpandWarp0 && warp < kExpandWarp0 + 4) {
-    const int e = tid - kExpandWarp0 * 32;  // 0..127: tile row / query row
-    uint32_t slot = 0, phase = 0, ga = 0;
+    const int e = tid - kExpandWarp0 * 32;  // 0..127: query row
+    // tile row: a warp may only access its own quarter of the TMEM lanes (warp % 4)
+    const int arow = kDual ? 32 * (warp & 3) + lane : e;
+    const uint32_t a_lane = static_cast<uint32_t>(32 * (warp & 3)) << 16;
+    uint32_t slot = 0, phase = 0, ga = 0, as_t = 0, aph_t = 0;  // as_t, aph_t: kDual stages
     for (uint32_t p = 0; p < n_passes; ++p) {
       // queries of this pass into B (N rows; padding rows are zero = contributes nothing)
       if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag)) goto fail;
@@ -297,9 +358,10 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
       if (lane == 0) mbar_arrive(&sm.b_full);
 
       for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
-        const uint32_t as = ga % kAStages;
+        const uint32_t as = kDual ? as_t : ga % kAStages;
+        const uint32_t aph = kDual ? aph_t : (ga / kAStages) & 1u;
         if (!mbar_wait(&sm.pk_full[slot], phase, abort_flag)) goto fail;
-        const uint4* src = reinterpret_cast<const uint4*>(packed + slot * kPackBytes + e * 32);
+        const uint4* src = reinterpret_cast<const uint4*>(packed + slot * kPackBytes + arow * 32);
         const uint4 w0 = src[0], w1 = src[1];
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.pk_empty[slot]);
@@ -307,23 +369,41 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           slot = 0;
           phase ^= 1u;
         }
-        if (!mbar_wait(&sm.a_empty[as], ((ga / kAStages) & 1u) ^ 1u, abort_flag)) goto fail;
-        expand_row(w0, w1, sm.a[as][0], sm.a[as][1], e);
-        fence_proxy_async_smem();
+        if (!mbar_wait(&sm.a_empty[as], aph ^ 1u, abort_flag)) goto fail;
+        if constexpr (kDual) {
+          __syncwarp();  // tcgen05.st is .sync.aligned: the lanes leave the wait one by one
+          expand_row_tmem(w0, w1, tmem_base + a_lane + a_col0 + 64 * as);
+          tmem_st_wait();
+          tc_fence_before();
+          if (++as_t == n_a) {
+            as_t = 0;
+            aph_t ^= 1u;
+          }
+        } else {
+          uint8_t* a = a_smem + static_cast<size_t>(as) * 2 * kChunkBytes;
+          expand_row(w0, w1, a, a + kChunkBytes, arow);
+          fence_proxy_async_smem();
+        }
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.a_full[as]);
       }
     }
+    // no TMEM access by this warp after this point
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.exp_exit);
     return;
   fail:
-    if (lane == 0) raise_abort(sm, prm.dev_err);
+    if (lane == 0) {
+      raise_abort(sm, prm.dev_err);
+      mbar_arrive(&sm.exp_exit);
+    }
     return;
   }
 
   if (warp == kMmaWarp || (kDual && warp == kMmaWarp2)) {
     const uint32_t idesc = idesc_f8(N);
     const uint32_t issuer = warp == kMmaWarp ? 0u : 1u;  // kDual: takes the tiles ga % 2 == issuer
-    uint32_t ga = 0;
+    uint32_t ga = 0, as_t = 0, aph_t = 0;  // as_t, aph_t: kDual stages, advanced every tile
     bool ok = true;
     if (lane == 0) {
       for (uint32_t p = 0; p < n_passes && ok; ++p) {
@@ -334,22 +414,38 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
         tc_fence_after();
         const uint32_t b0 = smem_u32(bchunk0), b1 = smem_u32(bchunk1);
         for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
+          const uint32_t as = kDual ? as_t : ga % kAStages;
+          const uint32_t aph = kDual ? aph_t : (ga / kAStages) & 1u;
+          if (kDual && ++as_t == n_a) {
+            as_t = 0;
+            aph_t ^= 1u;
+          }
           if (kDual && (ga & 1u) != issuer) continue;
-          const uint32_t as = ga % kAStages, ac = ga % kAccStages;
-          if (!mbar_wait(&sm.a_full[as], (ga / kAStages) & 1u, abort_flag) ||
+          const uint32_t ac = ga % kAccStages;
+          if (!mbar_wait(&sm.a_full[as], aph, abort_flag) ||
               !mbar_wait(&sm.acc_empty[ac], ((ga / kAccStages) & 1u) ^ 1u, abort_flag)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t a0 = smem_u32(sm.a[as][0]), a1 = smem_u32(sm.a[as][1]);
           const uint32_t d = tmem_base + ac * N;
+          if constexpr (kDual) {
+            const uint32_t ta = tmem_base + a_col0 + 64 * as;  // lane 0; K = 32 per 8 columns
 #pragma unroll
-          for (int ks = 0; ks < 8; ++ks) {
-            const uint32_t off = (ks & 3) * 32;
-            const uint64_t ad = sw128_desc((ks < 4 ? a0 : a1) + off);
-            const uint64_t bd = sw128_desc((ks < 4 ? b0 : b1) + off);
-            mma_f8(d, ad, bd, idesc, ks > 0 ? 1u : 0u);
+            for (int ks = 0; ks < 8; ++ks) {
+              const uint64_t bd = sw128_desc((ks < 4 ? b0 : b1) + (ks & 3) * 32);
+              mma_f8_ta(d, ta + 8 * ks, bd, idesc, ks > 0 ? 1u : 0u);
+            }
+          } else {
+            const uint32_t a0 = smem_u32(a_smem + static_cast<size_t>(as) * 2 * kChunkBytes);
+            const uint32_t a1 = a0 + kChunkBytes;
+#pragma unroll
+            for (int ks = 0; ks < 8; ++ks) {
+              const uint32_t off = (ks & 3) * 32;
+              const uint64_t ad = sw128_desc((ks < 4 ? a0 : a1) + off);
+              const uint64_t bd = sw128_desc((ks < 4 ? b0 : b1) + off);
+              mma_f8(d, ad, bd, idesc, ks > 0 ? 1u : 0u);
+            }
           }
           mma_commit(&sm.a_empty[as]);
           mma_commit(&sm.acc_full[ac]);
@@ -365,11 +461,15 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
     }
     __syncwarp();
     if (kDual && warp == kMmaWarp2) return;
-    // the epilogue warps arrive on epi_exit when they stop reading TMEM
+    // the epilogue warps arrive on epi_exit when they stop reading TMEM, the expanders on
+    // exp_exit when they stop writing it
     {
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(&sm.epi_exit, 0))
         if (globaltimer_ns() - t0 > kWaitLimitNs) break;
+      const uint64_t t1 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.exp_exit, 0))
+        if (globaltimer_ns() - t1 > kWaitLimitNs) break;
     }
     tc_fence_after();
     tmem_dealloc(tmem_base, tmem_cols);
@@ -377,17 +477,20 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
   }
 
   // ---- epilogue warps 0..7: rows (warp % 4) * 32 + lane of the tile; warp / 4 picks
-  // alternate 64-column chunks of the accumulator
+  // alternate 64-column chunks of the accumulator, or with kDual and N = 64 alternate tiles
+  // (one accumulator stage each), so that both groups work on a narrow pass
   {
     const float dot_min = 256.0f - 2.0f * static_cast<float>(prm.threshold);
     const uint32_t quarter = static_cast<uint32_t>(warp & 3);
     const uint32_t group = static_cast<uint32_t>(warp >> 2);
     const uint32_t lane_addr = (quarter * 32) << 16;
+    const bool by_tile = kDual && N <= 64;
     uint32_t ga = 0;
     bool ok = true;
     for (uint32_t p = 0; p < n_passes && ok; ++p) {
       const uint64_t q0 = static_cast<uint64_t>(p) * N;
       for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
+        if (by_tile && (ga & 1u) != group) continue;
         const uint64_t tile = blockIdx.x + k * gridDim.x;
         const uint32_t ac = ga % kAccStages;
         if (!mbar_wait(&sm.acc_full[ac], (ga / kAccStages) & 1u, abort_flag)) {
@@ -397,7 +500,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
         tc_fence_after();
         const uint64_t row = tile * kTileRows + quarter * 32 + lane;
         const bool row_ok = row < prm.n_rows;
-        for (uint32_t c0 = 64 * group; c0 < N; c0 += 64 * (kEpilogueWarps / 4)) {
+        for (uint32_t c0 = by_tile ? 0u : 64 * group; c0 < N; c0 += 64 * (kEpilogueWarps / 4)) {
           uint32_t raw[32];
           float unused[32];
           tmem_ld64_pack16_nowait(tmem_base + lane_addr + ac * N + c0, raw);
@@ -464,8 +567,20 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   prm.dev_err = p.dev_err;
   prm.query_base = p.query_base;
   prm.nq_dev = p.nq_dev;
-  // layout: [fixed Smem][B: 2 x N x 128][packed ring: stages x 4 KB], base aligned to 1024
-  const size_t b_end = tc::kBOffset + 2 * static_cast<size_t>(prm.n_tile) * 128;
+  // passes of <= 128 queries: two MMA issuers and A in tensor memory (the pass is bound by
+  // issuing and shared-memory traffic, not by the tensor core)
+  const bool dual = prm.n_tile <= 128;
+  uint32_t a_stages = tc::kAStages;
+  if (dual) {
+    a_stages = (tc::kTmemCols - tc::kAccStages * prm.n_tile) / 64;
+    if (a_stages > static_cast<uint32_t>(tc::kMaxAStages)) a_stages = tc::kMaxAStages;
+  }
+  prm.a_stages = a_stages;
+  // layout: [fixed Smem][A (shared-memory A only): 4 x 2 x 16 KB][B: 2 x N x 128]
+  //         [packed ring: stages x 4 KB], base aligned to 1024
+  prm.b_offset = static_cast<uint32_t>(
+      tc::kFixedBytes + (dual ? 0 : static_cast<size_t>(tc::kAStages) * 2 * tc::kChunkBytes));
+  const size_t b_end = prm.b_offset + 2 * static_cast<size_t>(prm.n_tile) * 128;
   const size_t avail = tc::kSmemLimit - 1024 - b_end;
   size_t stages = avail / tc::kPackBytes;
   if (stages > static_cast<size_t>(tc::kMaxPackStages)) stages = tc::kMaxPackStages;
@@ -475,8 +590,7 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   const size_t smem = b_end + stages * tc::kPackBytes + 1024;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
-  // passes of <= 128 queries: two MMA issuers (the pass is issue-bound, not tensor-bound)
-  if (prm.n_tile <= 128)
+  if (dual)
     tc::scan_tc_kernel<true><<<static_cast<unsigned>(grid), tc::threads_of(true), smem, s>>>(prm);
   else
     tc::scan_tc_kernel<false><<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
