@@ -146,7 +146,7 @@ def measured_peaks():
 def scan_algo_used(algo, nq, threshold):
     """The algorithm ypdq_scan runs for YPDQ_SCAN_AUTO (mirrors auto_scan_algo in scan.cu)."""
     if algo == 0:
-        return 1 if nq <= (40 if threshold <= 34 else 28 if threshold <= 62 else 16) else 3
+        return 1 if nq <= (36 if threshold <= 34 else 24 if threshold <= 62 else 12) else 3
     return algo
 
 

@@ -264,9 +264,9 @@ cudaError_t scan_init() {
 // SIMT is HBM-bound up to a few queries; past that it is bound by its popcount and logic
 // pipes, at 2, 3 or 4 popcounts per pair depending on the threshold (the prefix bound in
 // scan_simt_kernel), and the tensor-core pipeline's fixed cost per pass (about the time of
-// 40, 28 or 16 SIMT queries over the same rows) takes over.
+// 36, 24 or 12 SIMT queries over the same rows) takes over.
 int auto_scan_algo(uint32_t n_queries, uint32_t threshold) {
-  const uint32_t simt_max = threshold <= 34 ? 40 : threshold <= 62 ? 28 : 16;
+  const uint32_t simt_max = threshold <= 34 ? 36 : threshold <= 62 ? 24 : 12;
   return n_queries <= simt_max ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;
 }
 
