@@ -89,7 +89,8 @@ typedef enum {
  * 512x512 image, running sums in f32) and samples it; its DCT sums each output in one
  * sequential accumulator. Bit-exact with that kernel for finite inputs. Slower (four passes
  * over the image through two f32 planes per image; the context keeps up to 4 GiB of
- * scratch for chunks of 2,048 images); ypdq_hash_batch only.
+ * scratch for chunks of 2,048 images, and each server slot 2 MiB per image of its step).
+ * Accepted by ypdq_hash_batch, ypdq_screen_host and ypdq_server_config.dct_precision.
  */
 #define YPDQ_COMPRESS_JAROSZ 0x200
 

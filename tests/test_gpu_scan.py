@@ -154,6 +154,24 @@ def test_screen_host_end_to_end(ctx, yp, oracle):
     assert np.array_equal(as_tuples(hits2), as_tuples(want))
 
 
+def test_screen_host_reference_kernel(ctx, yp, oracle):
+    """ypdq_screen_host with YPDQ_COMPRESS_JAROSZ: the hashes are ypdq_hash_batch's
+    ReferenceKernel hashes (pinned to the oracle in test_gpu_hash.py) and the hits are the
+    scalar matcher's over them; 70 images span two screening chunks."""
+    imgs = yp.synth.blob_images(70, seed=51)
+    want_h = yp.hash_batch(ctx, imgs, dct=0x200)["hashes"]
+    queries = want_h.reshape(-1, 32)
+    rows = yp.synth.rows_128(40000, seed=52)
+    yp.synth.plant(rows, queries, 400, 0, 40, seed=53)
+    db = yp.Database(ctx, rows)
+    hits, hashes = yp.screen_host(ctx, db, imgs, threshold=31, dct=0x200, want_hashes=True)
+    assert np.array_equal(hashes, want_h)
+    want = oracle.find_all(rows, queries, 31)
+    assert len(want) > 0
+    assert np.array_equal(as_tuples(hits), as_tuples(want))
+    db.close()
+
+
 def test_synth_rows_match_cpu_twin(ctx, yp, oracle):
     n = 20000
     d = ctx.alloc(n * 32)

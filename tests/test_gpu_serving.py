@@ -4,7 +4,8 @@ Each request's result must not depend on what else was on the device: the hits o
 screened alone, the hits of the same request inside a mix of concurrent requests, and the
 hits of ypdq_screen_host on those images are the same (index, query, distance) lists, in
 (index, query) order, bit for bit; so are its 8 dihedral hashes. That holds for every DCT
-precision because each image is hashed by one CTA independently of its batch neighbours.
+precision because each image is hashed independently of its batch neighbours (by one CTA,
+or for the ReferenceKernel by per-line running sums within the image).
 """
 import numpy as np
 import pytest
@@ -34,7 +35,7 @@ def request_slices(rng, n_req):
     return [(int(rng.integers(0, POOL - n + 1)), int(n)) for n in sizes]
 
 
-@pytest.mark.parametrize("dct", [0, 2])
+@pytest.mark.parametrize("dct", [0, 2, 0x200])  # FP32, BF16x3, YPDQ_COMPRESS_JAROSZ
 def test_same_alone_and_in_mix(ctx, yp, workload, dct):
     imgs, rows, db = workload
     reqs = request_slices(np.random.default_rng(40 + dct), 36)

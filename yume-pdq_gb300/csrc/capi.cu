@@ -97,6 +97,31 @@ namespace ypdq {
 void set_last_error_text(const char* text) { g_last_error = text; }
 }  // namespace ypdq
 
+namespace {
+
+// YPDQ_COMPRESS_JAROSZ: the filter passes need two f32 planes per image in flight, in a
+// context-owned scratch for chunks of up to 2,048 images (4 GiB). Each pass runs one thread
+// per line, 512 per image, so a chunk is about nine rounds of the GPU's resident warps and
+// the last, partly filled round costs little. Calls on different streams take turns on it
+// (under ctx->mu): each waits for the previous user's completion event (jarosz_done) and
+// records its own.
+int64_t jarosz_chunk(int64_t n) { return n < 2048 ? (n > 0 ? n : 1) : 2048; }
+
+ypdq_status ensure_jarosz_scratch(ypdq_ctx* ctx, int64_t chunk) {
+  const size_t need = jarosz_scratch_bytes(chunk);
+  if (ctx->jarosz_bytes >= need) return YPDQ_OK;
+  // the previous user may still be running on another stream
+  CK(cudaEventSynchronize(ctx->jarosz_done), "wait jarosz scratch");
+  if (ctx->jarosz_scratch) CK(cudaFree(ctx->jarosz_scratch), "cudaFree(jarosz scratch)");
+  ctx->jarosz_scratch = nullptr;
+  ctx->jarosz_bytes = 0;
+  CK(cudaMalloc(&ctx->jarosz_scratch, need), "cudaMalloc(jarosz scratch)");
+  ctx->jarosz_bytes = need;
+  return YPDQ_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 // ----------------------------------------------------------------- context
@@ -233,22 +258,10 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
   p.dct = dct;
   p.separable = sep;
   if (jarosz) {
-    // The filter passes need two f32 planes per image in flight: a context-owned scratch
-    // for chunks of up to 2,048 images (4 GiB). Each pass runs one thread per line, 512 per
-    // image, so a chunk is about nine rounds of the GPU's resident warps and the last,
-    // partly filled round costs little. Calls on different streams take turns on it: each
-    // waits for the previous user's completion event and records its own.
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    const int64_t chunk = n < 2048 ? (n > 0 ? n : 1) : 2048;
-    const size_t need = jarosz_scratch_bytes(chunk);
-    if (ctx->jarosz_bytes < need) {
-      if (ctx->jarosz_scratch) CK(cudaFree(ctx->jarosz_scratch), "cudaFree(jarosz scratch)");
-      ctx->jarosz_scratch = nullptr;
-      ctx->jarosz_bytes = 0;
-      CK(cudaMalloc(&ctx->jarosz_scratch, need), "cudaMalloc(jarosz scratch)");
-      ctx->jarosz_bytes = need;
-    }
+    const int64_t chunk = jarosz_chunk(n);
+    if ((st = ensure_jarosz_scratch(ctx, chunk))) return st;
     CK(cudaStreamWaitEvent(s, ctx->jarosz_done, 0), "wait jarosz scratch");
     CK(launch_hash_jarosz(p, ctx->jarosz_scratch, chunk, s), "jarosz launch");
     CK(cudaEventRecord(ctx->jarosz_done, s), "record jarosz scratch");
@@ -403,9 +416,17 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
   }
   uint32_t rm, cm;
   semantics_masks(semantics, &rm, &cm);
+  const bool jarosz = dct_precision == YPDQ_COMPRESS_JAROSZ;
   int dct = 0, sep = 0;
-  if (!parse_precision(dct_precision, &dct, &sep))
+  if (!jarosz && !parse_precision(dct_precision, &dct, &sep))
     return fail(YPDQ_ERR_INVALID, "dct_precision %d", dct_precision);
+  int64_t jchunk = 1;
+  if (jarosz && n > 0) {
+    for (int c = 0; c < nch; ++c)
+      jchunk = std::max<int64_t>(jchunk, jarosz_chunk(bounds[c + 1] - bounds[c]));
+    if ((st = ensure_jarosz_scratch(ctx, jchunk))) return st;
+    CK(cudaStreamWaitEvent(s, ctx->jarosz_done, 0), "wait jarosz scratch");
+  }
   for (int c = 0; c < nch && n > 0; ++c) {
     const int64_t i0 = bounds[c], i1 = bounds[c + 1];
     const uint8_t* src = static_cast<const uint8_t*>(h_images) + i0 * img_bytes;
@@ -426,8 +447,11 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
     hp.dev_err = ctx->d_err;
     hp.dct = dct;
     hp.separable = sep;
-    CK(launch_hash(hp, ctx->num_sms, ctx->hash_ctas[hp.input_kind][dct][sep], s),
-       "hash launch");
+    if (jarosz)
+      CK(launch_hash_jarosz(hp, ctx->jarosz_scratch, jchunk, s), "jarosz launch");
+    else
+      CK(launch_hash(hp, ctx->num_sms, ctx->hash_ctas[hp.input_kind][dct][sep], s),
+         "hash launch");
     ScanLaunch sp{};
     sp.rows = db->d_rows;
     sp.n_rows = db->n_rows;
@@ -442,6 +466,7 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
     sp.query_base = static_cast<uint32_t>(i0 * 8);
     CK(launch_scan(sp, YPDQ_SCAN_AUTO, ctx->num_sms, s), "scan launch");
   }
+  if (jarosz && n > 0) CK(cudaEventRecord(ctx->jarosz_done, s), "record jarosz scratch");
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, d_cnt, sizeof(uint64_t), cudaMemcpyDeviceToHost, s), "D2H count");
   CK(cudaStreamSynchronize(s), "screen sync");
@@ -707,8 +732,8 @@ __attribute__((visibility("default"))) bool yume_pdq_visit_dihedrals_smart_kerne
     if (check_ctx(ctx) != YPDQ_OK) return false;
     cudaStream_t s = ctx->stream;
     void *d_in, *d_out;
-    ypdq_status st;
-    if ((st = scratch(ctx, 5, 1024 + 16, &d_in)) || (st = scratch(ctx, 7, sizeof(res), &d_out))) {
+    if (scratch(ctx, 5, 1024 + 16, &d_in) != YPDQ_OK ||
+        scratch(ctx, 7, sizeof(res), &d_out) != YPDQ_OK) {
       fprintf(stderr, "yume_pdq_visit_dihedrals_smart_kernel: %s\n", ypdq_last_error());
       return false;
     }

@@ -183,10 +183,18 @@ __device__ __forceinline__ void st4(float* p, float a, float b, float c, float d
 //     the last group of tile t - 1 is completed by the first input of tile t.
 //   * Tile t - 1 (complete now) goes out with 16-byte stores; kCompact keeps the sampled
 //     columns only: output column sample_at(j) goes to Yc[row][j].
+// Images at or past *n_dev (graph replay with fewer images than the capture's bound; image
+// blockIdx.y of the chunk is image i0 + blockIdx.y of the call) are skipped.
+__device__ __forceinline__ bool past_count(const int64_t* n_dev, int64_t i0, unsigned img) {
+  return n_dev && i0 + static_cast<int64_t>(img) >= *n_dev;
+}
+
 template <int kKind, bool kCompact>
 __global__ void __launch_bounds__(128) rows_kernel(const uint8_t* __restrict__ in,
-                                                   float* __restrict__ out) {
+                                                   float* __restrict__ out,
+                                                   const int64_t* n_dev, int64_t i0) {
   using P = Px4<kKind>;
+  if (past_count(n_dev, i0, blockIdx.y)) return;
   __shared__ __align__(16) float tiles[4][2][32][kTileStride];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int lr = lane >> 3, lc = 4 * (lane & 7);
@@ -267,7 +275,9 @@ __global__ void __launch_bounds__(128) rows_kernel(const uint8_t* __restrict__ i
 // Box along columns of full planes: thread c of block b owns column 128 b + c of image
 // blockIdx.y, with the next 16 rows' loads in flight while it filters the current 16.
 __global__ void __launch_bounds__(128) cols_kernel(const float* __restrict__ Y,
-                                                   float* __restrict__ X) {
+                                                   float* __restrict__ X,
+                                                   const int64_t* n_dev, int64_t i0) {
+  if (past_count(n_dev, i0, blockIdx.y)) return;
   const int col = 128 * blockIdx.x + threadIdx.x;
   const float* src = Y + blockIdx.y * kPlane + col;
   float* dst = X + blockIdx.y * kPlane + col;
@@ -302,7 +312,9 @@ __global__ void __launch_bounds__(128) cols_kernel(const float* __restrict__ Y,
 // that every thread reaches the barrier.
 __global__ void __launch_bounds__(128) cols_dct_kernel(const float* __restrict__ Yc,
                                                        float* __restrict__ pdqf,
-                                                       float* __restrict__ buf1) {
+                                                       float* __restrict__ buf1,
+                                                       const int64_t* n_dev, int64_t i0) {
+  if (past_count(n_dev, i0, blockIdx.x)) return;  // the whole block: no barrier is split
   __shared__ float4 dk[127][4];  // dk[k][q] = D[4 q .. 4 q + 3][k]
   __shared__ float dj[16][129];  // D[i][k]
   __shared__ float t[16][129];   // T[i][j]
@@ -363,8 +375,9 @@ __global__ void __launch_bounds__(128) cols_dct_kernel(const float* __restrict__
 }
 
 template <int kKind>
-void launch_rows1(const uint8_t* in, float* Y, dim3 grid, cudaStream_t s) {
-  rows_kernel<kKind, false><<<grid, 128, 0, s>>>(in, Y);
+void launch_rows1(const uint8_t* in, float* Y, dim3 grid, const int64_t* n_dev, int64_t i0,
+                  cudaStream_t s) {
+  rows_kernel<kKind, false><<<grid, 128, 0, s>>>(in, Y, n_dev, i0);
 }
 
 }  // namespace
@@ -394,16 +407,18 @@ cudaError_t launch_hash_jarosz(const HashLaunch& p, void* scratch, int64_t chunk
     const uint8_t* in =
         static_cast<const uint8_t*>(p.images) + static_cast<size_t>(i0) * kPlane * kBytesPerPixel[p.input_kind];
     const dim3 grid(kN / 128, static_cast<unsigned>(m));
+    const int64_t* nd = p.n_dev;
     switch (p.input_kind) {
-      case YPDQ_INPUT_F32: launch_rows1<YPDQ_INPUT_F32>(in, Y, grid, s); break;
-      case YPDQ_INPUT_U8: launch_rows1<YPDQ_INPUT_U8>(in, Y, grid, s); break;
-      case YPDQ_INPUT_RGB8: launch_rows1<YPDQ_INPUT_RGB8>(in, Y, grid, s); break;
-      default: launch_rows1<YPDQ_INPUT_RGBA8>(in, Y, grid, s); break;
+      case YPDQ_INPUT_F32: launch_rows1<YPDQ_INPUT_F32>(in, Y, grid, nd, i0, s); break;
+      case YPDQ_INPUT_U8: launch_rows1<YPDQ_INPUT_U8>(in, Y, grid, nd, i0, s); break;
+      case YPDQ_INPUT_RGB8: launch_rows1<YPDQ_INPUT_RGB8>(in, Y, grid, nd, i0, s); break;
+      default: launch_rows1<YPDQ_INPUT_RGBA8>(in, Y, grid, nd, i0, s); break;
     }
-    cols_kernel<<<grid, 128, 0, s>>>(Y, X);
-    rows_kernel<YPDQ_INPUT_F32, true><<<grid, 128, 0, s>>>(reinterpret_cast<const uint8_t*>(X), Y);
+    cols_kernel<<<grid, 128, 0, s>>>(Y, X, nd, i0);
+    rows_kernel<YPDQ_INPUT_F32, true><<<grid, 128, 0, s>>>(reinterpret_cast<const uint8_t*>(X), Y,
+                                                           nd, i0);
     cols_dct_kernel<<<static_cast<unsigned>(m), 128, 0, s>>>(
-        Y, P, p.buf1 ? p.buf1 + static_cast<size_t>(i0) * 127 * 128 : nullptr);
+        Y, P, p.buf1 ? p.buf1 + static_cast<size_t>(i0) * 127 * 128 : nullptr, nd, i0);
     DihedralLaunch d{};
     d.pdqf = P;
     d.thr_in = nullptr;

@@ -75,6 +75,7 @@ struct Slot {
   uint8_t* d_hashes = nullptr;
   float* d_quality = nullptr;
   ypdq_hit* d_hits = nullptr;
+  void* d_jarosz = nullptr;  // YPDQ_COMPRESS_JAROSZ: the filter planes of a whole step
   StepHeader* d_hdr = nullptr;
   StepHeader* h_hdr = nullptr;  // pinned
   ypdq_hit* h_hits = nullptr;   // pinned, step_hit_capacity entries
@@ -142,7 +143,8 @@ ypdq_status capture_bucket(ypdq_server* S, Slot& sl, const Bucket& b, cudaGraphE
   hp.quality = sl.d_quality;
   hp.pdqf_slots = 1;
   hp.dev_err = &sl.d_hdr->err;
-  parse_precision(S->cfg.dct_precision, &hp.dct, &hp.separable);
+  const bool jarosz = S->cfg.dct_precision == YPDQ_COMPRESS_JAROSZ;
+  if (!jarosz) parse_precision(S->cfg.dct_precision, &hp.dct, &hp.separable);
   ScanLaunch sp{};
   sp.rows = S->db->d_rows;
   sp.n_rows = S->db->n_rows;
@@ -160,7 +162,8 @@ ypdq_status capture_bucket(ypdq_server* S, Slot& sl, const Bucket& b, cudaGraphE
   cudaError_t e = cudaMemcpyAsync(sl.d_hdr, sl.h_hdr, 16, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(&sl.d_hdr->count, 0, 16, s);
   if (e == cudaSuccess)
-    e = launch_hash(hp, S->ctx->num_sms, S->ctx->hash_ctas[kind][hp.dct][hp.separable], s);
+    e = jarosz ? launch_hash_jarosz(hp, sl.d_jarosz, nb, s)
+               : launch_hash(hp, S->ctx->num_sms, S->ctx->hash_ctas[kind][hp.dct][hp.separable], s);
   if (e == cudaSuccess) e = launch_scan(sp, b.algo, S->ctx->num_sms, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&sl.h_hdr->count, &sl.d_hdr->count, 16, cudaMemcpyDeviceToHost, s);
@@ -384,6 +387,7 @@ void release(ypdq_server* S) {
     cudaFree(sl.d_hashes);
     cudaFree(sl.d_quality);
     cudaFree(sl.d_hits);
+    cudaFree(sl.d_jarosz);
     cudaFree(sl.d_hdr);
     cudaFreeHost(sl.h_hdr);
     cudaFreeHost(sl.h_hits);
@@ -401,6 +405,8 @@ ypdq_status alloc_slot(ypdq_server* S, Slot& sl) {
   CK(cudaMalloc(&sl.d_hashes, size_t(B) * 256), "cudaMalloc(slot hashes)");
   CK(cudaMalloc(&sl.d_quality, size_t(B) * 32), "cudaMalloc(slot quality)");
   CK(cudaMalloc(&sl.d_hits, S->cfg.step_hit_capacity * sizeof(ypdq_hit)), "cudaMalloc(slot hits)");
+  if (S->cfg.dct_precision == YPDQ_COMPRESS_JAROSZ)
+    CK(cudaMalloc(&sl.d_jarosz, jarosz_scratch_bytes(B)), "cudaMalloc(slot jarosz planes)");
   CK(cudaMalloc(&sl.d_hdr, sizeof(StepHeader)), "cudaMalloc(slot header)");
   CK(cudaMallocHost(&sl.h_hdr, sizeof(StepHeader)), "cudaMallocHost(slot header)");
   CK(cudaMallocHost(&sl.h_hits, S->cfg.step_hit_capacity * sizeof(ypdq_hit)), "cudaMallocHost(slot hits)");
@@ -504,7 +510,8 @@ ypdq_status ypdq_server_create(ypdq_ctx* ctx, ypdq_db* db, const ypdq_server_con
   if (image_bytes_of(cfg.input_kind) == 0)
     return fail(YPDQ_ERR_INVALID, "input_kind %d", cfg.input_kind);
   int dct_v = 0, sep_v = 0;
-  if (!parse_precision(cfg.dct_precision, &dct_v, &sep_v))
+  if (cfg.dct_precision != YPDQ_COMPRESS_JAROSZ &&
+      !parse_precision(cfg.dct_precision, &dct_v, &sep_v))
     return fail(YPDQ_ERR_INVALID, "dct_precision %d", cfg.dct_precision);
   if (cfg.semantics < YPDQ_DIHEDRAL_EXACT || cfg.semantics > YPDQ_DIHEDRAL_SCALAR)
     return fail(YPDQ_ERR_INVALID, "semantics %d", cfg.semantics);
@@ -541,8 +548,10 @@ ypdq_status ypdq_server_create(ypdq_ctx* ctx, ypdq_db* db, const ypdq_server_con
     return cuda_fail(e, "cudaMemGetInfo");
   }
   const uint64_t budget = cfg.device_bytes ? cfg.device_bytes : free_b / 2;
-  const uint64_t slot_bytes = uint64_t(cfg.max_step_images) * (S->image_bytes + 256 + 32) +
-                              cfg.step_hit_capacity * sizeof(ypdq_hit) + sizeof(StepHeader);
+  const uint64_t slot_bytes =
+      uint64_t(cfg.max_step_images) * (S->image_bytes + 256 + 32) +
+      cfg.step_hit_capacity * sizeof(ypdq_hit) + sizeof(StepHeader) +
+      (cfg.dct_precision == YPDQ_COMPRESS_JAROSZ ? jarosz_scratch_bytes(cfg.max_step_images) : 0);
   const uint64_t fit = budget / slot_bytes;
   const uint32_t n_slots = static_cast<uint32_t>(std::min<uint64_t>(fit, cfg.slots));
   if (n_slots == 0) {
