@@ -52,6 +52,17 @@ def test_rgb8_stream_bin(yp, oracle):
     assert out == expected(pipe, h, q, "bin", 1)
 
 
+def test_reference_kernel_stream(yp, oracle):
+    """--reference-kernel: ReferenceKernel<f32> hashes (oracle restatement of ref.rs), scalar
+    dihedral semantics as that kernel's trait defaults."""
+    pipe = load_pipe()
+    frames = yp.synth.to_u8(yp.synth.blob_images(3, seed=503))
+    out = run(["-f", "hex+lf", "--dihedrals", "--semantics", "scalar", "--reference-kernel"],
+              frames.tobytes())
+    h, q, t, p, b = oracle.hash_batch_reference(frames, semantics="scalar")
+    assert out == expected(pipe, h, q, "hex+lf", 8)
+
+
 def test_partial_frame_is_an_error(yp):
     r = subprocess.run([sys.executable, PIPE, "-f", "hex"], input=b"\0" * 1000,
                        capture_output=True, cwd=ROOT, timeout=600)

@@ -17,6 +17,8 @@ reference's formats (src/main.rs:683-773):
 With --db the frames go through the continuous-batching server (ypdq_server_*), which also
 matches all 8 hashes of each frame against the database; after a frame's hashes one line
 per hit follows in text formats: "match <slot> <row index> <distance>" (not in the reference).
+--reference-kernel hashes with ReferenceKernel<f32> (not in the reference's CLI, which always
+uses its default kernel).
 """
 import argparse
 import os
@@ -104,6 +106,9 @@ def main(argv=None):
     ap.add_argument("--dihedrals", action="store_true", help="output all 8 hashes per frame")
     ap.add_argument("--semantics", default="exact", choices=["exact", "avx2", "scalar"],
                     help="dihedral sign convention (the reference's kernels differ)")
+    ap.add_argument("--reference-kernel", action="store_true",
+                    help="hash with ReferenceKernel<f32> (full Jarosz filter, "
+                         "YPDQ_COMPRESS_JAROSZ) instead of the default kernel (an extension)")
     ap.add_argument("--batch", type=int, default=256, help="frames per GPU launch")
     ap.add_argument("--db", help="database file of 32-byte rows: screen every frame")
     ap.add_argument("--threshold", type=int, default=31)
@@ -119,6 +124,7 @@ def main(argv=None):
     fout = sys.stdout.buffer if a.output == "-" else open(a.output, "wb")
     slots = 8 if a.dihedrals else 1
     text = kind != "raw"
+    dct = 0x200 if a.reference_kernel else 0  # YPDQ_COMPRESS_JAROSZ or the FP32 default
 
     def emit(hashes, quality, hits_per_frame):
         for f in range(hashes.shape[0]):
@@ -133,14 +139,14 @@ def main(argv=None):
             frames = read_frames(fin, bpp, a.batch)
             if frames is None:
                 break
-            out = yp.hash_batch(ctx, frames, semantics=a.semantics)
+            out = yp.hash_batch(ctx, frames, semantics=a.semantics, dct=dct)
             emit(out["hashes"], out["quality"], None)
             fout.flush()
     else:
         db = yp.Database.from_file(ctx, a.db)
         in_kind = {1: "u8", 3: "rgb8", 4: "rgba8"}[bpp]
         batch = 1 << max(0, (a.batch - 1).bit_length())
-        with yp.Server(ctx, db, threshold=a.threshold, input_kind=in_kind,
+        with yp.Server(ctx, db, threshold=a.threshold, input_kind=in_kind, dct=dct,
                        semantics=a.semantics, max_step_images=batch) as srv:
             pending, done = [], {}
 
