@@ -60,6 +60,9 @@ def lib():
             "ypdqo_luma": (None, [P, i64, i32, P]),
             "ypdqo_jarosz_compress": (None, [P, P]),
             "ypdqo_dct2d_reference": (None, [P, P]),
+            "ypdqo_hash_batch_avx2": (None, [P, i64, i32, P, P, P, P, i32]),
+            "ypdqo_dct2d_matrix": (None, [P, P, P]),
+            "ypdqo_dct2d_avx2_matrix": (None, [P, P, P]),
             "ypdqo_hash_batch_reference": (None, [P, i64, i32, ctypes.c_uint32, ctypes.c_uint32,
                                                   P, P, P, P, P, i32]),
             "ypdqo_synth_clustered": (None, [P, i64, ctypes.c_uint64, ctypes.c_uint64,
@@ -261,3 +264,40 @@ def hash_batch_reference(imgs, semantics="scalar", nthreads=None):
     lib().ypdqo_hash_batch_reference(_p(imgs), n, int(is_u8), rm, cm, _p(h), _p(q), _p(t), _p(p),
                                      _p(b), nthreads or os.cpu_count() or 1)
     return h, q, t, p, b
+
+
+def hash_batch_avx2(imgs, nthreads=None):
+    """yume-pdq's Avx2F32Kernel (FMA compress and DCT, residual-mean quantizer, its own
+    dihedral sign patterns) over n images (f32 or u8 [n, 512, 512]); returns hashes
+    [n,8,32], quality [n,8], thresholds [n,8], pdqf [n,16,16]."""
+    imgs = np.ascontiguousarray(imgs)
+    is_u8 = imgs.dtype == np.uint8
+    if not is_u8:
+        imgs = imgs.astype(np.float32, copy=False)
+    n = imgs.shape[0]
+    h = np.zeros((n, 8, 32), np.uint8)
+    q = np.zeros((n, 8), np.float32)
+    t = np.zeros((n, 8), np.float32)
+    p = np.zeros((n, 16, 16), np.float32)
+    lib().ypdqo_hash_batch_avx2(_p(imgs), n, int(is_u8), _p(h), _p(q), _p(t), _p(p),
+                                nthreads or os.cpu_count() or 1)
+    return h, q, t, p
+
+
+def dct2d_matrix(D, buf127):
+    """The DefaultKernel DCT (four partial sums) of a 127x127 buffer with a given 16x127
+    matrix."""
+    D = np.ascontiguousarray(D, np.float32)
+    b = np.ascontiguousarray(buf127, np.float32)
+    out = np.zeros((16, 16), np.float32)
+    lib().ypdqo_dct2d_matrix(_p(D), _p(b), _p(out))
+    return out
+
+
+def dct2d_avx2_matrix(D, buf128):
+    """The Avx2F32Kernel DCT of a 128x128 zero-padded buffer with a given 16x127 matrix."""
+    D = np.ascontiguousarray(D, np.float32)
+    b = np.ascontiguousarray(buf128, np.float32)
+    out = np.zeros((16, 16), np.float32)
+    lib().ypdqo_dct2d_avx2_matrix(_p(D), _p(b), _p(out))
+    return out

@@ -19,11 +19,16 @@
  *                         src/kernel/x86.rs:989-1079 (AVX-512)
  *   - dct2d f64 twin    : ReferenceKernel<f64>::dct2d     src/kernel/mod.rs:838-864
  *   - scalar matcher    : CpuMatcher::find (u64 scalar)   src/matching/mod.rs:336-362
+ *   - Avx2F32Kernel     : jarosz_compress_avx2 src/kernel/x86.rs:626-682, dct2d_impl
+ *                         :100-281, quantize_impl :440-621, sign patterns :285-436;
+ *                         restated lane by lane with fmaf for every fused multiply-add
  *
  * The f32 arithmetic keeps the reference's operation order: a multiply and then an
- * add, each rounded, with no fused multiply-add, because Rust does not contract a*b+c.
+ * add, each rounded, with no fused multiply-add, because Rust does not contract a*b+c
+ * (the Avx2F32Kernel restatement calls fmaf exactly where that kernel fuses).
  * Build this file with -ffp-contract=off.
  */
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
@@ -87,9 +92,9 @@ YPDQO_EXPORT void ypdqo_compress(const float* img, float* out /* 127*127 */) {
   }
 }
 
-/* 127x127 -> 16x16 with four interleaved partial sums, as dct2d_impl does. */
-YPDQO_EXPORT void ypdqo_dct2d(const float* buf /* 127*127 */, float* pdqf /* 256 */) {
-  init_constants();
+/* 127x127 -> 16x16 with four interleaved partial sums, as dct2d_impl does, for a given
+ * 16 x 127 matrix D (the reference's tests also run it on test matrices). */
+static void dct2d_with(const float* DCT32, const float* buf, float* pdqf) {
   float tmp[127];
   for (int k = 0; k < 16; k++) {
     for (int j = 0; j < 127; j++) {
@@ -109,6 +114,15 @@ YPDQO_EXPORT void ypdqo_dct2d(const float* buf /* 127*127 */, float* pdqf /* 256
       pdqf[k * 16 + j] = ((s[0] + s[1]) + s[2]) + s[3];
     }
   }
+}
+
+YPDQO_EXPORT void ypdqo_dct2d(const float* buf /* 127*127 */, float* pdqf /* 256 */) {
+  init_constants();
+  dct2d_with(DCT32, buf, pdqf);
+}
+YPDQO_EXPORT void ypdqo_dct2d_matrix(const float* D /* 16*127 */, const float* buf /* 127*127 */,
+                                     float* pdqf /* 256 */) {
+  dct2d_with(D, buf, pdqf);
 }
 
 /* FP64 DCT (straight sums) on the f32 compress output, for coefficient-error reports. */
@@ -247,10 +261,11 @@ static void transpose16(float* p) {
     }
 }
 
-YPDQO_EXPORT void ypdqo_dihedrals(const float* pdqf_in, float threshold, uint32_t row_mask,
-                                  uint32_t col_mask, uint8_t* out_hashes /* 7*32 */,
-                                  float* out_thr /* 7 */, float* out_quality /* 7 */,
-                                  float* out_pdqf /* 7*256 or NULL */) {
+typedef void (*quantize_fn)(const float* p, float* thr, uint8_t* out);
+
+static void dihedrals_with(const float* pdqf_in, float threshold, uint32_t row_mask,
+                           uint32_t col_mask, uint8_t* out_hashes, float* out_thr,
+                           float* out_quality, float* out_pdqf, quantize_fn ypdqo_quantize) {
   float p[256];
   memcpy(p, pdqf_in, sizeof(p));
   float t_cols = threshold, t_rows = threshold, t_diag = threshold;
@@ -285,6 +300,14 @@ YPDQO_EXPORT void ypdqo_dihedrals(const float* pdqf_in, float threshold, uint32_
   ypdqo_threshold_2d(p, out_hashes + v * 32, t_rows);
   EMIT(t_rows); /* ROTATED_90 */
 #undef EMIT
+}
+
+YPDQO_EXPORT void ypdqo_dihedrals(const float* pdqf_in, float threshold, uint32_t row_mask,
+                                  uint32_t col_mask, uint8_t* out_hashes /* 7*32 */,
+                                  float* out_thr /* 7 */, float* out_quality /* 7 */,
+                                  float* out_pdqf /* 7*256 or NULL */) {
+  dihedrals_with(pdqf_in, threshold, row_mask, col_mask, out_hashes, out_thr, out_quality,
+                 out_pdqf, ypdqo_quantize);
 }
 
 /* ------------------------------------------------------------------ threads */
@@ -756,4 +779,198 @@ YPDQO_EXPORT void ypdqo_hash_batch_reference(const void* imgs, int64_t n, int is
   init_constants();
   ref_batch_ctx c = {imgs, is_u8, row_mask, col_mask, hashes, quality, thresholds, pdqf, buf127};
   parallel_ranges(ref_batch_range, &c, n, nthreads);
+}
+
+/* ----------------------------------------------- Avx2F32Kernel (x86.rs), restated */
+
+/* The sum of the 8 lanes as the kernel's permute-and-add reduction forms it:
+ * ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7)). */
+static float hsum8(const float* a) {
+  return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+}
+
+/* jarosz_compress_avx2 (src/kernel/x86.rs:626-682): per output, 8 lanes l accumulate
+ * fma(img[in_i + di][in_j + l], W8[di][l], .) over di (W8 = the 7 tent weights of a row
+ * and a 0), reduced by two hadds as ((l0 + l1) + (l2 + l3)) + ((l4 + l5) + (l6 + l7)).
+ * Lane 7 reads the next pixel in memory (weight 0); for the last output of the last row
+ * it reads in_j + 6 again (the kernel's rewind-and-permute), staying inside the image.
+ * out is 128 x 128 with a zero last row and column, as the kernel's buffer. */
+static void avx2_compress(const float* img, float* out) {
+  memset(out, 0, 128 * 128 * sizeof(float));
+  for (int oi = 0; oi < 127; oi++) {
+    const int in_i = YPDQO_CONV_OFFSET[oi] - YPDQO_TENT_OFFSET;
+    for (int oj = 0; oj < 127; oj++) {
+      const int in_j = YPDQO_CONV_OFFSET[oj] - YPDQO_TENT_OFFSET;
+      float lane[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (int di = 0; di < 7; di++) {
+        const int64_t row = (int64_t)(in_i + di) * 512 + in_j;
+        for (int l = 0; l < 8; l++) {
+          int64_t idx = row + l;
+          if (l == 7 && di == 6 && oi == 126 && oj == 126) idx = row + 6;
+          const float w = l < 7 ? TENT[di * 7 + l] : 0.0f;
+          lane[l] = fmaf(img[idx], w, lane[l]);
+        }
+      }
+      /* _mm256_hadd_ps twice with zero, then element 0 + element 4 */
+      const float h0 = (lane[0] + lane[1]) + (lane[2] + lane[3]);
+      const float h4 = (lane[4] + lane[5]) + (lane[6] + lane[7]);
+      out[oi * 128 + oj] = h0 + h4;
+    }
+  }
+}
+
+/* A 16 x 127 DCT matrix as the kernel reads it: row-major followed by zero padding, so
+ * element (k, 127) is element (k + 1, 0), and (15, 127) is 0. */
+static float dct_padded(const float* D, int k, int c) {
+  const int idx = k * 127 + c;
+  return idx < 16 * 127 ? D[idx] : 0.0f;
+}
+
+/* Avx2F32Kernel::dct2d_impl (src/kernel/x86.rs:100-281). Stage 1: for each frequency k and
+ * column j, two accumulators take the products of rows k2 = 0..127 (the padding row
+ * included) by fma in the pattern 1, 0, 0, 1, 1, 0, 0, 1 per 8 rows; a NaN sum becomes 0;
+ * tmp[j] = sum0 + sum1. Stage 2: per output j, two 8-lane accumulators take 8-column
+ * blocks in the pattern 1, 0, 0, 1; their lane sums are added and reduced by hsum8. */
+static void avx2_dct2d(const float* D, const float* buf /* 128*128 */, float* pdqf /* 256 */) {
+  static const int pat8[8] = {1, 0, 0, 1, 1, 0, 0, 1};
+  float tmp[128];
+  for (int k = 0; k < 16; k++) {
+    for (int j = 0; j < 128; j++) {
+      float acc[2] = {0.0f, 0.0f};
+      for (int k2 = 0; k2 < 128; k2++)
+        acc[pat8[k2 & 7]] = fmaf(buf[k2 * 128 + j], dct_padded(D, k, k2), acc[pat8[k2 & 7]]);
+      const float s0 = isnan(acc[0]) ? 0.0f : acc[0];
+      const float s1 = isnan(acc[1]) ? 0.0f : acc[1];
+      tmp[j] = s0 + s1;
+    }
+    for (int j = 0; j < 16; j++) {
+      float acc[2][8];
+      memset(acc, 0, sizeof(acc));
+      for (int blk = 0; blk < 16; blk++) {
+        const int t = pat8[blk & 3];
+        for (int l = 0; l < 8; l++)
+          acc[t][l] = fmaf(tmp[blk * 8 + l], dct_padded(D, j, blk * 8 + l), acc[t][l]);
+      }
+      float sum[8];
+      for (int l = 0; l < 8; l++) sum[l] = acc[0][l] + acc[1][l];
+      pdqf[k * 16 + j] = hsum8(sum);
+    }
+  }
+}
+
+/* Avx2F32Kernel::quantize_impl (src/kernel/x86.rs:440-621): a search for the threshold by
+ * the mean of the residual elements beyond the guess, at most 32 rounds. Each round writes
+ * the bits x > guess (byte 31 - c for elements 8c .. 8c + 7); 8-lane residual sums are
+ * reduced by hsum8 and divided by their counts. */
+/* _mm256_min_ps / _mm256_max_ps per lane: the first operand if it compares less /
+ * greater, else the second (so ties and NaNs take the second). */
+static float vmin(float a, float b) { return a < b ? a : b; }
+static float vmax(float a, float b) { return a > b ? a : b; }
+/* The kernel's horizontal min / max: op(a[i], a[i+1]), then op(.[i], .[i+2]), then
+ * op(.[0], .[4]), indices mod 8 (permutevar8x32 rotations). */
+static float htree(const float* a, float (*op)(float, float)) {
+  float pw[8], e4[8];
+  for (int i = 0; i < 8; i++) pw[i] = op(a[i], a[(i + 1) & 7]);
+  for (int i = 0; i < 8; i++) e4[i] = op(pw[i], pw[(i + 2) & 7]);
+  return op(e4[0], e4[4]);
+}
+
+static void avx2_quantize(const float* p, float* thr, uint8_t* out) {
+  float lmin[8], lmax[8];
+  for (int l = 0; l < 8; l++) {
+    lmin[l] = FLT_MAX;
+    lmax[l] = -FLT_MAX;
+  }
+  for (int c = 0; c < 32; c++)
+    for (int l = 0; l < 8; l++) {
+      const float x = p[8 * c + l];
+      lmin[l] = vmin(lmin[l], x);
+      lmax[l] = vmax(lmax[l], x);
+    }
+  float mx = htree(lmax, vmax), mn = htree(lmin, vmin);
+  const uint32_t half = 128;
+  float guess = (mn + mx) * 0.5f;
+  uint32_t num_over = 0, num_under = 0;
+  for (int iter = 0; iter < 32; iter++) {
+    float rgt[8] = {0, 0, 0, 0, 0, 0, 0, 0}, rlt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t gt_count = 0, lt_count = 0;
+    for (int c = 0; c < 32; c++) {
+      uint8_t bits = 0;
+      for (int l = 0; l < 8; l++) {
+        const float x = p[8 * c + l];
+        const int gt = x > guess, lt = x < guess;
+        if (gt) bits |= (uint8_t)(1u << l);
+        const int mgt = gt && x <= mx, mlt = lt && x >= mn;
+        gt_count += (uint32_t)mgt;
+        lt_count += (uint32_t)mlt;
+        rgt[l] = rgt[l] + (mgt ? x : 0.0f);  /* and_ps(mask, x): x or +0 */
+        rlt[l] = rlt[l] + (mlt ? x : 0.0f);
+      }
+      out[31 - c] = bits;
+    }
+    if (gt_count + num_over > half) {
+      num_under += lt_count;
+      mn = guess;
+      guess = hsum8(rgt) / (float)gt_count;
+    } else if (lt_count + num_under > half) {
+      num_over += gt_count;
+      mx = guess;
+      guess = hsum8(rlt) / (float)lt_count;
+    } else {
+      break;
+    }
+  }
+  *thr = guess;
+}
+
+/* u8 -> f32 is exact in both kernels; quality is the trait's sum of gradients over the
+ * kernel's PDQF (same loop order) and the same adjustment. */
+typedef struct {
+  const void* imgs;
+  int is_u8;
+  uint8_t* hashes;
+  float *quality, *thresholds, *pdqf;
+} avx2_batch_ctx;
+
+static void avx2_batch_range(void* vctx, int64_t b, int64_t e) {
+  avx2_batch_ctx* c = (avx2_batch_ctx*)vctx;
+  float* img = (float*)malloc(512 * 512 * sizeof(float));
+  float* bb = (float*)malloc(128 * 128 * sizeof(float));
+  for (int64_t n = b; n < e; n++) {
+    if (c->is_u8) {
+      const uint8_t* u = (const uint8_t*)c->imgs + n * 512 * 512;
+      for (int i = 0; i < 512 * 512; i++) img[i] = (float)u[i];
+    } else {
+      memcpy(img, (const float*)c->imgs + n * 512 * 512, 512 * 512 * sizeof(float));
+    }
+    float p[256], t;
+    avx2_compress(img, bb);
+    avx2_dct2d(DCT32, bb, p);
+    c->quality[n * 8] = ypdqo_adjust_quality(ypdqo_sum_of_gradients(p));
+    avx2_quantize(p, &t, c->hashes + n * 256);
+    c->thresholds[n * 8] = t;
+    if (c->pdqf) memcpy(c->pdqf + n * 256, p, sizeof(p));
+    /* Avx2F32Kernel sign patterns: rows 0, 2, .., 14; columns 0, 2, 4, 6 */
+    dihedrals_with(p, t, 0x5555u, 0x0055u, c->hashes + n * 256 + 32, c->thresholds + n * 8 + 1,
+                   c->quality + n * 8 + 1, NULL, avx2_quantize);
+  }
+  free(bb);
+  free(img);
+}
+
+/* yume-pdq's Avx2F32Kernel (smart_kernel on AVX2 + FMA hosts) over n images, with its
+ * dihedrals: hashes n x 8 x 32, quality and thresholds n x 8, pdqf n x 256 (or NULL). */
+YPDQO_EXPORT void ypdqo_hash_batch_avx2(const void* imgs, int64_t n, int is_u8, uint8_t* hashes,
+                                        float* quality, float* thresholds, float* pdqf,
+                                        int nthreads) {
+  init_constants();
+  avx2_batch_ctx c = {imgs, is_u8, hashes, quality, thresholds, pdqf};
+  parallel_ranges(avx2_batch_range, &c, n, nthreads);
+}
+
+/* The Avx2F32Kernel DCT alone on a 128 x 128 zero-padded buffer and a given matrix (the
+ * reference's AVX2-equivalence test, src/kernel/mod.rs:1249-1345). */
+YPDQO_EXPORT void ypdqo_dct2d_avx2_matrix(const float* D /* 16*127 */,
+                                          const float* buf /* 128*128 */, float* pdqf /* 256 */) {
+  avx2_dct2d(D, buf, pdqf);
 }

@@ -286,3 +286,23 @@ def test_reference_kernel_color(ctx, yp, oracle, channels):
     h, q, t, p, b = oracle.hash_batch_reference(oracle.luma(rgb), semantics="scalar")
     assert np.array_equal(got["hashes"], h) and np.array_equal(got["quality"], q)
     assert np.array_equal(got["pdqf"][:, 0].view(np.uint32), p.view(np.uint32))
+
+
+def test_disagreement_vs_avx2_kernel(ctx, yp, oracle):
+    """Hash-bit disagreement of the bit-exact FP32 kernel (with the AVX2 sign patterns) with
+    the restated Avx2F32Kernel, yume-pdq's smart_kernel on AVX2 hosts, over 512 mixed images
+    (constant images excluded: their coefficients are rounding noise in every kernel).
+    Measured: primary hashes 0 %, all 8 slots ~0.03 % (the transposed slots, through the
+    quantizer's threshold value)."""
+    imgs, kind = yp.synth.mixed_images(512, seed=2036)
+    live = kind != 2
+    got = yp.hash_batch(ctx, imgs, semantics="avx2")
+    ha, qa, ta, pa = oracle.hash_batch_avx2(imgs)
+    d0 = float(np.unpackbits(got["hashes"][live, 0] ^ ha[live, 0]).mean())
+    dall = float(np.unpackbits(got["hashes"][live] ^ ha[live]).mean())
+    print("disagreement vs Avx2F32Kernel: primary %.5f %%, all slots %.5f %%"
+          % (100 * d0, 100 * dall))
+    assert d0 <= 0.001 and dall <= 0.005
+    # qualities are gradients of slightly different PDQFs (FMA rounding): equal to ~1e-7
+    assert np.abs(got["quality"][live, 0] - qa[live, 0]).max() <= 1e-5
+

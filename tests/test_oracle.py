@@ -28,6 +28,50 @@ def test_readme_fm_sine_kat(oracle):
     assert q == 1.0
 
 
+def test_avx2_kernel_readme_kat(oracle):
+    """The Avx2F32Kernel restatement (FMA compress and DCT, residual-mean quantizer) against
+    the README known-answer vector (README.md:305-451)."""
+    kat = json.load(open(os.path.join(GOLDEN, "readme_fm_sine.json")))
+    img = oracle.fm_sine_image()
+    h, q, t, p = oracle.hash_batch_avx2(img[None])
+    expected = np.frombuffer(bytes.fromhex(kat["expected_hash_hex"]), np.uint8)
+    assert bits_diff(h[0, 0], expected) <= kat["max_bits_different"]
+    printed = np.array(kat["pdqf_printed_1dp"], np.float64)
+    assert np.all(np.abs(p[0].astype(np.float64) - printed) <= 0.0500001)
+    assert q[0, 0] == 1.0
+
+
+def test_avx2_dct_equivalence(oracle):
+    """test_dct64_impl_avx2_equivalence (src/kernel/mod.rs:1249-1345) restated on the two
+    DCT restatements: a matrix of ones and a ramp buffer (relative difference < 4e-7), then
+    a constant buffer and a ramp matrix (< 8e-7)."""
+    i, j = np.meshgrid(np.arange(127), np.arange(127), indexing="ij")
+    cases = [
+        (np.ones(16 * 127, np.float32),
+         (i * 127 + j).astype(np.float32) * np.float32(0.00001), 4e-7),
+        (np.arange(16 * 127).astype(np.float32),
+         np.full((127, 127), np.float32(0.00001), np.float32), 8e-7),
+    ]
+    for D, b127, tol in cases:
+        b128 = np.zeros((128, 128), np.float32)
+        b128[:127, :127] = b127
+        ref = oracle.dct2d_matrix(D, b127)
+        got = oracle.dct2d_avx2_matrix(D, b128)
+        assert np.all(np.abs(ref - got) / ref < tol)
+
+
+def test_avx2_kernel_agrees_with_default(oracle, yp):
+    """Seeded blob images: the Avx2F32Kernel and DefaultKernel restatements give the same
+    primary hashes up to rare FMA-rounding flips; with the same sign patterns the derived
+    slots differ only where the residual-mean quantizer's threshold value (which the
+    transposed slots reuse) departs from the median."""
+    imgs = yp.synth.blob_images(24, seed=77)
+    ha, qa, ta, pa = oracle.hash_batch_avx2(imgs)
+    hd = oracle.hash_batch(imgs, semantics="avx2")[0]
+    assert np.unpackbits(ha[:, 0] ^ hd[:, 0]).mean() <= 0.002
+    assert np.unpackbits(ha ^ hd).mean() <= 0.01
+
+
 def test_constants_pinned(oracle, yp):
     """The oracle's 128-bit tables equal the tables compiled into the library."""
     import ctypes
