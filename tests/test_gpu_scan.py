@@ -172,6 +172,23 @@ def test_screen_host_reference_kernel(ctx, yp, oracle):
     db.close()
 
 
+@pytest.mark.parametrize("algo", [1, 3])
+def test_row_sharded_scan(ctx, yp, oracle, algo):
+    """A database row-sharded in 3 device slices (shard_rows), each scanned with the whole
+    query batch, merged with its row offset (merge_shard_hits): the hits of one scan of the
+    whole database. The shards run one after another on this GPU."""
+    rows = yp.synth.rows_128(50021, seed=71)
+    q = yp.synth.rows_128(96, seed=72)
+    yp.synth.plant(rows, q, 600, 0, 40, seed=73)
+    parts = []
+    for rank in range(3):
+        lo, hi = yp.shard_rows(rows.shape[0], 3, rank)
+        parts.append((yp.scan(ctx, rows[lo:hi], q, 31, algo=algo), lo))
+    merged = yp.merge_shard_hits(parts)
+    want = oracle.find_all(rows, q, 31)
+    assert len(want) > 0 and np.array_equal(as_tuples(merged), as_tuples(want))
+
+
 def test_synth_rows_match_cpu_twin(ctx, yp, oracle):
     n = 20000
     d = ctx.alloc(n * 32)

@@ -1,6 +1,10 @@
-"""bench.py's multi-GPU mode runs one replica per rank (the path needs no collective): the
-job time is the slowest rank's and the value counts every rank's images. Checked here with
-two gloo ranks on the CPU."""
+"""Multi-GPU paths, checked with gloo ranks on the CPU.
+
+bench.py's multi-GPU mode runs one replica per rank (the path needs no collective): the job
+time is the slowest rank's and the value counts every rank's images. A database can also be
+row-sharded (shard_rows / merge_shard_hits): each rank scans its slice with the whole query
+batch and rank 0 gathers the hit lists with their row offsets; the merged list must be the
+scan of the whole database."""
 import os
 import socket
 
@@ -45,3 +49,44 @@ def test_replica_aggregation_two_gloo_ranks():
         assert (rank, world, local) == (r, 2, r)
         assert t == 7.0  # the slowest replica
         assert abs(v - 2 * 1000 / 0.007) < 1e-6
+
+
+def _shard_rank(rank, world, port, out):
+    import sys
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import __graft_entry__ as g
+    import oracle
+    yp = g.load_package()
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    rows = yp.synth.rows_128(30011, seed=61)  # every rank builds the same database
+    q = yp.synth.rows_128(24, seed=62)
+    yp.synth.plant(rows, q, 300, 0, 40, seed=63)
+    lo, hi = yp.shard_rows(rows.shape[0], world, rank)
+    # this rank's scan of its slice (the oracle's matcher stands in for the GPU scan)
+    local = oracle.find_all(rows[lo:hi], q, 31)
+    gathered = [None] * world
+    dist.all_gather_object(gathered, (local, lo))
+    if rank == 0:
+        merged = yp.merge_shard_hits(gathered)
+        full = oracle.find_all(rows, q, 31)
+        out.put(bool(len(full) > 0 and np.array_equal(merged, full)))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_row_sharded_scan_three_gloo_ranks():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_shard_rank, args=(r, 3, port, q)) for r in range(3)]
+    for p in procs:
+        p.start()
+    ok = q.get(timeout=180)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert ok
+

@@ -11,7 +11,8 @@ The directory name contains a hyphen, so import it through `load_package()` in
 """
 from . import _lib, build, core, kernel, matching, serving, synth  # noqa: F401
 from ._lib import HIT_DTYPE, YpdqError  # noqa: F401
-from .core import Context, Database, DeviceBuffer, hash_batch, scan, screen_host  # noqa: F401
+from .core import (Context, Database, DeviceBuffer, hash_batch, merge_shard_hits,  # noqa: F401
+                   scan, screen_host, shard_rows)
 from .kernel import (CudaKernel, Dihedrals, SLOT_DIHEDRALS, hash, hash_float,  # noqa: F401
                      hash_get_threshold, visit_dihedrals)
 from .matching import CudaMatcher, CudaVectorDatabase  # noqa: F401

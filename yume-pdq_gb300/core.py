@@ -282,6 +282,28 @@ class Database:
             pass
 
 
+def shard_rows(n_rows, world, rank):
+    """Row range [lo, hi) of shard `rank` when a database of n_rows is split over `world`
+    GPUs in contiguous slices (sizes differ by at most one row). Each GPU scans its slice
+    with the whole query batch; no collective is needed."""
+    if not 0 <= rank < world:
+        raise ValueError("rank %d of world %d" % (rank, world))
+    return n_rows * rank // world, n_rows * (rank + 1) // world
+
+
+def merge_shard_hits(parts):
+    """One hit list from per-shard lists: `parts` holds (hits, row_offset) pairs, hits with
+    shard-local indices; the result has global indices in the scalar matcher's
+    (index, query) order, the list a single scan of the whole database returns."""
+    arrs = []
+    for hits, offset in parts:
+        h = np.array(hits, dtype=HIT_DTYPE, copy=True)
+        h["index"] += np.uint64(offset)
+        arrs.append(h)
+    out = np.concatenate(arrs) if arrs else np.zeros(0, HIT_DTYPE)
+    return out[np.lexsort((out["query"], out["index"]))]
+
+
 def screen_host(ctx, db, images, threshold=31, semantics="exact", dct=_lib.DCT_FP32,
                 capacity=1 << 16, want_hashes=False):
     """ypdq_screen_host: hash + 8 dihedrals + scan, from host images to sorted host hits."""
