@@ -154,6 +154,34 @@ def test_screen_host_end_to_end(ctx, yp, oracle):
     assert np.array_equal(as_tuples(hits2), as_tuples(want))
 
 
+def test_screen_64_images_against_100k_rows(ctx, yp, oracle):
+    """The reference's small workload end to end: 64 seeded blob images hashed with their 8
+    dihedrals and matched at t = 31 against 100,000 rows of exactly 128 set bits plus 1,000
+    rows planted at distances U{0..40} from randomly chosen dihedral hashes of the images.
+    Hashes equal the oracle's f32 pipeline; hits equal its scalar matcher's over them."""
+    imgs = yp.synth.blob_images(64, seed=2025)
+    h, q, t, _ = oracle.hash_batch(imgs)
+    queries = h.reshape(-1, 32)
+    rng = np.random.default_rng(2027)
+    qid = rng.integers(0, queries.shape[0], 1000)
+    dist = rng.integers(0, 41, 1000)
+    planted = np.stack([yp.synth.flip_bits(queries[q_], int(d_), rng)
+                        for q_, d_ in zip(qid, dist)])
+    rows = np.concatenate([yp.synth.rows_128(100_000, seed=2026), planted])
+    pos = np.arange(100_000, 101_000)
+    db = yp.Database(ctx, rows)
+    hits, hashes = yp.screen_host(ctx, db, imgs, threshold=31, want_hashes=True)
+    db.close()
+    assert np.array_equal(hashes, h)
+    want = oracle.find_all(rows, queries, 31)
+    assert np.array_equal(as_tuples(hits), as_tuples(want))
+    # every planted row within the threshold is found at (at most) its planted distance
+    found = {(int(i), int(qq)): int(d) for i, qq, d in as_tuples(hits)}
+    for p_, q_, d_ in zip(pos, qid, dist):
+        if d_ <= 31:
+            assert found[(int(p_), int(q_))] <= d_
+
+
 def test_screen_host_reference_kernel(ctx, yp, oracle):
     """ypdq_screen_host with YPDQ_COMPRESS_JAROSZ: the hashes are ypdq_hash_batch's
     ReferenceKernel hashes (pinned to the oracle in test_gpu_hash.py) and the hits are the
