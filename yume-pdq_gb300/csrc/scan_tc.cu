@@ -33,6 +33,13 @@
 //               tiles in flight.
 // Queries are processed in passes of N <= 256; the database streams once per pass. The
 // shared memory left after the operands holds as many packed tiles in flight as fit.
+//
+// kHalfK (passes of 256 queries, t <= 36): only the first 128 bits of rows and queries are
+// expanded and multiplied (4 MMAs per tile instead of 8). Their distance is a lower bound
+// of the full one, so a pair can only be a hit if that partial distance is <= t; the
+// epilogue re-checks every such candidate exactly with popcounts of the packed row and
+// query and reports the exact distance. For random rows a 128-bit partial distance is
+// 64 +- 6, so candidates are rare and the hit set is the full scan's.
 #include <cuda_fp16.h>
 
 #include "ypdq_internal.cuh"
@@ -141,12 +148,14 @@ __host__ __device__ constexpr uint32_t idesc_f8(uint32_t n) {
 // makes each 4-byte output word a shift, a mask and an OR: byte i of output word m (m = 0..7)
 // of packed word p holds bit 8i + 7 - m of that word, which `<< m` moves to the byte's sign
 // bit. Output word (p, m) goes to K chunk p / 4, 16-byte unit 2 (p % 4) + m / 4.
+// kHalf: only packed words 0..3 (K chunk 0, the first 128 bits).
+template <bool kHalf = false>
 __device__ __forceinline__ void expand_row(const uint4 w0, const uint4 w1, uint8_t* chunk0,
                                            uint8_t* chunk1, int row) {
   const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
   const int sw = row & 7;
 #pragma unroll
-  for (int p = 0; p < 8; ++p) {
+  for (int p = 0; p < (kHalf ? 4 : 8); ++p) {
     uint8_t* base = (p < 4 ? chunk0 : chunk1) + row * 128;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -223,13 +232,41 @@ __device__ __forceinline__ void emit_hit(bool row_ok, uint64_t row, uint64_t q, 
   }
 }
 
+// kHalfK: the same for a candidate whose exact distance d the epilogue has computed.
+__device__ __forceinline__ void emit_hit_exact(bool cand, uint64_t row, uint64_t q, uint32_t d,
+                                               const Params& prm, int lane) {
+  const bool hit = cand && d <= prm.threshold;
+  const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
+  if (ballot == 0) return;
+  const int leader = __ffs(ballot) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(prm.count, static_cast<unsigned long long>(__popc(ballot)));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (hit) {
+    const uint64_t pos = base + __popc(ballot & lanemask_lt());
+    if (pos < prm.capacity) {
+      ypdq_hit h;
+      h.index = row;
+      h.query = static_cast<uint32_t>(q) + prm.query_base;
+      h.distance = d;
+      prm.hits[pos] = h;
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t popc256(uint4 a0, uint4 a1, uint4 b0, uint4 b1) {
+  return __popc(a0.x ^ b0.x) + __popc(a0.y ^ b0.y) + __popc(a0.z ^ b0.z) + __popc(a0.w ^ b0.w) +
+         __popc(a1.x ^ b1.x) + __popc(a1.y ^ b1.y) + __popc(a1.z ^ b1.z) + __popc(a1.w ^ b1.w);
+}
+
 __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
   *reinterpret_cast<volatile int*>(&sm.abort_flag) = 1;
   atomicOr(dev_err, kDevErrTimeout);
 }
 
-template <bool kDual>
+template <bool kDual, bool kHalfK>
 __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Params prm) {
+  static_assert(!(kDual && kHalfK), "the half-K variant is for passes of 256 queries");
   extern __shared__ uint8_t smem_raw[];
   // Align by offsetting the shared array itself so the compiler keeps the shared address
   // space (an integer round trip would turn every access into a generic one).
@@ -344,7 +381,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
         const uint64_t qi = static_cast<uint64_t>(p) * N + qr;
         if (qi < n_queries) {
           const uint4* src = reinterpret_cast<const uint4*>(prm.queries + qi * 32);
-          expand_row(src[0], src[1], bchunk0, bchunk1, static_cast<int>(qr));
+          expand_row<kHalfK>(src[0], src[1], bchunk0, bchunk1, static_cast<int>(qr));
         } else {
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
@@ -381,7 +418,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           }
         } else {
           uint8_t* a = a_smem + static_cast<size_t>(as) * 2 * kChunkBytes;
-          expand_row(w0, w1, a, a + kChunkBytes, arow);
+          expand_row<kHalfK>(w0, w1, a, a + kChunkBytes, arow);
           fence_proxy_async_smem();
         }
         __syncwarp();
@@ -440,7 +477,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
             const uint32_t a0 = smem_u32(a_smem + static_cast<size_t>(as) * 2 * kChunkBytes);
             const uint32_t a1 = a0 + kChunkBytes;
 #pragma unroll
-            for (int ks = 0; ks < 8; ++ks) {
+            for (int ks = 0; ks < (kHalfK ? 4 : 8); ++ks) {
               const uint32_t off = (ks & 3) * 32;
               const uint64_t ad = sw128_desc((ks < 4 ? a0 : a1) + off);
               const uint64_t bd = sw128_desc((ks < 4 ? b0 : b1) + off);
@@ -480,7 +517,8 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
   // alternate 64-column chunks of the accumulator, or with kDual and N = 64 alternate tiles
   // (one accumulator stage each), so that both groups work on a narrow pass
   {
-    const float dot_min = 256.0f - 2.0f * static_cast<float>(prm.threshold);
+    // kHalfK: the accumulator holds 128 - 2 * (distance over the first 128 bits)
+    const float dot_min = (kHalfK ? 128.0f : 256.0f) - 2.0f * static_cast<float>(prm.threshold);
     const uint32_t quarter = static_cast<uint32_t>(warp & 3);
     const uint32_t group = static_cast<uint32_t>(warp >> 2);
     const uint32_t lane_addr = (quarter * 32) << 16;
@@ -511,14 +549,39 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           for (int i = 1; i < 32; ++i) mh = __hmax2(mh, *reinterpret_cast<const __half2*>(&raw[i]));
           const float m = fmaxf(__low2float(mh), __high2float(mh));
           if (__any_sync(0xffffffffu, row_ok && m >= dot_min)) {
-            // rare: some lane holds a hit in these 64 columns; fully unrolled so that the
-            // accumulator words stay in registers
+            // rare: some lane holds a hit (kHalfK: a candidate) in these 64 columns; fully
+            // unrolled so that the accumulator words stay in registers
+            if constexpr (kHalfK) {
+              uint4 r0 = make_uint4(0, 0, 0, 0), r1 = r0;
+              if (row_ok) {
+                const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + row * 32);
+                r0 = rp[0];
+                r1 = rp[1];
+              }
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              const __half2 h2 = *reinterpret_cast<const __half2*>(&raw[j]);
-              emit_hit(row_ok, row, q0 + c0 + 2 * j, __low2float(h2), dot_min, prm, lane, n_queries);
-              emit_hit(row_ok, row, q0 + c0 + 2 * j + 1, __high2float(h2), dot_min, prm, lane,
-                       n_queries);
+              for (int j = 0; j < 64; ++j) {
+                const __half2 h2 = *reinterpret_cast<const __half2*>(&raw[j >> 1]);
+                const float v = (j & 1) ? __high2float(h2) : __low2float(h2);
+                const uint64_t q = q0 + c0 + j;
+                const bool cand = row_ok && q < n_queries && v >= dot_min;
+                if (__any_sync(0xffffffffu, cand)) {
+                  uint32_t d = 0;
+                  if (cand) {
+                    const uint4* qp = reinterpret_cast<const uint4*>(prm.queries + q * 32);
+                    d = popc256(r0, r1, qp[0], qp[1]);
+                  }
+                  emit_hit_exact(cand, row, q, d, prm, lane);
+                }
+              }
+            } else {
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                const __half2 h2 = *reinterpret_cast<const __half2*>(&raw[j]);
+                emit_hit(row_ok, row, q0 + c0 + 2 * j, __low2float(h2), dot_min, prm, lane,
+                         n_queries);
+                emit_hit(row_ok, row, q0 + c0 + 2 * j + 1, __high2float(h2), dot_min, prm, lane,
+                         n_queries);
+              }
             }
           }
         }
@@ -537,13 +600,14 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
 }  // namespace tc
 
 cudaError_t scan_tc_init() {
-  cudaError_t e = cudaFuncSetAttribute(tc::scan_tc_kernel<true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(tc::kSmemLimit));
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(tc::scan_tc_kernel<false>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(tc::kSmemLimit));
+  for (const void* f : {reinterpret_cast<const void*>(tc::scan_tc_kernel<true, false>),
+                        reinterpret_cast<const void*>(tc::scan_tc_kernel<false, false>),
+                        reinterpret_cast<const void*>(tc::scan_tc_kernel<false, true>)}) {
+    const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(tc::kSmemLimit));
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
@@ -590,10 +654,14 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   const size_t smem = b_end + stages * tc::kPackBytes + 1024;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
+  // passes of 256 queries at a small threshold: the first 128 bits bound the distance
+  const bool half_k = !dual && p.threshold <= 36;
   if (dual)
-    tc::scan_tc_kernel<true><<<static_cast<unsigned>(grid), tc::threads_of(true), smem, s>>>(prm);
+    tc::scan_tc_kernel<true, false><<<static_cast<unsigned>(grid), tc::threads_of(true), smem, s>>>(prm);
+  else if (half_k)
+    tc::scan_tc_kernel<false, true><<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
   else
-    tc::scan_tc_kernel<false><<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
+    tc::scan_tc_kernel<false, false><<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
   return cudaGetLastError();
 }
 
