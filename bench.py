@@ -478,9 +478,12 @@ def run_ours(args):
     algo = scan_algo_used(args.algo, nq, args.threshold)
     scan_launches = 1 if algo == 3 else (nq + 2047) // 2048
     if scan_avg >= hash_avg and algo == 3:
-        # tensor-core scan: 2 * 256 FP8 flops per (row, query) pair, one launch per step;
-        # FP8 dense peak taken as 2x the measured bf16 dense burst (the nominal 4.5 : 2.25 ratio)
-        flops = 2.0 * 256 * nq * n
+        # tensor-core scan, one launch per step: FP8 flops the MMAs execute per (row, query)
+        # pair, 2 * 256, or 2 * 128 when passes of 256 queries at t <= 36 multiply only the
+        # first 128 bits (an exact lower bound; mirrors launch_scan_tc); FP8 dense peak taken
+        # as 2x the measured bf16 dense burst (the nominal 4.5 : 2.25 ratio)
+        k_bits = 128 if (nq > 128 and args.threshold <= 36) else 256
+        flops = 2.0 * k_bits * nq * n
         achieved = flops / (scan_avg / 1000.0) / 1e12
         # DRAM traffic: 320.5 MB per query pass of 256 (ncu capture of the 10M-row scan at
         # 2,048 queries, profiles/scan_tc_10M_rows_2048_queries.md), scaled by passes and rows
@@ -492,6 +495,8 @@ def run_ours(args):
                     "traffic_unit": "bytes per launch (scaled from an ncu capture)",
                     "peak_source": "%s bf16 burst x 2 (fp8 dense)" % peak_kind,
                     "launch_ms": scan_avg, "launches_per_step": 1,
+                    "mma_k_bits": k_bits,
+                    "pairs_per_s": nq * n / (scan_avg / 1e3),
                     "db_stream_gbs": (n * 32 * ((nq + 255) // 256)) / (scan_avg / 1e3) / 1e9}
     elif scan_avg >= hash_avg:
         # SIMT scan: one launch reads the whole database once for up to 2048 queries

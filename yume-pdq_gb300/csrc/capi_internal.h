@@ -18,7 +18,7 @@ struct ypdq_ctx {
   int* d_err = nullptr;
   cudaStream_t stream = nullptr;       // compute stream of the blocking _host calls
   cudaStream_t copy_stream = nullptr;  // host->device copies that overlap that compute
-  static constexpr int kMaxChunks = 8;
+  static constexpr int kMaxChunks = 32;
   cudaEvent_t chunk_copied[kMaxChunks] = {};
   std::mutex mu;                  // guards the scratch buffers below
   void* scratch[8] = {};
