@@ -146,7 +146,9 @@ def measured_peaks():
 def scan_algo_used(algo, nq, threshold):
     """The algorithm ypdq_scan runs for YPDQ_SCAN_AUTO (mirrors auto_scan_algo in scan.cu)."""
     if algo == 0:
-        return 1 if nq <= (36 if threshold <= 34 else 24 if threshold <= 62 else 12) else 3
+        simt_max = (24 if threshold <= 34 else 16 if threshold <= 36 else
+                    24 if threshold <= 62 else 12)
+        return 1 if nq <= simt_max else 3
     return algo
 
 

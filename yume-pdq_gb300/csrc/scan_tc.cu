@@ -34,7 +34,7 @@
 // Queries are processed in passes of N <= 256; the database streams once per pass. The
 // shared memory left after the operands holds as many packed tiles in flight as fit.
 //
-// kHalfK (passes of 256 queries, t <= 36): only the first 128 bits of rows and queries are
+// kHalfK (t <= 36, any pass width): only the first 128 bits of rows and queries are
 // expanded and multiplied (4 MMAs per tile instead of 8). Their distance is a lower bound
 // of the full one, so a pair can only be a hit if that partial distance is <= t; the
 // epilogue re-checks every such candidate exactly with popcounts of the packed row and
@@ -58,7 +58,7 @@ constexpr int kTileRows = 128;
 constexpr int kMaxN = 256;
 constexpr int kMaxPackStages = 16;
 constexpr int kAStages = 4;       // A tiles in shared memory (32 KiB each)
-constexpr int kMaxAStages = 6;    // A tiles in tensor memory (kDual; 64 columns each)
+constexpr int kMaxAStages = 8;    // A tiles in tensor memory (kDual; 64 or 32 columns each)
 constexpr int kAccStages = 2;
 constexpr int kTmemCols = 512;
 constexpr int kChunkBytes = kTileRows * 128;  // one 128-byte K-chunk of a 128-row tile
@@ -173,12 +173,14 @@ __device__ __forceinline__ void expand_row(const uint4 w0, const uint4 w1, uint8
 
 // The expansion of expand_row as 64 column words of one TMEM lane: K element 4 c + i is
 // byte i of column c. Output word (p, m) of expand_row holds K elements 32 p + 4 m .. + 3,
-// so it is column 8 p + m, and rows and queries keep the same bijection.
+// so it is column 8 p + m, and rows and queries keep the same bijection. kHalf: the first
+// 32 columns only (packed words 0..3, the first 128 bits).
+template <bool kHalf = false>
 __device__ __forceinline__ void expand_row_tmem(const uint4 w0, const uint4 w1,
                                                 uint32_t taddr) {
   const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
-  for (int half = 0; half < 2; ++half) {
+  for (int half = 0; half < (kHalf ? 1 : 2); ++half) {
     uint32_t r[32];
 #pragma unroll
     for (int pp = 0; pp < 4; ++pp) {
@@ -266,7 +268,7 @@ __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
 
 template <bool kDual, bool kHalfK>
 __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Params prm) {
-  static_assert(!(kDual && kHalfK), "the half-K variant is for passes of 256 queries");
+  constexpr uint32_t kACols = kHalfK ? 32 : 64;  // TMEM columns of one A tile (kDual)
   extern __shared__ uint8_t smem_raw[];
   // Align by offsetting the shared array itself so the compiler keeps the shared address
   // space (an integer round trip would turn every access into a generic one).
@@ -409,7 +411,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
         if (!mbar_wait(&sm.a_empty[as], aph ^ 1u, abort_flag)) goto fail;
         if constexpr (kDual) {
           __syncwarp();  // tcgen05.st is .sync.aligned: the lanes leave the wait one by one
-          expand_row_tmem(w0, w1, tmem_base + a_lane + a_col0 + 64 * as);
+          expand_row_tmem<kHalfK>(w0, w1, tmem_base + a_lane + a_col0 + kACols * as);
           tmem_st_wait();
           tc_fence_before();
           if (++as_t == n_a) {
@@ -467,9 +469,9 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           tc_fence_after();
           const uint32_t d = tmem_base + ac * N;
           if constexpr (kDual) {
-            const uint32_t ta = tmem_base + a_col0 + 64 * as;  // lane 0; K = 32 per 8 columns
+            const uint32_t ta = tmem_base + a_col0 + kACols * as;  // lane 0; K = 32 per 8 columns
 #pragma unroll
-            for (int ks = 0; ks < 8; ++ks) {
+            for (int ks = 0; ks < (kHalfK ? 4 : 8); ++ks) {
               const uint64_t bd = sw128_desc((ks < 4 ? b0 : b1) + (ks & 3) * 32);
               mma_f8_ta(d, ta + 8 * ks, bd, idesc, ks > 0 ? 1u : 0u);
             }
@@ -601,6 +603,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
 
 cudaError_t scan_tc_init() {
   for (const void* f : {reinterpret_cast<const void*>(tc::scan_tc_kernel<true, false>),
+                        reinterpret_cast<const void*>(tc::scan_tc_kernel<true, true>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, false>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, true>)}) {
     const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -634,9 +637,11 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   // passes of <= 128 queries: two MMA issuers and A in tensor memory (the pass is bound by
   // issuing and shared-memory traffic, not by the tensor core)
   const bool dual = prm.n_tile <= 128;
+  // at a small threshold the first 128 bits bound the distance (kHalfK)
+  const bool half_k = p.threshold <= 36;
   uint32_t a_stages = tc::kAStages;
   if (dual) {
-    a_stages = (tc::kTmemCols - tc::kAccStages * prm.n_tile) / 64;
+    a_stages = (tc::kTmemCols - tc::kAccStages * prm.n_tile) / (half_k ? 32 : 64);
     if (a_stages > static_cast<uint32_t>(tc::kMaxAStages)) a_stages = tc::kMaxAStages;
   }
   prm.a_stages = a_stages;
@@ -654,9 +659,9 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   const size_t smem = b_end + stages * tc::kPackBytes + 1024;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
-  // passes of 256 queries at a small threshold: the first 128 bits bound the distance
-  const bool half_k = !dual && p.threshold <= 36;
-  if (dual)
+  if (dual && half_k)
+    tc::scan_tc_kernel<true, true><<<static_cast<unsigned>(grid), tc::threads_of(true), smem, s>>>(prm);
+  else if (dual)
     tc::scan_tc_kernel<true, false><<<static_cast<unsigned>(grid), tc::threads_of(true), smem, s>>>(prm);
   else if (half_k)
     tc::scan_tc_kernel<false, true><<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
