@@ -25,8 +25,9 @@ def test_scan_matches_oracle(ctx, yp, oracle, algo, n_rows, n_q):
     q = yp.synth.rows_128(n_q, seed=n_q + 1000)
     if n_rows:
         yp.synth.plant(rows, q, min(n_rows, 60), 0, 96, seed=7)
-    # both sides of the SIMT scan's prefix-bound switches (t = 34 / 35 and 62 / 63)
-    for t in (0, 16, 31, 34, 35, 48, 62, 63, 90):
+    # both sides of the SIMT scan's prefix-bound switches (t = 34 / 35 and 62 / 63) and of
+    # the tensor-core scan's 128-bit bound (t = 36 / 37)
+    for t in (0, 16, 31, 34, 35, 36, 37, 48, 62, 63, 90):
         got = yp.scan(ctx, rows, q, t, algo=algo)
         want = oracle.find_all(rows, q, t)
         assert np.array_equal(as_tuples(got), as_tuples(want)), (t, len(got), len(want))
