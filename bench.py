@@ -481,10 +481,11 @@ def run_ours(args):
     scan_launches = 1 if algo == 3 else (nq + 2047) // 2048
     if scan_avg >= hash_avg and algo == 3:
         # tensor-core scan, one launch per step: FP8 flops the MMAs execute per (row, query)
-        # pair, 2 * 256, or 2 * 128 when passes of 256 queries at t <= 36 multiply only the
-        # first 128 bits (an exact lower bound; mirrors launch_scan_tc); FP8 dense peak taken
-        # as 2x the measured bf16 dense burst (the nominal 4.5 : 2.25 ratio)
-        k_bits = 128 if (nq > 128 and args.threshold <= 36) else 256
+        # pair, 2 * K: K = 128 at t <= 36 and 192 for passes of 256 queries at t <= 62 (the
+        # prefix bound; mirrors launch_scan_tc), else 256; FP8 dense peak taken as 2x the
+        # measured bf16 dense burst (the nominal 4.5 : 2.25 ratio)
+        k_bits = (128 if args.threshold <= 36 else
+                  192 if (nq > 128 and args.threshold <= 62) else 256)
         flops = 2.0 * k_bits * nq * n
         achieved = flops / (scan_avg / 1000.0) / 1e12
         # DRAM traffic: 320.5 MB per query pass of 256 (ncu capture of the 10M-row scan at

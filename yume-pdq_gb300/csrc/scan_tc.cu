@@ -34,12 +34,14 @@
 // Queries are processed in passes of N <= 256; the database streams once per pass. The
 // shared memory left after the operands holds as many packed tiles in flight as fit.
 //
-// kHalfK (t <= 36, any pass width): only the first 128 bits of rows and queries are
-// expanded and multiplied (4 MMAs per tile instead of 8). Their distance is a lower bound
+// kKSteps < 8 (a prefix bound): only the first 32 * kKSteps bits of rows and queries are
+// expanded and multiplied (kKSteps MMAs per tile instead of 8): 128 bits at t <= 36 (any
+// pass width), 192 bits at t <= 62 (passes of 256 queries). Their distance is a lower bound
 // of the full one, so a pair can only be a hit if that partial distance is <= t; the
 // epilogue re-checks every such candidate exactly with popcounts of the packed row and
 // query and reports the exact distance. For random rows a 128-bit partial distance is
-// 64 +- 6, so candidates are rare and the hit set is the full scan's.
+// 64 +- 6 and a 192-bit one 96 +- 7, so candidates are rare and the hit set is the full
+// scan's.
 #include <cuda_fp16.h>
 
 #include "ypdq_internal.cuh"
@@ -148,14 +150,14 @@ __host__ __device__ constexpr uint32_t idesc_f8(uint32_t n) {
 // makes each 4-byte output word a shift, a mask and an OR: byte i of output word m (m = 0..7)
 // of packed word p holds bit 8i + 7 - m of that word, which `<< m` moves to the byte's sign
 // bit. Output word (p, m) goes to K chunk p / 4, 16-byte unit 2 (p % 4) + m / 4.
-// kHalf: only packed words 0..3 (K chunk 0, the first 128 bits).
-template <bool kHalf = false>
+// kWords < 8: only packed words 0 .. kWords - 1 (the first 32 * kWords bits).
+template <int kWords = 8>
 __device__ __forceinline__ void expand_row(const uint4 w0, const uint4 w1, uint8_t* chunk0,
                                            uint8_t* chunk1, int row) {
   const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
   const int sw = row & 7;
 #pragma unroll
-  for (int p = 0; p < (kHalf ? 4 : 8); ++p) {
+  for (int p = 0; p < kWords; ++p) {
     uint8_t* base = (p < 4 ? chunk0 : chunk1) + row * 128;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -234,7 +236,7 @@ __device__ __forceinline__ void emit_hit(bool row_ok, uint64_t row, uint64_t q, 
   }
 }
 
-// kHalfK: the same for a candidate whose exact distance d the epilogue has computed.
+// kKSteps < 8: the same for a candidate whose exact distance d the epilogue has computed.
 __device__ __forceinline__ void emit_hit_exact(bool cand, uint64_t row, uint64_t q, uint32_t d,
                                                const Params& prm, int lane) {
   const bool hit = cand && d <= prm.threshold;
@@ -266,9 +268,11 @@ __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
   atomicOr(dev_err, kDevErrTimeout);
 }
 
-template <bool kDual, bool kHalfK>
+template <bool kDual, int kKSteps>
 __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Params prm) {
-  constexpr uint32_t kACols = kHalfK ? 32 : 64;  // TMEM columns of one A tile (kDual)
+  static_assert(kKSteps == 4 || kKSteps == 8 || (!kDual && kKSteps == 6), "K steps");
+  constexpr bool kPrefix = kKSteps < 8;
+  constexpr uint32_t kACols = kKSteps == 4 ? 32 : 64;  // TMEM columns of one A tile (kDual)
   extern __shared__ uint8_t smem_raw[];
   // Align by offsetting the shared array itself so the compiler keeps the shared address
   // space (an integer round trip would turn every access into a generic one).
@@ -383,7 +387,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
         const uint64_t qi = static_cast<uint64_t>(p) * N + qr;
         if (qi < n_queries) {
           const uint4* src = reinterpret_cast<const uint4*>(prm.queries + qi * 32);
-          expand_row<kHalfK>(src[0], src[1], bchunk0, bchunk1, static_cast<int>(qr));
+          expand_row<kKSteps>(src[0], src[1], bchunk0, bchunk1, static_cast<int>(qr));
         } else {
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
@@ -411,7 +415,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
         if (!mbar_wait(&sm.a_empty[as], aph ^ 1u, abort_flag)) goto fail;
         if constexpr (kDual) {
           __syncwarp();  // tcgen05.st is .sync.aligned: the lanes leave the wait one by one
-          expand_row_tmem<kHalfK>(w0, w1, tmem_base + a_lane + a_col0 + kACols * as);
+          expand_row_tmem<kKSteps == 4>(w0, w1, tmem_base + a_lane + a_col0 + kACols * as);
           tmem_st_wait();
           tc_fence_before();
           if (++as_t == n_a) {
@@ -420,7 +424,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           }
         } else {
           uint8_t* a = a_smem + static_cast<size_t>(as) * 2 * kChunkBytes;
-          expand_row<kHalfK>(w0, w1, a, a + kChunkBytes, arow);
+          expand_row<kKSteps>(w0, w1, a, a + kChunkBytes, arow);
           fence_proxy_async_smem();
         }
         __syncwarp();
@@ -471,7 +475,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           if constexpr (kDual) {
             const uint32_t ta = tmem_base + a_col0 + kACols * as;  // lane 0; K = 32 per 8 columns
 #pragma unroll
-            for (int ks = 0; ks < (kHalfK ? 4 : 8); ++ks) {
+            for (int ks = 0; ks < kKSteps; ++ks) {
               const uint64_t bd = sw128_desc((ks < 4 ? b0 : b1) + (ks & 3) * 32);
               mma_f8_ta(d, ta + 8 * ks, bd, idesc, ks > 0 ? 1u : 0u);
             }
@@ -479,7 +483,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
             const uint32_t a0 = smem_u32(a_smem + static_cast<size_t>(as) * 2 * kChunkBytes);
             const uint32_t a1 = a0 + kChunkBytes;
 #pragma unroll
-            for (int ks = 0; ks < (kHalfK ? 4 : 8); ++ks) {
+            for (int ks = 0; ks < kKSteps; ++ks) {
               const uint32_t off = (ks & 3) * 32;
               const uint64_t ad = sw128_desc((ks < 4 ? a0 : a1) + off);
               const uint64_t bd = sw128_desc((ks < 4 ? b0 : b1) + off);
@@ -519,8 +523,8 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
   // alternate 64-column chunks of the accumulator, or with kDual and N = 64 alternate tiles
   // (one accumulator stage each), so that both groups work on a narrow pass
   {
-    // kHalfK: the accumulator holds 128 - 2 * (distance over the first 128 bits)
-    const float dot_min = (kHalfK ? 128.0f : 256.0f) - 2.0f * static_cast<float>(prm.threshold);
+    // the accumulator holds 32 * kKSteps - 2 * (distance over the first 32 * kKSteps bits)
+    const float dot_min = 32.0f * kKSteps - 2.0f * static_cast<float>(prm.threshold);
     const uint32_t quarter = static_cast<uint32_t>(warp & 3);
     const uint32_t group = static_cast<uint32_t>(warp >> 2);
     const uint32_t lane_addr = (quarter * 32) << 16;
@@ -551,9 +555,9 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           for (int i = 1; i < 32; ++i) mh = __hmax2(mh, *reinterpret_cast<const __half2*>(&raw[i]));
           const float m = fmaxf(__low2float(mh), __high2float(mh));
           if (__any_sync(0xffffffffu, row_ok && m >= dot_min)) {
-            // rare: some lane holds a hit (kHalfK: a candidate) in these 64 columns; fully
+            // rare: some lane holds a hit (kPrefix: a candidate) in these 64 columns; fully
             // unrolled so that the accumulator words stay in registers
-            if constexpr (kHalfK) {
+            if constexpr (kPrefix) {
               uint4 r0 = make_uint4(0, 0, 0, 0), r1 = r0;
               if (row_ok) {
                 const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + row * 32);
@@ -602,10 +606,11 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
 }  // namespace tc
 
 cudaError_t scan_tc_init() {
-  for (const void* f : {reinterpret_cast<const void*>(tc::scan_tc_kernel<true, false>),
-                        reinterpret_cast<const void*>(tc::scan_tc_kernel<true, true>),
-                        reinterpret_cast<const void*>(tc::scan_tc_kernel<false, false>),
-                        reinterpret_cast<const void*>(tc::scan_tc_kernel<false, true>)}) {
+  for (const void* f : {reinterpret_cast<const void*>(tc::scan_tc_kernel<true, 4>),
+                        reinterpret_cast<const void*>(tc::scan_tc_kernel<true, 8>),
+                        reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 4>),
+                        reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 6>),
+                        reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 8>)}) {
     const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                static_cast<int>(tc::kSmemLimit));
     if (e != cudaSuccess) return e;
@@ -637,7 +642,7 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   // passes of <= 128 queries: two MMA issuers and A in tensor memory (the pass is bound by
   // issuing and shared-memory traffic, not by the tensor core)
   const bool dual = prm.n_tile <= 128;
-  // at a small threshold the first 128 bits bound the distance (kHalfK)
+  // at a small threshold the first 128 bits bound the distance (kKSteps = 4)
   const bool half_k = p.threshold <= 36;
   uint32_t a_stages = tc::kAStages;
   if (dual) {
@@ -659,14 +664,19 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   const size_t smem = b_end + stages * tc::kPackBytes + 1024;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
+  // passes of 256 queries at t <= 62: the first 192 bits bound the distance
+  const bool prefix192 = !dual && !half_k && p.threshold <= 62;
+  const unsigned g = static_cast<unsigned>(grid);
   if (dual && half_k)
-    tc::scan_tc_kernel<true, true><<<static_cast<unsigned>(grid), tc::threads_of(true), smem, s>>>(prm);
+    tc::scan_tc_kernel<true, 4><<<g, tc::threads_of(true), smem, s>>>(prm);
   else if (dual)
-    tc::scan_tc_kernel<true, false><<<static_cast<unsigned>(grid), tc::threads_of(true), smem, s>>>(prm);
+    tc::scan_tc_kernel<true, 8><<<g, tc::threads_of(true), smem, s>>>(prm);
   else if (half_k)
-    tc::scan_tc_kernel<false, true><<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
+    tc::scan_tc_kernel<false, 4><<<g, tc::threads_of(false), smem, s>>>(prm);
+  else if (prefix192)
+    tc::scan_tc_kernel<false, 6><<<g, tc::threads_of(false), smem, s>>>(prm);
   else
-    tc::scan_tc_kernel<false, false><<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
+    tc::scan_tc_kernel<false, 8><<<g, tc::threads_of(false), smem, s>>>(prm);
   return cudaGetLastError();
 }
 
