@@ -544,12 +544,8 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
         tc_fence_after();
         const uint64_t row = tile * kTileRows + quarter * 32 + lane;
         const bool row_ok = row < prm.n_rows;
-        for (uint32_t c0 = by_tile ? 0u : 64 * group; c0 < N; c0 += 64 * (kEpilogueWarps / 4)) {
-          uint32_t raw[32];
-          float unused[32];
-          tmem_ld64_pack16_nowait(tmem_base + lane_addr + ac * N + c0, raw);
-          tmem_ld_wait();
-          tmem_take(raw, unused);
+        // the 64 accumulator columns c .. c + 63 in raw: any hit (or candidate) in them?
+        auto scan_chunk = [&](const uint32_t (&raw)[32], uint32_t c0) {
           __half2 mh = *reinterpret_cast<const __half2*>(&raw[0]);
 #pragma unroll
           for (int i = 1; i < 32; ++i) mh = __hmax2(mh, *reinterpret_cast<const __half2*>(&raw[i]));
@@ -589,6 +585,31 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
                          n_queries);
               }
             }
+          }
+        };
+        float unused[32];
+        if constexpr (!kDual && kKSteps == 4) {
+          // N = 192 or 256 with the 128-bit bound: group g reads chunks g and g + 2 with
+          // both loads in flight before one wait (the readout is on the pass's critical path
+          // once the MMAs are cut to a quarter of the tile's time; with 6 or 8 MMAs the extra
+          // registers cost more than the overlap gains)
+          const uint32_t c0 = 64 * group, c1 = c0 + 128;
+          const bool two = c1 < N;
+          uint32_t raw0[32], raw1[32];
+          tmem_ld64_pack16_nowait(tmem_base + lane_addr + ac * N + c0, raw0);
+          if (two) tmem_ld64_pack16_nowait(tmem_base + lane_addr + ac * N + c1, raw1);
+          tmem_ld_wait();
+          tmem_take(raw0, unused);
+          if (two) tmem_take(raw1, unused);
+          scan_chunk(raw0, c0);
+          if (two) scan_chunk(raw1, c1);
+        } else {
+          for (uint32_t c0 = by_tile ? 0u : 64 * group; c0 < N; c0 += 64 * (kEpilogueWarps / 4)) {
+            uint32_t raw[32];
+            tmem_ld64_pack16_nowait(tmem_base + lane_addr + ac * N + c0, raw);
+            tmem_ld_wait();
+            tmem_take(raw, unused);
+            scan_chunk(raw, c0);
           }
         }
         tc_fence_before();
