@@ -8,28 +8,27 @@
 //     distance = (256 - dot) / 2,    hit  <=>  dot >= 256 - 2 * threshold.
 // The hit set equals the scalar matcher's (CpuMatcher::find, src/matching/mod.rs:336-362).
 //
-// CTA (one per SM, persistent over 128-row database tiles; 14 warps):
+// CTA (one per SM, persistent over 128-row database tiles; 14 warps, 15 with kDual):
 //   warps 0-7   epilogue: tcgen05.ld the 128 x N f16 accumulator, two warps per TMEM lane
-//               quarter (warp w reads lanes 32(w%4).. = tile rows, alternate 64-column
-//               chunks), half2 max against the threshold, compact hits. Reading the
-//               accumulator out of TMEM is the scan's limit (one f16 per (row, query) pair
-//               against 256 MACs), so it gets twice the warps of the other roles.
+//               quarter (warp w reads lanes 32(w%4).. = tile rows; the two groups take
+//               alternate 64-column chunks, or with kDual and N = 64 alternate tiles),
+//               half2 max against the threshold, compact hits. One f16 is read per
+//               (row, query) pair, so the readout gets twice the warps of the other roles.
 //   warp 8      producer: one lane bulk-copies packed tiles (128 rows x 32 B) into a ring.
-//   warps 9, 14 MMA: one lane issues 8 x tcgen05.mma (M=128, N, K=32) per tile into a
+//   warps 9, 14 MMA: one lane issues kKSteps tcgen05.mma (M=128, N, K=32) per tile into a
 //               double-buffered accumulator and commits to mbarriers (tcgen05.commit tracks
 //               the issuing thread's own MMAs). Issuing and its barrier handoffs keep one
 //               thread busy ~1,100 clk per tile, longer than the MMAs of a pass of <= 128
-//               queries take on the tensor core; there the two warps take alternate tiles
-//               (one accumulator stage each; kDual), 7-14 % faster. Wider passes are
-//               tensor-bound and launch without warp 14. Warp 9 also allocates and frees
-//               TMEM.
+//               queries take on the tensor core; there (kDual) the two warps take alternate
+//               tiles, one accumulator stage each. Wider passes launch without warp 14.
+//               Warp 9 also allocates and frees TMEM.
 //   warps 10-13 expanders: packed bits -> FP8 +-1. The queries (B, once per pass) go to
 //               shared memory in the 128B-swizzled K-major layout that the MMA descriptors
-//               describe. The database tiles (A) go there too for passes of 256 queries;
-//               for <= 128 (kDual) they go straight into tensor memory with tcgen05.st (row
+//               describe. The database tiles (A) go there too for passes of 192-256
+//               queries; with kDual they go straight into tensor memory with tcgen05.st (row
 //               r = TMEM lane r, K in column order) and the MMA reads A from there: a narrow
 //               pass is otherwise bound by shared-memory traffic (expansion stores plus the
-//               MMA's operand reads), and the columns the accumulators leave free hold 4-6
+//               MMA's operand reads), and the columns the accumulators leave free hold 4-8
 //               tiles in flight.
 // Queries are processed in passes of N <= 256; the database streams once per pass. The
 // shared memory left after the operands holds as many packed tiles in flight as fit.
