@@ -46,6 +46,36 @@ def test_scan_thresholds_extremes(ctx, yp, oracle, algo):
 
 
 @pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("n_q", [40, 100, 300])
+def test_dense_hits_per_row(ctx, yp, oracle, algo, n_q):
+    """Rows that hit every query of a pass: queries are variants of one hash within 6 bits,
+    planted rows within 10 bits of it, so each planted row hits all n_q queries at t >= 16
+    (several hits per lane and column chunk in the tensor-core epilogue; 300 queries make a
+    wide pass plus a 44-query tail pass)."""
+    rng = np.random.default_rng(n_q)
+    base = yp.synth.rows_128(1, seed=77)[0]
+    q = np.stack([yp.synth.flip_bits(base, int(rng.integers(0, 7)), rng) for _ in range(n_q)])
+    rows = yp.synth.rows_128(3000, seed=78)
+    pos = rng.choice(3000, size=45, replace=False)
+    for p in pos:
+        rows[p] = yp.synth.flip_bits(base, int(rng.integers(0, 11)), rng)
+    for t in (16, 31, 48, 64, 90):
+        got = yp.scan(ctx, rows, q, t, algo=algo, capacity=1 << 16)
+        want = oracle.find_all(rows, q, t)
+        assert len(want) >= 45 * n_q
+        assert np.array_equal(as_tuples(got), as_tuples(want)), (t, len(got), len(want))
+    # a hit buffer smaller than the hit count: the total is still exact, the stored hits a subset
+    d_rows, d_q = ctx.to_device(rows), ctx.to_device(q)
+    d_hits, d_cnt = ctx.alloc(1000 * 16), ctx.alloc(8)
+    yp.core.scan_device(ctx, d_rows, 3000, d_q, n_q, 31, d_hits, 1000, d_cnt, algo)
+    ctx.sync()
+    want = {tuple(x) for x in as_tuples(oracle.find_all(rows, q, 31))}
+    assert int(d_cnt.download((1,), np.uint64)[0]) == len(want)
+    stored = {tuple(x) for x in as_tuples(d_hits.download((1000,), yp.HIT_DTYPE))}
+    assert len(stored) == 1000 and stored <= want
+
+
+@pytest.mark.parametrize("algo", ALGOS)
 def test_planted_controls(ctx, yp, algo):
     """src/matching/mod.rs:460-553 structure on the GPU: no false hits, every control found."""
     rng = np.random.default_rng(0x79756D652D706471)

@@ -212,54 +212,77 @@ struct Params {
   uint32_t b_offset;      // byte offset of the expanded queries
 };
 
-// Compact one column of hits across the warp (one atomic per warp with a hit).
-__device__ __forceinline__ void emit_hit(bool row_ok, uint64_t row, uint64_t q, float v,
-                                         float dot_min, const Params& prm, int lane,
-                                         uint32_t n_queries) {
-  const bool hit = row_ok && q < n_queries && v >= dot_min;
-  const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
-  if (ballot == 0) return;
-  const int leader = __ffs(ballot) - 1;
-  unsigned long long base = 0;
-  if (lane == leader) base = atomicAdd(prm.count, static_cast<unsigned long long>(__popc(ballot)));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (hit) {
-    const uint64_t pos = base + __popc(ballot & lanemask_lt());
-    if (pos < prm.capacity) {
-      ypdq_hit h;
-      h.index = row;
-      h.query = static_cast<uint32_t>(q) + prm.query_base;
-      h.distance = static_cast<uint32_t>((256.0f - v) * 0.5f);
-      prm.hits[pos] = h;
-    }
-  }
-}
-
-// kKSteps < 8: the same for a candidate whose exact distance d the epilogue has computed.
-__device__ __forceinline__ void emit_hit_exact(bool cand, uint64_t row, uint64_t q, uint32_t d,
-                                               const Params& prm, int lane) {
-  const bool hit = cand && d <= prm.threshold;
-  const uint32_t ballot = __ballot_sync(0xffffffffu, hit);
-  if (ballot == 0) return;
-  const int leader = __ffs(ballot) - 1;
-  unsigned long long base = 0;
-  if (lane == leader) base = atomicAdd(prm.count, static_cast<unsigned long long>(__popc(ballot)));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (hit) {
-    const uint64_t pos = base + __popc(ballot & lanemask_lt());
-    if (pos < prm.capacity) {
-      ypdq_hit h;
-      h.index = row;
-      h.query = static_cast<uint32_t>(q) + prm.query_base;
-      h.distance = d;
-      prm.hits[pos] = h;
-    }
-  }
-}
-
 __device__ __forceinline__ uint32_t popc256(uint4 a0, uint4 a1, uint4 b0, uint4 b1) {
   return __popc(a0.x ^ b0.x) + __popc(a0.y ^ b0.y) + __popc(a0.z ^ b0.z) + __popc(a0.w ^ b0.w) +
          __popc(a1.x ^ b1.x) + __popc(a1.y ^ b1.y) + __popc(a1.z ^ b1.z) + __popc(a1.w ^ b1.w);
+}
+
+// Bit j set when column j of the 64 in raw (f16 pairs, one row) holds a dot product of at
+// least dot_min: a hit, or with a prefix bound a candidate.
+__device__ __forceinline__ uint64_t candidate_mask(const uint32_t (&raw)[32], float dot_min) {
+  uint32_t lo = 0, hi = 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const __half2 a = *reinterpret_cast<const __half2*>(&raw[i]);
+    const __half2 b = *reinterpret_cast<const __half2*>(&raw[16 + i]);
+    lo |= (__low2float(a) >= dot_min ? 1u : 0u) << (2 * i);
+    lo |= (__high2float(a) >= dot_min ? 1u : 0u) << (2 * i + 1);
+    hi |= (__low2float(b) >= dot_min ? 1u : 0u) << (2 * i);
+    hi |= (__high2float(b) >= dot_min ? 1u : 0u) << (2 * i + 1);
+  }
+  return (static_cast<uint64_t>(hi) << 32) | lo;
+}
+
+// Report this lane's candidates (bit j of cand: query q_first + j against `row`): the exact
+// distance of each from popcounts of the packed row and query, the ones within the threshold
+// written as hits at positions taken with one atomic per warp. Called by all 32 lanes; a
+// lane without candidates passes cand = 0. The loops run once per candidate of the lane,
+// which keeps this rare path short: it runs while the tile's epilogue warp holds up the next
+// tile, and a planted near-duplicate row makes it run for several queries of a pass.
+__device__ __forceinline__ void emit_candidates(uint64_t cand, uint64_t row, uint64_t q_first,
+                                                uint32_t n_queries, const Params& prm,
+                                                int lane) {
+  if (q_first >= n_queries) {
+    cand = 0;
+  } else if (n_queries - q_first < 64) {
+    cand &= (1ull << (n_queries - q_first)) - 1;
+  }
+  uint4 r0 = make_uint4(0, 0, 0, 0), r1 = r0;
+  if (cand) {
+    const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + row * 32);
+    r0 = __ldg(rp);
+    r1 = __ldg(rp + 1);
+  }
+  const uint8_t* const qbase = prm.queries + q_first * 32;
+  uint64_t hits = 0;
+  for (uint64_t m = cand; m; m &= m - 1) {
+    const int j = __ffsll(static_cast<long long>(m)) - 1;
+    const uint4* qp = reinterpret_cast<const uint4*>(qbase + j * 32);
+    if (popc256(r0, r1, __ldg(qp), __ldg(qp + 1)) <= prm.threshold) hits |= 1ull << j;
+  }
+  const uint32_t mine = static_cast<uint32_t>(__popcll(hits));
+  uint32_t incl = mine;  // inclusive prefix sum over the lanes
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total == 0) return;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(prm.count, static_cast<unsigned long long>(total));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  uint64_t pos = base + incl - mine;
+  for (uint64_t m = hits; m; m &= m - 1, ++pos) {
+    if (pos >= prm.capacity) break;
+    const int j = __ffsll(static_cast<long long>(m)) - 1;
+    const uint4* qp = reinterpret_cast<const uint4*>(qbase + j * 32);
+    ypdq_hit h;
+    h.index = row;
+    h.query = static_cast<uint32_t>(q_first + j) + prm.query_base;
+    h.distance = popc256(r0, r1, __ldg(qp), __ldg(qp + 1));
+    prm.hits[pos] = h;
+  }
 }
 
 __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
@@ -270,7 +293,6 @@ __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
 template <bool kDual, int kKSteps>
 __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Params prm) {
   static_assert(kKSteps == 4 || kKSteps == 8 || (!kDual && kKSteps == 6), "K steps");
-  constexpr bool kPrefix = kKSteps < 8;
   constexpr uint32_t kACols = kKSteps == 4 ? 32 : 64;  // TMEM columns of one A tile (kDual)
   extern __shared__ uint8_t smem_raw[];
   // Align by offsetting the shared array itself so the compiler keeps the shared address
@@ -543,48 +565,23 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
         tc_fence_after();
         const uint64_t row = tile * kTileRows + quarter * 32 + lane;
         const bool row_ok = row < prm.n_rows;
-        // the 64 accumulator columns c .. c + 63 in raw: any hit (or candidate) in them?
+        // the 64 accumulator columns c0 .. c0 + 63 in raw: any hit (or candidate) in them?
         auto scan_chunk = [&](const uint32_t (&raw)[32], uint32_t c0) {
           __half2 mh = *reinterpret_cast<const __half2*>(&raw[0]);
 #pragma unroll
           for (int i = 1; i < 32; ++i) mh = __hmax2(mh, *reinterpret_cast<const __half2*>(&raw[i]));
           const float m = fmaxf(__low2float(mh), __high2float(mh));
           if (__any_sync(0xffffffffu, row_ok && m >= dot_min)) {
-            // rare: some lane holds a hit (kPrefix: a candidate) in these 64 columns; fully
-            // unrolled so that the accumulator words stay in registers
-            if constexpr (kPrefix) {
-              uint4 r0 = make_uint4(0, 0, 0, 0), r1 = r0;
-              if (row_ok) {
-                const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + row * 32);
-                r0 = rp[0];
-                r1 = rp[1];
-              }
-#pragma unroll
-              for (int j = 0; j < 64; ++j) {
-                const __half2 h2 = *reinterpret_cast<const __half2*>(&raw[j >> 1]);
-                const float v = (j & 1) ? __high2float(h2) : __low2float(h2);
-                const uint64_t q = q0 + c0 + j;
-                const bool cand = row_ok && q < n_queries && v >= dot_min;
-                if (__any_sync(0xffffffffu, cand)) {
-                  uint32_t d = 0;
-                  if (cand) {
-                    const uint4* qp = reinterpret_cast<const uint4*>(prm.queries + q * 32);
-                    d = popc256(r0, r1, qp[0], qp[1]);
-                  }
-                  emit_hit_exact(cand, row, q, d, prm, lane);
-                }
-              }
-            } else {
-#pragma unroll
-              for (int j = 0; j < 32; ++j) {
-                const __half2 h2 = *reinterpret_cast<const __half2*>(&raw[j]);
-                emit_hit(row_ok, row, q0 + c0 + 2 * j, __low2float(h2), dot_min, prm, lane,
-                         n_queries);
-                emit_hit(row_ok, row, q0 + c0 + 2 * j + 1, __high2float(h2), dot_min, prm, lane,
-                         n_queries);
-              }
-            }
+            const uint64_t cand = row_ok && m >= dot_min ? candidate_mask(raw, dot_min) : 0;
+            emit_candidates(cand, row, q0 + c0, n_queries, prm, lane);
           }
+        };
+        // hand the accumulator stage back once its last columns are in registers, before
+        // the (rarely slow) hit reporting
+        auto release_acc = [&]() {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
         };
         float unused[32];
         if constexpr (!kDual && kKSteps == 4) {
@@ -600,20 +597,25 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           tmem_ld_wait();
           tmem_take(raw0, unused);
           if (two) tmem_take(raw1, unused);
+          release_acc();
           scan_chunk(raw0, c0);
           if (two) scan_chunk(raw1, c1);
         } else {
-          for (uint32_t c0 = by_tile ? 0u : 64 * group; c0 < N; c0 += 64 * (kEpilogueWarps / 4)) {
+          const uint32_t step = 64 * (kEpilogueWarps / 4);
+          bool released = false;
+          for (uint32_t c0 = by_tile ? 0u : 64 * group; c0 < N; c0 += step) {
             uint32_t raw[32];
             tmem_ld64_pack16_nowait(tmem_base + lane_addr + ac * N + c0, raw);
             tmem_ld_wait();
             tmem_take(raw, unused);
+            if (c0 + step >= N) {
+              release_acc();
+              released = true;
+            }
             scan_chunk(raw, c0);
           }
+          if (!released) release_acc();
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
       }
     }
     if (!ok && lane == 0) raise_abort(sm, prm.dev_err);
