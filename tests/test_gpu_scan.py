@@ -275,6 +275,20 @@ def test_screen_host_chunked(ctx, yp, oracle):
     assert np.array_equal(as_tuples(hits_u8), as_tuples(oracle.find_all(rows, hu.reshape(-1, 32), 31)))
 
 
+def test_screen_host_growing_chunks(ctx, yp, oracle):
+    """Against 4M rows a u8 image takes longer to hash and scan than to copy, so the chunks
+    of ypdq_screen_host grow geometrically from 32 images (the other screen tests run even
+    chunks); the hit list must equal the oracle's."""
+    imgs = yp.synth.to_u8(yp.synth.blob_images(600, seed=47))
+    h, _, _, _ = oracle.hash_batch(imgs)
+    queries = h.reshape(-1, 32)
+    rows = oracle.synth_rows(4_000_000, 48)
+    yp.synth.plant(rows, queries, 3000, 0, 40, seed=49)
+    db = yp.Database(ctx, rows)
+    hits = yp.screen_host(ctx, db, imgs, threshold=31)
+    assert np.array_equal(as_tuples(hits), as_tuples(oracle.find_all(rows, queries, 31)))
+
+
 def test_db_file_round_trip_and_scan(ctx, yp, oracle, tmp_path):
     """ypdq_db_load_file / ypdq_db_save_file: a flat row file, padded the reference's way to
     whole 2,048-row batches by repeating the last row, loads in chunks (a chunk size that

@@ -107,6 +107,42 @@ namespace {
 // records its own.
 int64_t jarosz_chunk(int64_t n) { return n < 2048 ? (n > 0 ? n : 1) : 2048; }
 
+// Chunk bounds for ypdq_screen_host. The copy of chunk c+1 (copy stream) runs while chunk c
+// is hashed and scanned (compute stream). The copies run back to back, so with u the copy
+// time and v the compute time per image, chunk c+1 arrives in time when its end S_{c+1}
+// (images counted from the start) satisfies S_{c+1} u <= S_1 u + S_c v, i.e.
+// S_{c+1} <= S_1 + (v / u) S_c: chunks grow geometrically by the compute/copy ratio, and
+// only the first chunk's copy is exposed. Chunks are whole multiples of 32 images (whole
+// 256-query scan passes); the first is 32 images unless more than `max_chunks` chunks would
+// be needed. When copying is the longer stage (ratio <= 1) the chunks are even and the last
+// chunk's compute is what remains exposed.
+int plan_screen_chunks(int64_t n, double ratio, int max_chunks, int64_t* bounds) {
+  const double r = std::min(2.0, std::max(1.0, ratio));
+  bounds[0] = 0;
+  if (n <= 0) return 0;
+  for (int64_t first = 32;; first *= 2) {
+    int nch = 0;
+    int64_t end = n < first + 32 ? n : first;
+    bounds[++nch] = end;
+    while (end < n && nch < max_chunks) {
+      int64_t next = std::max<int64_t>(end + 32, static_cast<int64_t>(first + r * end) / 32 * 32);
+      if (next + 32 > n) next = n;  // no remainder smaller than 32 images
+      end = next;
+      bounds[++nch] = end;
+    }
+    if (end == n) return nch;
+  }
+}
+
+// Estimated device time per image of ypdq_screen_host in microseconds on a GB300: the hash
+// (a few hundred ns; about 1 us with the Jarosz filter) plus 8 dihedral queries scanned
+// against n_rows rows at the tensor-core scan's rate for the threshold (11.5 T (row, query)
+// pairs/s with the 128-bit prefix bound, 9.5 T with the 192-bit one, 8.3 T with all 256 bits).
+double screen_us_per_image(bool jarosz, uint64_t n_rows, uint32_t threshold) {
+  const double pairs_per_us = threshold <= 36 ? 11.5e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
+  return (jarosz ? 1.1 : 0.18) + 8.0 * static_cast<double>(n_rows) / pairs_per_us;
+}
+
 ypdq_status ensure_jarosz_scratch(ypdq_ctx* ctx, int64_t chunk) {
   const size_t need = jarosz_scratch_bytes(chunk);
   if (ctx->jarosz_bytes >= need) return YPDQ_OK;
@@ -401,22 +437,14 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
   if ((st = scratch(ctx, 3, sizeof(ypdq_hit) * (capacity > 0 ? capacity : 1), &d_hits))) return st;
   if ((st = scratch(ctx, 4, 64, &d_cnt))) return st;
   CK(cudaMemsetAsync(d_cnt, 0, sizeof(uint64_t), s), "clear count");
-  // Chunks that grow from 32 images (one 256-query scan pass) by at most 1.5x, in whole
-  // multiples of 32 images (whole scan passes), up to 512: the copy of chunk c+1 (copy
-  // stream) overlaps the hash and scan of chunk c (compute stream), and with this growth
-  // the copy stays the shorter of the two (f32 images copy at ~5 us each over the host
-  // link, while hashing and scanning one takes ~8 us against 10M rows). Only the small
-  // first chunk's copy is exposed. Every chunk's scan appends to one hit list.
+  // Chunks whose copies (copy stream) overlap the hash and scan of the chunk before
+  // (compute stream); pinned host memory copies at ~200 GB/s. Every chunk's scan appends to
+  // one hit list.
   int64_t bounds[ypdq_ctx::kMaxChunks + 1];
-  int nch = 0;
-  bounds[0] = 0;
-  for (int64_t size = 32; bounds[nch] < n;) {
-    const int64_t rest = n - bounds[nch];
-    const int64_t take = (nch == ypdq_ctx::kMaxChunks - 1 || rest <= size + size / 2) ? rest : size;
-    bounds[nch + 1] = bounds[nch] + take;
-    ++nch;
-    size = std::min<int64_t>(512, (size * 3 / 2 + 31) / 32 * 32);
-  }
+  const double copy_us = static_cast<double>(img_bytes) / 2.0e5;
+  const double ratio =
+      screen_us_per_image(dct_precision == YPDQ_COMPRESS_JAROSZ, db->n_rows, threshold) / copy_us;
+  const int nch = plan_screen_chunks(n, 0.95 * ratio, ypdq_ctx::kMaxChunks, bounds);
   uint32_t rm, cm;
   semantics_masks(semantics, &rm, &cm);
   const bool jarosz = dct_precision == YPDQ_COMPRESS_JAROSZ;
