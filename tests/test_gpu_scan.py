@@ -46,12 +46,12 @@ def test_scan_thresholds_extremes(ctx, yp, oracle, algo):
 
 
 @pytest.mark.parametrize("algo", ALGOS)
-@pytest.mark.parametrize("n_q", [40, 100, 300])
+@pytest.mark.parametrize("n_q", [40, 100, 150, 300])
 def test_dense_hits_per_row(ctx, yp, oracle, algo, n_q):
     """Rows that hit every query of a pass: queries are variants of one hash within 6 bits,
     planted rows within 10 bits of it, so each planted row hits all n_q queries at t >= 16
-    (several hits per lane and column chunk in the tensor-core epilogue; 300 queries make a
-    wide pass plus a 44-query tail pass)."""
+    (several hits per lane and column chunk in the tensor-core epilogue; 150 queries run
+    one 192-query pass, 300 a 256-query pass plus a 44-query tail pass)."""
     rng = np.random.default_rng(n_q)
     base = yp.synth.rows_128(1, seed=77)[0]
     q = np.stack([yp.synth.flip_bits(base, int(rng.integers(0, 7)), rng) for _ in range(n_q)])
