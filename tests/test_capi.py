@@ -108,6 +108,40 @@ def test_server_config_default_and_argument_checks(yp):
     assert lib.ypdq_server_destroy(None) == yp._lib.ERR_INVALID
 
 
+def test_screen_chunk_plan(yp):
+    """ypdq_screen_plan (host-only): the chunks of ypdq_screen_host cover [0, n) in order,
+    are whole multiples of 32 images except the last, number at most 32, grow when hashing
+    and scanning an image takes longer than copying it, and are even when it does not."""
+    lib = yp._lib.load()
+    bounds = (ctypes.c_int64 * 33)()
+    k = ctypes.c_int()
+
+    def plan(n, kind, rows, t, dct=0):
+        assert lib.ypdq_screen_plan(n, kind, dct, rows, t, bounds, ctypes.byref(k)) == yp._lib.OK
+        return [bounds[i] for i in range(k.value + 1)]
+
+    cases = [(0, 10_000_000, 31), (1, 4_000_000, 31), (0, 60_000, 31), (0, 10_000_000, 64),
+             (3, 100_000_000, 48), (0, 0, 0)]
+    for n in (0, 1, 31, 32, 33, 63, 64, 65, 300, 1024, 4096, 100_000, 10_000_000):
+        for kind, rows, t in cases:
+            b = plan(n, kind, rows, t)
+            sizes = np.diff(b)
+            assert b[0] == 0 and b[-1] == n and (sizes > 0).all() and len(sizes) <= 32
+            assert (sizes[:-1] % 32 == 0).all()
+    # 1,024 f32 images against 10M rows at t = 31: ~7 us of hash and scan per image against
+    # ~5 us of copy, so the chunks grow from 32 images
+    sizes = np.diff(plan(1024, 0, 10_000_000, 31))
+    assert sizes[0] == 32 and (np.diff(sizes[:-1]) >= 0).all() and sizes.max() >= 128
+    # a small database: copying dominates, the chunks are even
+    sizes = np.diff(plan(1024, 0, 60_000, 31))
+    assert len(set(sizes[:-1].tolist())) == 1
+    # the Jarosz filter (dct_precision 0x200) makes compute longer: chunks grow at least as fast
+    assert len(plan(1024, 0, 2_000_000, 31, dct=0x200)) <= len(plan(1024, 0, 2_000_000, 31))
+    assert lib.ypdq_screen_plan(10, 9, 0, 1, 31, bounds, ctypes.byref(k)) == yp._lib.ERR_INVALID
+    assert lib.ypdq_screen_plan(-1, 0, 0, 1, 31, bounds, ctypes.byref(k)) == yp._lib.ERR_INVALID
+    assert lib.ypdq_screen_plan(10, 0, 0, 1, 31, None, ctypes.byref(k)) == yp._lib.ERR_INVALID
+
+
 LAYOUT_PROBE = r"""
 #include <stddef.h>
 #include <stdio.h>

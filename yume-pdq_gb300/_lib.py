@@ -98,6 +98,7 @@ SIGNATURES = {
     "ypdq_db_load_file": (i32, [P, ctypes.c_char_p, u64, PP]),
     "ypdq_db_save_file": (i32, [P, ctypes.c_char_p, u64]),
     "ypdq_screen_host": (i32, [P, P, P, i64, i32, i32, i32, u32, P, u64, P, P, P]),
+    "ypdq_screen_plan": (i32, [i64, i32, i32, u64, u32, P, ctypes.POINTER(ctypes.c_int)]),
     "ypdq_malloc_device": (i32, [P, sz, PP]),
     "ypdq_free_device": (i32, [P, P]),
     "ypdq_malloc_host": (i32, [P, sz, PP]),

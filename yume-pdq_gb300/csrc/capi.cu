@@ -143,6 +143,16 @@ double screen_us_per_image(bool jarosz, uint64_t n_rows, uint32_t threshold) {
   return (jarosz ? 1.1 : 0.18) + 8.0 * static_cast<double>(n_rows) / pairs_per_us;
 }
 
+// The chunk plan of ypdq_screen_host (and ypdq_screen_plan).
+int screen_chunks(int64_t n, size_t img_bytes, int dct_precision, uint64_t n_rows,
+                  uint32_t threshold, int64_t* bounds) {
+  // pinned host memory copies at ~200 GB/s
+  const double copy_us = static_cast<double>(img_bytes) / 2.0e5;
+  const double ratio =
+      screen_us_per_image(dct_precision == YPDQ_COMPRESS_JAROSZ, n_rows, threshold) / copy_us;
+  return plan_screen_chunks(n, 0.95 * ratio, ypdq_ctx::kMaxChunks, bounds);
+}
+
 ypdq_status ensure_jarosz_scratch(ypdq_ctx* ctx, int64_t chunk) {
   const size_t need = jarosz_scratch_bytes(chunk);
   if (ctx->jarosz_bytes >= need) return YPDQ_OK;
@@ -438,13 +448,9 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
   if ((st = scratch(ctx, 4, 64, &d_cnt))) return st;
   CK(cudaMemsetAsync(d_cnt, 0, sizeof(uint64_t), s), "clear count");
   // Chunks whose copies (copy stream) overlap the hash and scan of the chunk before
-  // (compute stream); pinned host memory copies at ~200 GB/s. Every chunk's scan appends to
-  // one hit list.
+  // (compute stream). Every chunk's scan appends to one hit list.
   int64_t bounds[ypdq_ctx::kMaxChunks + 1];
-  const double copy_us = static_cast<double>(img_bytes) / 2.0e5;
-  const double ratio =
-      screen_us_per_image(dct_precision == YPDQ_COMPRESS_JAROSZ, db->n_rows, threshold) / copy_us;
-  const int nch = plan_screen_chunks(n, 0.95 * ratio, ypdq_ctx::kMaxChunks, bounds);
+  const int nch = screen_chunks(n, img_bytes, dct_precision, db->n_rows, threshold, bounds);
   uint32_t rm, cm;
   semantics_masks(semantics, &rm, &cm);
   const bool jarosz = dct_precision == YPDQ_COMPRESS_JAROSZ;
@@ -511,6 +517,18 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
   *n_hits = total;
   if (total > capacity) return fail(YPDQ_ERR_OVERFLOW, "%llu hits > capacity %llu",
                                     (unsigned long long)total, (unsigned long long)capacity);
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_screen_plan(int64_t n, int input_kind, int dct_precision, uint64_t n_rows,
+                             uint32_t threshold, int64_t* bounds, int* n_chunks) {
+  static_assert(ypdq_ctx::kMaxChunks == YPDQ_MAX_SCREEN_CHUNKS, "chunk bound");
+  if (!bounds || !n_chunks) return fail(YPDQ_ERR_INVALID, "NULL argument");
+  if (n < 0) return fail(YPDQ_ERR_INVALID, "n out of range");
+  if (image_bytes_of(input_kind) == 0)
+    return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
+  *n_chunks = screen_chunks(n, image_bytes_of(input_kind), dct_precision, n_rows, threshold,
+                            bounds);
   return YPDQ_OK;
 }
 
