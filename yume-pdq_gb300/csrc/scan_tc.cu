@@ -12,8 +12,11 @@
 //   warps 0-7   epilogue: tcgen05.ld the 128 x N f16 accumulator, two warps per TMEM lane
 //               quarter (warp w reads lanes 32(w%4).. = tile rows; the two groups take
 //               alternate 64-column chunks, or with kDual and N = 64 alternate tiles),
-//               half2 max against the threshold, compact hits. One f16 is read per
-//               (row, query) pair, so the readout gets twice the warps of the other roles.
+//               hand the stage back, then a half2 max per 64 columns against the
+//               threshold; the rare chunk with a hit becomes a per-lane column mask whose
+//               hits are written with one atomic per warp. One f16 is read per (row, query)
+//               pair, so the readout gets twice the warps of the other roles (four per
+//               quarter were slower: the extra warps take issue slots from the expanders).
 //   warp 8      producer: one lane bulk-copies packed tiles (128 rows x 32 B) into a ring.
 //   warps 9, 14 MMA: one lane issues kKSteps tcgen05.mma (M=128, N, K=32) per tile into a
 //               double-buffered accumulator and commits to mbarriers (tcgen05.commit tracks
