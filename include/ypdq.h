@@ -237,10 +237,11 @@ ypdq_status ypdq_screen_host(ypdq_ctx *ctx, ypdq_db *db, const void *h_images, i
 /*
  * The chunks ypdq_screen_host cuts n images into (host-only; no device or context needed).
  * The copy of each chunk overlaps the hash and scan of the one before. Chunks grow from
- * 32 images by the estimated ratio of compute time (hash + scan of 8 queries against n_rows
- * rows at `threshold`) to copy time per image, in whole multiples of 32 images. They are
- * even when copying takes longer. Writes bounds[0] = 0 < bounds[1] < ... <
- * bounds[*n_chunks] = n (at most YPDQ_MAX_SCREEN_CHUNKS + 1 entries).
+ * 32 images, in whole multiples of 32, as fast as the copies stay ahead of the compute
+ * (estimated for a GB300 from the input kind, the hash kernel's fixed cost per chunk and
+ * the scan of 8 queries per image against n_rows rows at `threshold`). Writes
+ * bounds[0] = 0 < bounds[1] < ... < bounds[*n_chunks] = n (at most
+ * YPDQ_MAX_SCREEN_CHUNKS + 1 entries).
  */
 #define YPDQ_MAX_SCREEN_CHUNKS 32
 ypdq_status ypdq_screen_plan(int64_t n, int input_kind, int dct_precision, uint64_t n_rows,

@@ -110,8 +110,9 @@ def test_server_config_default_and_argument_checks(yp):
 
 def test_screen_chunk_plan(yp):
     """ypdq_screen_plan (host-only): the chunks of ypdq_screen_host cover [0, n) in order,
-    are whole multiples of 32 images except the last, number at most 32, grow when hashing
-    and scanning an image takes longer than copying it, and are even when it does not."""
+    are whole multiples of 32 images except the last and number at most 32. They grow
+    geometrically when hashing and scanning an image takes longer than copying it, and
+    slowly (by the hash kernel's fixed cost per chunk) when it does not."""
     lib = yp._lib.load()
     bounds = (ctypes.c_int64 * 33)()
     k = ctypes.c_int()
@@ -129,14 +130,17 @@ def test_screen_chunk_plan(yp):
             assert b[0] == 0 and b[-1] == n and (sizes > 0).all() and len(sizes) <= 32
             assert (sizes[:-1] % 32 == 0).all()
     # 1,024 f32 images against 10M rows at t = 31: ~7 us of hash and scan per image against
-    # ~5 us of copy, so the chunks grow from 32 images
+    # ~5 us of copy, so the chunks grow from 32 images to a few hundred
     sizes = np.diff(plan(1024, 0, 10_000_000, 31))
-    assert sizes[0] == 32 and (np.diff(sizes[:-1]) >= 0).all() and sizes.max() >= 128
-    # a small database: copying dominates, the chunks are even
-    sizes = np.diff(plan(1024, 0, 60_000, 31))
-    assert len(set(sizes[:-1].tolist())) == 1
-    # the Jarosz filter (dct_precision 0x200) makes compute longer: chunks grow at least as fast
-    assert len(plan(1024, 0, 2_000_000, 31, dct=0x200)) <= len(plan(1024, 0, 2_000_000, 31))
+    assert sizes[0] == 32 and (np.diff(sizes[:-1]) >= 0).all() and sizes.max() >= 256
+    assert 6 <= len(sizes) <= 12
+    # a small database: copying dominates and a chunk's compute is mostly the hash kernel's
+    # one round over its images, so chunks grow only by that fixed cost
+    small = np.diff(plan(1024, 0, 60_000, 31))
+    assert (np.diff(small[:-1]) >= 0).all() and len(small) > len(sizes) and small.max() <= 304
+    # the Jarosz filter (dct_precision 0x200) adds ~1 us of compute per image: where the scan
+    # dominates, its chunks grow at least as fast
+    assert len(plan(1024, 0, 10_000_000, 31, dct=0x200)) <= len(plan(1024, 0, 10_000_000, 31))
     assert lib.ypdq_screen_plan(10, 9, 0, 1, 31, bounds, ctypes.byref(k)) == yp._lib.ERR_INVALID
     assert lib.ypdq_screen_plan(-1, 0, 0, 1, 31, bounds, ctypes.byref(k)) == yp._lib.ERR_INVALID
     assert lib.ypdq_screen_plan(10, 0, 0, 1, 31, None, ctypes.byref(k)) == yp._lib.ERR_INVALID

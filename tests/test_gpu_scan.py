@@ -277,8 +277,8 @@ def test_screen_host_chunked(ctx, yp, oracle):
 
 def test_screen_host_growing_chunks(ctx, yp, oracle):
     """Against 4M rows a u8 image takes longer to hash and scan than to copy, so the chunks
-    of ypdq_screen_host grow geometrically from 32 images (the other screen tests run even
-    chunks); the hit list must equal the oracle's."""
+    of ypdq_screen_host grow geometrically from 32 images (32, 64, 160, 344; the other
+    screen tests run slowly growing chunks); the hit list must equal the oracle's."""
     imgs = yp.synth.to_u8(yp.synth.blob_images(600, seed=47))
     h, _, _, _ = oracle.hash_batch(imgs)
     queries = h.reshape(-1, 32)

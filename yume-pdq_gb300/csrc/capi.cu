@@ -109,15 +109,18 @@ int64_t jarosz_chunk(int64_t n) { return n < 2048 ? (n > 0 ? n : 1) : 2048; }
 
 // Chunk bounds for ypdq_screen_host. The copy of chunk c+1 (copy stream) runs while chunk c
 // is hashed and scanned (compute stream). The copies run back to back, so with u the copy
-// time and v the compute time per image, chunk c+1 arrives in time when its end S_{c+1}
-// (images counted from the start) satisfies S_{c+1} u <= S_1 u + S_c v, i.e.
-// S_{c+1} <= S_1 + (v / u) S_c: chunks grow geometrically by the compute/copy ratio, and
-// only the first chunk's copy is exposed. Chunks are whole multiples of 32 images (whole
+// time per image and v s + h the compute time of a chunk of s images, chunk c+1 arrives in
+// time when its end S_{c+1} (images counted from the start) satisfies
+// S_{c+1} u <= S_1 u + S_c v + c h, i.e. S_{c+1} <= S_1 + (v / u) S_c + c (h / u): chunks
+// grow geometrically by the compute/copy ratio, and only the first chunk's copy is exposed.
+// `ratio` is v / u and `chunk_images` h / u. Chunks are whole multiples of 32 images (whole
 // 256-query scan passes); the first is 32 images unless more than `max_chunks` chunks would
-// be needed. When copying is the longer stage (ratio <= 1) the chunks are even and the last
-// chunk's compute is what remains exposed.
-int plan_screen_chunks(int64_t n, double ratio, int max_chunks, int64_t* bounds) {
+// be needed. When copying is the longer stage (v / u <= 1) chunks still grow by h / u each,
+// since a chunk's fixed cost is then all its compute.
+int plan_screen_chunks(int64_t n, double ratio, double chunk_images, int max_chunks,
+                       int64_t* bounds) {
   const double r = std::min(2.0, std::max(1.0, ratio));
+  const double h = std::min(256.0, std::max(0.0, chunk_images));
   bounds[0] = 0;
   if (n <= 0) return 0;
   for (int64_t first = 32;; first *= 2) {
@@ -125,7 +128,8 @@ int plan_screen_chunks(int64_t n, double ratio, int max_chunks, int64_t* bounds)
     int64_t end = n < first + 32 ? n : first;
     bounds[++nch] = end;
     while (end < n && nch < max_chunks) {
-      int64_t next = std::max<int64_t>(end + 32, static_cast<int64_t>(first + r * end) / 32 * 32);
+      const double limit = static_cast<double>(first) + r * static_cast<double>(end) + nch * h;
+      int64_t next = std::max<int64_t>(end + 32, static_cast<int64_t>(limit) / 32 * 32);
       if (next + 32 > n) next = n;  // no remainder smaller than 32 images
       end = next;
       bounds[++nch] = end;
@@ -134,23 +138,34 @@ int plan_screen_chunks(int64_t n, double ratio, int max_chunks, int64_t* bounds)
   }
 }
 
-// Estimated device time per image of ypdq_screen_host in microseconds on a GB300: the hash
-// (a few hundred ns; about 1 us with the Jarosz filter) plus 8 dihedral queries scanned
-// against n_rows rows at the tensor-core scan's rate for the threshold (11.5 T (row, query)
-// pairs/s with the 128-bit prefix bound, 9.5 T with the 192-bit one, 8.3 T with all 256 bits).
-double screen_us_per_image(bool jarosz, uint64_t n_rows, uint32_t threshold) {
+// Estimated device time of one ypdq_screen_host chunk on a GB300 (152 SMs), in
+// microseconds: fixed_us + per_image_us x images.
+struct ChunkCost {
+  double fixed_us, per_image_us;
+};
+ChunkCost screen_chunk_cost(int input_kind, bool jarosz, uint64_t n_rows, uint32_t threshold) {
+  // the tensor-core scan: 11.5 T (row, query) pairs/s with the 128-bit prefix bound, 9.5 T
+  // with the 192-bit one, 8.3 T with all 256 bits; 8 queries per image
   const double pairs_per_us = threshold <= 36 ? 11.5e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
-  return (jarosz ? 1.1 : 0.18) + 8.0 * static_cast<double>(n_rows) / pairs_per_us;
+  const double scan_us = 8.0 * static_cast<double>(n_rows) / pairs_per_us;
+  // the Jarosz filter: four passes, each at least one line's sequential replay (512
+  // dependent steps, ~5 us) however few images the chunk holds, plus the DCT
+  if (jarosz) return {30.0, (input_kind == YPDQ_INPUT_U8 ? 0.95 : 1.1) + scan_us};
+  // hash_kernel runs one image per CTA, two CTAs per SM: a chunk of up to 304 images takes
+  // one image's time on a CTA, 304 x the per-image rate
+  const double hash_us = input_kind == YPDQ_INPUT_U8 ? 0.135 : input_kind == YPDQ_INPUT_F32 ? 0.18 : 0.28;
+  return {304.0 * hash_us, hash_us + scan_us};
 }
 
 // The chunk plan of ypdq_screen_host (and ypdq_screen_plan).
-int screen_chunks(int64_t n, size_t img_bytes, int dct_precision, uint64_t n_rows,
+int screen_chunks(int64_t n, int input_kind, int dct_precision, uint64_t n_rows,
                   uint32_t threshold, int64_t* bounds) {
   // pinned host memory copies at ~200 GB/s
-  const double copy_us = static_cast<double>(img_bytes) / 2.0e5;
-  const double ratio =
-      screen_us_per_image(dct_precision == YPDQ_COMPRESS_JAROSZ, n_rows, threshold) / copy_us;
-  return plan_screen_chunks(n, 0.95 * ratio, ypdq_ctx::kMaxChunks, bounds);
+  const double copy_us = static_cast<double>(image_bytes_of(input_kind)) / 2.0e5;
+  const ChunkCost cost =
+      screen_chunk_cost(input_kind, dct_precision == YPDQ_COMPRESS_JAROSZ, n_rows, threshold);
+  return plan_screen_chunks(n, 0.95 * cost.per_image_us / copy_us, 0.95 * cost.fixed_us / copy_us,
+                            ypdq_ctx::kMaxChunks, bounds);
 }
 
 ypdq_status ensure_jarosz_scratch(ypdq_ctx* ctx, int64_t chunk) {
@@ -450,7 +465,7 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
   // Chunks whose copies (copy stream) overlap the hash and scan of the chunk before
   // (compute stream). Every chunk's scan appends to one hit list.
   int64_t bounds[ypdq_ctx::kMaxChunks + 1];
-  const int nch = screen_chunks(n, img_bytes, dct_precision, db->n_rows, threshold, bounds);
+  const int nch = screen_chunks(n, input_kind, dct_precision, db->n_rows, threshold, bounds);
   uint32_t rm, cm;
   semantics_masks(semantics, &rm, &cm);
   const bool jarosz = dct_precision == YPDQ_COMPRESS_JAROSZ;
@@ -527,8 +542,7 @@ ypdq_status ypdq_screen_plan(int64_t n, int input_kind, int dct_precision, uint6
   if (n < 0) return fail(YPDQ_ERR_INVALID, "n out of range");
   if (image_bytes_of(input_kind) == 0)
     return fail(YPDQ_ERR_INVALID, "input_kind %d", input_kind);
-  *n_chunks = screen_chunks(n, image_bytes_of(input_kind), dct_precision, n_rows, threshold,
-                            bounds);
+  *n_chunks = screen_chunks(n, input_kind, dct_precision, n_rows, threshold, bounds);
   return YPDQ_OK;
 }
 
