@@ -459,13 +459,16 @@ def run_ours(args):
     for _ in range(max(1, args.warmup)):
         e2e_step()
     lat = []
+    if pg:
+        pg.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         s = time.perf_counter()
         e2e_step()
         lat.append(time.perf_counter() - s)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_value = world * B / e2e_s
+    # like the device-resident value: all ranks' images over the slowest rank's time
+    _, e2e_value = aggregate_over_ranks(pg, (time.perf_counter() - t0) * 1e3, world,
+                                        B * args.steps)
     ctx.lib.ypdq_free_host(ctx.handle, h_img)
     # the serving sweep, the heavy-hit database and the precision variants describe one GPU:
     # rank 0 runs them (the other replicas wait at the final barrier)
