@@ -564,7 +564,7 @@ def run_ours(args):
 def cpu_workload(args, sample):
     """Images and database rows for the CPU baseline: the same generators as the GPU arm
     (the database rows come from the CPU twin of the GPU row generator)."""
-    import oracle  # noqa: the checker, timed here as yume-pdq's CPU path
+    import oracle  # noqa: the oracle, timed here as yume-pdq's CPU path
     import __graft_entry__ as g
     yp = g.load_package()
     imgs = yp.synth.blob_images(sample, seed=args.seed)

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (``oracle/ypdq_oracle.c``).
 
 TEST INFRASTRUCTURE ONLY. The tests, ``__graft_entry__.smoke()`` and the CPU-baseline
-leg of ``bench.py`` use it as the checker. The product never imports it.
+leg of ``bench.py`` use it as the reference for results. The product never imports it.
 """
 import ctypes
 import os

@@ -2,7 +2,8 @@
  * ypdq_oracle.c -- CPU oracle for the yume-pdq hot path.
  *
  * TEST INFRASTRUCTURE ONLY. The tests and the CPU baseline of the benchmark load
- * this code as the checker. The product library never calls, links or executes it.
+ * this code as the reference for results. The product library never calls, links or
+ * executes it.
  *
  * It is a plain-C restatement of yume-pdq's scalar path. Citations point into the
  * yume-pdq sources:
