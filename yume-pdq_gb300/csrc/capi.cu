@@ -595,6 +595,7 @@ ypdq_status ypdq_memset(ypdq_ctx* ctx, void* d_ptr, int value, size_t bytes, ypd
 ypdq_status ypdq_stream_create(ypdq_ctx* ctx, ypdq_stream_t* out) {
   ypdq_status st = check_ctx(ctx);
   if (st) return st;
+  if (!out) return fail(YPDQ_ERR_INVALID, "out is NULL");
   cudaStream_t s;
   CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
   *out = reinterpret_cast<ypdq_stream_t>(s);
@@ -615,6 +616,7 @@ ypdq_status ypdq_stream_sync(ypdq_ctx* ctx, ypdq_stream_t stream) {
 ypdq_status ypdq_event_create(ypdq_ctx* ctx, ypdq_event_t* out) {
   ypdq_status st = check_ctx(ctx);
   if (st) return st;
+  if (!out) return fail(YPDQ_ERR_INVALID, "out is NULL");
   cudaEvent_t ev;
   CK(cudaEventCreate(&ev), "cudaEventCreate");
   *out = reinterpret_cast<ypdq_event_t>(ev);
@@ -636,6 +638,7 @@ ypdq_status ypdq_event_record(ypdq_ctx* ctx, ypdq_event_t ev, ypdq_stream_t stre
 ypdq_status ypdq_event_elapsed_ms(ypdq_ctx* ctx, ypdq_event_t a, ypdq_event_t b, float* ms) {
   ypdq_status st = check_ctx(ctx);
   if (st) return st;
+  if (!ms) return fail(YPDQ_ERR_INVALID, "ms is NULL");
   CK(cudaEventSynchronize(reinterpret_cast<cudaEvent_t>(b)), "cudaEventSynchronize");
   CK(cudaEventElapsedTime(ms, reinterpret_cast<cudaEvent_t>(a), reinterpret_cast<cudaEvent_t>(b)),
      "cudaEventElapsedTime");
