@@ -90,3 +90,39 @@ def test_row_sharded_scan_three_gloo_ranks():
         assert p.exitcode == 0
     assert ok
 
+
+
+def test_shard_rows_partition_and_merge():
+    """shard_rows tiles [0, n_rows) in rank order with slice sizes differing by at most one,
+    also with more ranks than rows; merge_shard_hits restores global indices in
+    (index, query) order and accepts empty shards."""
+    import sys
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import __graft_entry__ as g
+    yp = g.load_package()
+    for n_rows in (0, 1, 2, 7, 1000, 10_000_019):
+        for world in (1, 2, 3, 8):
+            parts = [yp.shard_rows(n_rows, world, r) for r in range(world)]
+            assert parts[0][0] == 0 and parts[-1][1] == n_rows
+            assert all(parts[r][1] == parts[r + 1][0] for r in range(world - 1))
+            sizes = [hi - lo for lo, hi in parts]
+            assert max(sizes) - min(sizes) <= 1
+    rng = np.random.default_rng(3)
+    full = np.zeros(50, yp.HIT_DTYPE)
+    full["index"] = np.sort(rng.choice(1000, 50, replace=False))
+    full["query"] = rng.integers(0, 9, 50)
+    full["distance"] = rng.integers(0, 32, 50)
+    full = full[np.lexsort((full["query"], full["index"]))]
+    shards = []
+    for lo, hi in [yp.shard_rows(1000, 4, r) for r in range(4)] + [(1000, 1000)]:
+        local = full[(full["index"] >= lo) & (full["index"] < hi)].copy()
+        local["index"] -= np.uint64(lo)
+        shards.append((local[::-1], lo))  # any order within a shard
+    merged = yp.merge_shard_hits(shards)
+    assert np.array_equal(merged, full)
+    try:
+        yp.shard_rows(10, 2, 2)
+        raise AssertionError("rank out of range accepted")
+    except ValueError:
+        pass
