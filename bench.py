@@ -58,7 +58,31 @@ def parse():
                     help="1: report the 1/8/64/256/1024-query scan sweep (0 skips the section)")
     ap.add_argument("--dct-variants", type=int, default=1,
                     help="1: time and check the FP32 / TF32 / BF16x3 hash variants")
+    ap.add_argument("--peaks", action="store_true",
+                    help="only measure the dense FP8 burst of GPU 0 and print it as JSON")
+    ap.add_argument("--ranks-only", action="store_true",
+                    help="only join the replicas' process group and print this rank's view "
+                         "(tests the multi-process launch without a GPU)")
     return ap.parse_args()
+
+
+def launch_replicas(argv, n):
+    """`bench.py --gpus N` started outside torchrun: run N replica processes of this script,
+    one per GPU (RANK = LOCAL_RANK = i, WORLD_SIZE = N, rendezvous on 127.0.0.1 at a free
+    port), as torchrun would. Returns the first non-zero exit status, else 0. Rank 0 prints
+    the JSON line."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n),
+                   LOCAL_WORLD_SIZE=str(n), MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__)] + list(argv),
+                                      env=env))
+    rcs = [p.wait() for p in procs]
+    return next((rc for rc in rcs if rc), 0)
 
 
 def aggregate_over_ranks(pg, local_ms, world, images_per_rank):
@@ -143,6 +167,39 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+def fp8_dense_burst(device=0, n=8192, reps=10):
+    """Dense FP8 (e4m3) tensor-core rate of this GPU in TFLOP/s: torch._scaled_mm of two
+    n x n e4m3 matrices (per-tensor unit scales, bf16 out), best of `reps` launches timed
+    with CUDA events on torch's stream, 2 n^3 FLOP each. The method of the bf16 burst in
+    MEASURED_PEAKS.json with the FP8 operand type. None if torch or FP8 GEMMs are absent."""
+    try:
+        import torch
+        dev = torch.device("cuda", device)
+        a = torch.randn(n, n, device=dev).to(torch.float8_e4m3fn)
+        b = torch.randn(n, n, device=dev).to(torch.float8_e4m3fn).t()  # column-major
+        one = torch.ones((), device=dev)
+
+        def mm():
+            return torch._scaled_mm(a, b, one, one, out_dtype=torch.bfloat16)
+
+        for _ in range(3):
+            mm()
+        best = float("inf")
+        for _ in range(reps):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            mm()
+            e.record()
+            e.synchronize()
+            best = min(best, s.elapsed_time(e))
+        del a, b
+        torch.cuda.empty_cache()
+        return 2.0 * n ** 3 / (best / 1e3) / 1e12
+    except Exception as exc:  # reported, never silently replaced by a guess
+        sys.stderr.write("fp8 burst not measured: %s\n" % exc)
+        return None
+
+
 def scan_algo_used(algo, nq, threshold):
     """The algorithm ypdq_scan runs for YPDQ_SCAN_AUTO (mirrors auto_scan_algo in scan.cu)."""
     if algo == 0:
@@ -153,7 +210,10 @@ def scan_algo_used(algo, nq, threshold):
 
 
 def setup_workload(yp, ctx, args, rank):
-    """Images on the device, database on the device with planted near-duplicates."""
+    """Images on the device and the database with its planted near-duplicates, on the device
+    and (for the CPU baseline and the parity check) on the host. The rows are
+    ypdq_synth_rows(seed); args.planted of them become copies of the step's dihedral hashes
+    at distances 0..31 (synth.plant_near_duplicates, the same edit the CPU arm makes)."""
     batch = yp.synth.blob_images(args.batch, seed=args.seed + 1000 * rank)
     d_img = ctx.to_device(batch)
     n = args.db_rows
@@ -164,15 +224,10 @@ def setup_workload(yp, ctx, args, rank):
     yp.core.hash_batch_device(ctx, d_img, args.batch, yp._lib.INPUT_F32, d_hash, d_q)
     ctx.sync()
     queries = d_hash.download((args.batch * 8, 32), np.uint8)
-    # plant near-duplicates: overwrite rows at random positions (small scatter via host rows)
-    prng = np.random.default_rng(args.seed + 99)
-    pos = np.sort(prng.choice(n, size=min(args.planted, n), replace=False))
-    qid = prng.integers(0, len(queries), size=len(pos))
-    dist = prng.integers(0, 32, size=len(pos))
-    for p, q, d in zip(pos, qid, dist):
-        row = yp.synth.flip_bits(queries[q], int(d), prng)
-        d_rows.upload(row, offset=int(p) * 32)
-    return batch, d_img, d_rows, d_hash, d_q
+    rows = d_rows.download((n, 32), np.uint8)
+    yp.synth.plant_near_duplicates(rows, queries, args.planted, args.seed + 99)
+    d_rows.upload(rows)
+    return batch, d_img, rows, d_rows, d_hash, d_q
 
 
 def serve_run(yp, srv, pool, rate, seconds, rng, hit_cap=4096):
@@ -385,17 +440,25 @@ def dct_variants(yp, ctx, args, n_distinct=512, n_launch=4096):
     return out
 
 
-def run_ours(args):
-    import __graft_entry__ as g
-    yp = g.load_package()
+def join_ranks(args):
+    """(rank, world, local rank, process group or None); the world must be --gpus."""
     rank, world, local = dist_info()
+    if world != args.gpus:
+        raise SystemExit("bench.py: %d ranks running for --gpus %d" % (world, args.gpus))
     pg = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
         pg = dist
+    return rank, world, local, pg
+
+
+def run_ours(args):
+    import __graft_entry__ as g
+    yp = g.load_package()
+    rank, world, local, pg = join_ranks(args)
     ctx = yp.Context(local)
-    batch, d_img, d_rows, d_hash, d_q = setup_workload(yp, ctx, args, rank)
+    batch, d_img, rows, d_rows, d_hash, d_q = setup_workload(yp, ctx, args, rank)
     n, B = args.db_rows, args.batch
     nq = 8 * B
     cap = 1 << 22
@@ -441,6 +504,11 @@ def run_ours(args):
     clk = clocks.stop()
     total_ms, value = aggregate_over_ranks(pg, total_ms, world, B * args.steps)
     ms_per_step = total_ms / args.steps
+    # the last timed step's hits in the scalar matcher's order, for the parity check
+    step_hits = int(d_cnt.download((1,), np.uint64)[0])
+    yp.core.sort_hits_device(ctx, d_hits, min(step_hits, cap), stream)
+    ctx.sync(stream)
+    gpu_step_hits = d_hits.download((min(step_hits, cap),), yp.HIT_DTYPE)
 
     # end to end through the public C ABI from pinned host memory
     db = yp.Database(ctx, device_buffer=d_rows, n_rows=n)
@@ -469,6 +537,7 @@ def run_ours(args):
     # like the device-resident value: all ranks' images over the slowest rank's time
     _, e2e_value = aggregate_over_ranks(pg, (time.perf_counter() - t0) * 1e3, world,
                                         B * args.steps)
+    e2e_hits = h_hits[:min(nh.value, len(h_hits))].copy()
     ctx.lib.ypdq_free_host(ctx.handle, h_img)
     # the serving sweep, the heavy-hit database and the precision variants describe one GPU:
     # rank 0 runs them (the other replicas wait at the final barrier)
@@ -485,25 +554,30 @@ def run_ours(args):
     if scan_avg >= hash_avg and algo == 3:
         # tensor-core scan, one launch per step: FP8 flops the MMAs execute per (row, query)
         # pair, 2 * K: K = 128 at t <= 36 and 192 for passes of 256 queries at t <= 62 (the
-        # prefix bound; mirrors launch_scan_tc), else 256; FP8 dense peak taken as 2x the
-        # measured bf16 dense burst (the nominal 4.5 : 2.25 ratio)
+        # prefix bound; mirrors launch_scan_tc), else 256. Peak: the dense FP8 burst measured
+        # on this GPU in this run (else twice the measured bf16 burst, the nominal ratio).
         k_bits = (128 if args.threshold <= 36 else
                   192 if (nq > 128 and args.threshold <= 62) else 256)
         flops = 2.0 * k_bits * nq * n
         achieved = flops / (scan_avg / 1000.0) / 1e12
-        # DRAM traffic: 320.5 MB per query pass of 256 (ncu capture of the 10M-row scan at
-        # 2,048 queries, profiles/scan_tc_10M_rows_2048_queries.md), scaled by passes and rows
+        fp8 = fp8_dense_burst(local) if rank == 0 else None
+        peak = fp8 if fp8 else 2 * bf16_peak
         passes = (nq + 255) // 256
-        traffic = passes * 320.5e6 * (n / 10_000_000)
         roofline = {"bound": "tensor", "kernel": "scan_tc_kernel (tcgen05 kind::f8f6f4)",
-                    "achieved": achieved, "peak": 2 * bf16_peak, "unit": "TFLOP/s",
-                    "frac": achieved / (2 * bf16_peak), "traffic": traffic,
-                    "traffic_unit": "bytes per launch (scaled from an ncu capture)",
-                    "peak_source": "%s bf16 burst x 2 (fp8 dense)" % peak_kind,
+                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak,
+                    "peak_source": ("measured fp8 burst (torch._scaled_mm e4m3 8192^3, best of "
+                                    "10, this GPU, this run)" if fp8 else
+                                    "%s bf16 burst x 2 (fp8 dense)" % peak_kind),
+                    "traffic": None,
+                    "traffic_computed": passes * 32.0 * n + hits_per_step * 16.0,
+                    "traffic_note": "traffic_computed = 32 B x rows x query passes of 256 + "
+                                    "16 B per hit (the database streams once per pass), "
+                                    "computed, not a counter",
                     "launch_ms": scan_avg, "launches_per_step": 1,
                     "mma_k_bits": k_bits,
                     "pairs_per_s": nq * n / (scan_avg / 1e3),
-                    "db_stream_gbs": (n * 32 * ((nq + 255) // 256)) / (scan_avg / 1e3) / 1e9}
+                    "db_stream_gbs": (n * 32 * passes) / (scan_avg / 1e3) / 1e9}
     elif scan_avg >= hash_avg:
         # SIMT scan: one launch reads the whole database once for up to 2048 queries
         dom_ms = scan_avg / scan_launches
@@ -554,7 +628,9 @@ def run_ours(args):
         "clocks": clk,
     }
     if rank == 0:
-        out["cpu_baseline"] = cpu_baseline(args, sample=args.cpu_sample)
+        out["cpu_baseline"] = cpu_baseline(args, args.cpu_sample,
+                                           workload=(batch[:args.cpu_sample], rows))
+        out["parity"] = parity_check(args, batch, rows, gpu_step_hits, step_hits, e2e_hits)
         print(json.dumps(out))
     if pg:
         pg.barrier()
@@ -562,14 +638,43 @@ def run_ours(args):
 
 
 def cpu_workload(args, sample):
-    """Images and database rows for the CPU baseline: the same generators as the GPU arm
-    (the database rows come from the CPU twin of the GPU row generator)."""
+    """Images and database of the CPU arm: the GPU arm's generators and its planted rows.
+    The rows come from the CPU twin of ypdq_synth_rows; the step's args.batch images are
+    hashed by the oracle (bit-identical to the GPU's hashes) and args.planted rows become
+    copies of those hashes (synth.plant_near_duplicates, the GPU arm's edit). Returns the
+    first `sample` images and the rows."""
     import oracle  # noqa: the oracle, timed here as yume-pdq's CPU path
     import __graft_entry__ as g
     yp = g.load_package()
-    imgs = yp.synth.blob_images(sample, seed=args.seed)
+    imgs = yp.synth.blob_images(args.batch, seed=args.seed)
     rows = oracle.synth_rows(args.db_rows, args.seed, nthreads=os.cpu_count() or 1)
-    return imgs, rows
+    hashes, _, _, _ = oracle.hash_batch(imgs)
+    yp.synth.plant_near_duplicates(rows, hashes, args.planted, args.seed + 99)
+    return imgs[:sample], rows
+
+
+def parity_check(args, imgs, rows, gpu_hits, gpu_count, e2e_hits):
+    """The timed step against the oracle, once, after the timed regions: the oracle hashes
+    the step's images (its f32 pipeline) and its scalar matcher lists every hit of the 8B
+    hashes in the same planted rows. Equal when the GPU step's sorted hit list and the last
+    ypdq_screen_host call's are both that list."""
+    import oracle
+    import __graft_entry__ as g
+    yp = g.load_package()
+    t0 = time.perf_counter()
+    hashes, _, _, _ = oracle.hash_batch(imgs)
+    want = oracle.find_all(rows, hashes.reshape(-1, 32), args.threshold)
+
+    def same(h):
+        return (len(h) == len(want) and all(np.array_equal(h[f], want[f])
+                                            for f in ("index", "query", "distance")))
+    return {"gpu_hits": int(gpu_count), "oracle_hits": int(len(want)),
+            "equal": bool(gpu_count == len(want) and same(gpu_hits)),
+            "e2e_equal": bool(same(e2e_hits)),
+            "oracle_s": round(time.perf_counter() - t0, 2),
+            "what": "sorted (index, query, distance) lists of the timed step and of the last "
+                    "ypdq_screen_host call vs the oracle's scalar matcher over all %d x %d pairs "
+                    "of the same planted rows" % (8 * len(imgs), rows.shape[0])}
 
 
 def cpu_time(args, imgs, rows):
@@ -600,14 +705,26 @@ def published_rate_estimate(n_images, db_rows, cores):
     return n_images / (scan_s + hash_s)
 
 
+def host_cpu():
+    """'<vendor> <model name>' of this host's CPU from lscpu (None if unavailable)."""
+    try:
+        info = dict(line.split(":", 1) for line in subprocess.run(
+            ["lscpu"], capture_output=True, text=True, timeout=10).stdout.splitlines()
+            if ":" in line)
+        return " ".join(info[k].strip() for k in ("Vendor ID", "Model name") if k in info) or None
+    except (OSError, subprocess.SubprocessError, ValueError):
+        return None
+
+
 def cpu_baseline(args, sample, workload=None, reps=1):
     imgs, rows = workload or cpu_workload(args, sample)
     cores = os.cpu_count() or 1
     times = [cpu_time(args, imgs, rows) for _ in range(reps)]
     tot, th, ts = min(times)
     return {"value": len(imgs) / tot, "unit": UNIT, "cores": cores, "kind": "port",
+            "cpu": host_cpu(),
             "sample": "%d images hashed (+7 dihedrals each) and %d hashes scanned vs %d rows "
-                      "at t=%d; hash %.3f s, scan %.3f s"
+                      "(the planted database of the GPU step) at t=%d; hash %.3f s, scan %.3f s"
                       % (len(imgs), 8 * len(imgs), args.db_rows, args.threshold, th, ts),
             "published_rate_upper_bound": {
                 "value": published_rate_estimate(len(imgs), args.db_rows, cores), "unit": UNIT,
@@ -643,6 +760,20 @@ def run_reference(args):
 def main():
     args = parse()
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    if args.peaks:
+        print(json.dumps({"fp8_e4m3_dense_tflops": fp8_dense_burst(),
+                          "how": "torch._scaled_mm e4m3 8192^3, unit scales, bf16 out, best of "
+                                 "10, CUDA events"}))
+        return
+    if args.impl == "ours" and args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_replicas(sys.argv[1:], args.gpus))
+    if args.ranks_only:
+        rank, world, local, pg = join_ranks(args)
+        t, v = aggregate_over_ranks(pg, float(rank + 1), world, 1)
+        print(json.dumps({"rank": rank, "world": world, "local_rank": local, "max_ms": t}))
+        if pg:
+            pg.destroy_process_group()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

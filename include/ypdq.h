@@ -408,6 +408,15 @@ ypdq_status ypdq_synth_clustered_rows(ypdq_ctx *ctx, uint8_t *d_rows, uint64_t n
                                       uint64_t first_row, uint64_t members_per_centre,
                                       uint32_t flip_trials, uint64_t seed, ypdq_stream_t stream);
 
+/*
+ * The dihedral sign convention (ypdq_dihedral_semantics) that the drop-in symbols of
+ * yume_pdq.h use: what yume-pdq's smart_kernel() computes on this host in its default build
+ * (src/kernel/mod.rs:79-176), i.e. AVX2 on an x86_64 CPU with AVX2 and FMA, SCALAR on any
+ * other host, unless the environment variable YUME_PDQ_DIHEDRAL_SEMANTICS (exact | avx2 |
+ * scalar) overrides it. Read once per process. Host-only; needs no device.
+ */
+ypdq_status ypdq_dropin_semantics(int *semantics);
+
 /* The f32 DCT matrix (16 x 127) and tent weights (7 x 7) compiled into the library. */
 ypdq_status ypdq_constants(float *h_dct16x127, float *h_tent7x7);
 

@@ -16,6 +16,15 @@
  * creates. Calls are synchronous and thread-safe, like the reference's. The reference
  * returns no error for these symbols, so a CUDA failure here prints a message to stderr
  * and returns quality -1.0f (hash) or false (visit).
+ *
+ * Dihedral signs. yume-pdq's CPU kernels derive ROTATED_180, FLIPPED and three transposed
+ * variants with different sign patterns, and smart_kernel() picks the kernel by host
+ * (src/kernel/mod.rs:79-176): Avx2F32Kernel on x86_64 with AVX2 and FMA, the trait-default
+ * DefaultKernel elsewhere (an aarch64 host, for one). The visit symbol follows the same
+ * choice, so it returns what the replaced library returns on the same host. The
+ * environment variable YUME_PDQ_DIHEDRAL_SEMANTICS = exact | avx2 | scalar overrides it
+ * (exact is Avx512F32Kernel's pattern, the sign pattern of a true flip); the batched API in
+ * ypdq.h takes the convention as an argument and ypdq_dropin_semantics() reports this one.
  */
 #ifndef YUME_PDQ_GB300_DROPIN_H
 #define YUME_PDQ_GB300_DROPIN_H

@@ -416,26 +416,50 @@ typedef struct {
   int64_t* caps;
 } find_ctx;
 
+static void push_hit(ypdqo_hit** buf, int64_t* cnt, int64_t* cap, int64_t r, int q,
+                     uint32_t d) {
+  if (*cnt == *cap) {
+    *cap *= 2;
+    *buf = (ypdqo_hit*)realloc(*buf, *cap * sizeof(ypdqo_hit));
+  }
+  (*buf)[*cnt].index = (uint64_t)r;
+  (*buf)[*cnt].query = (uint32_t)q;
+  (*buf)[*cnt].distance = d;
+  (*cnt)++;
+}
+
+/* The scalar matcher's loop (src/matching/mod.rs:336-362): rows in order, each row loaded
+ * once and compared with the needles in order, 8 at a time without branches; the rare
+ * block holding a hit is then visited needle by needle, so hits come out in (row, needle)
+ * order. */
 static void find_range(void* vctx, int64_t b, int64_t e) {
   find_ctx* c = (find_ctx*)vctx;
+  const int full = c->n_needles / 8 * 8;
+  const uint32_t t_max = c->threshold;
   for (int64_t t = b; t < e; t++) {
     int64_t r0 = c->n_rows * t / c->nthreads, r1 = c->n_rows * (t + 1) / c->nthreads;
     int64_t cnt = 0, cap = 64;
     ypdqo_hit* buf = (ypdqo_hit*)malloc(cap * sizeof(ypdqo_hit));
     for (int64_t r = r0; r < r1; r++) {
       const uint64_t* row = c->db + r * 4;
-      for (int q = 0; q < c->n_needles; q++) {
-        uint32_t d = dist256(row, c->needles + q * 4);
-        if (d <= c->threshold) {
-          if (cnt == cap) {
-            cap *= 2;
-            buf = (ypdqo_hit*)realloc(buf, cap * sizeof(ypdqo_hit));
-          }
-          buf[cnt].index = (uint64_t)r;
-          buf[cnt].query = (uint32_t)q;
-          buf[cnt].distance = d;
-          cnt++;
+      const uint64_t a0 = row[0], a1 = row[1], a2 = row[2], a3 = row[3];
+      for (int q = 0; q < full; q += 8) {
+        const uint64_t* n = c->needles + q * 4;
+        uint32_t d[8], any = 0;
+        for (int k = 0; k < 8; k++) {
+          d[k] = (uint32_t)(__builtin_popcountll(a0 ^ n[4 * k]) +
+                            __builtin_popcountll(a1 ^ n[4 * k + 1]) +
+                            __builtin_popcountll(a2 ^ n[4 * k + 2]) +
+                            __builtin_popcountll(a3 ^ n[4 * k + 3]));
+          any |= (uint32_t)(d[k] <= t_max) << k;
         }
+        if (any)
+          for (int k = 0; k < 8; k++)
+            if ((any >> k) & 1u) push_hit(&buf, &cnt, &cap, r, q + k, d[k]);
+      }
+      for (int q = full; q < c->n_needles; q++) {
+        const uint32_t d = dist256(row, c->needles + q * 4);
+        if (d <= t_max) push_hit(&buf, &cnt, &cap, r, q, d);
       }
     }
     c->bufs[t] = buf;

@@ -191,3 +191,46 @@ def test_struct_layouts_match_header(yp, tmp_path):
             assert ctypes.sizeof(mirrors[t]) == v, t
         else:
             assert getattr(mirrors[t], m).offset == v, (t, m)
+
+
+def _host_dropin_semantics():
+    """What yume-pdq's smart_kernel() computes on this host in its default build
+    (src/kernel/mod.rs:79-176): Avx2F32Kernel's signs on x86_64 with AVX2 and FMA, the
+    trait default elsewhere."""
+    import platform
+    flags = set()
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.startswith("flags"):
+                flags |= set(line.split(":", 1)[1].split())
+    except OSError:
+        pass
+    if platform.machine() in ("x86_64", "AMD64") and {"avx2", "fma"} <= flags:
+        return 1  # YPDQ_DIHEDRAL_AVX2
+    return 2      # YPDQ_DIHEDRAL_SCALAR
+
+
+def _dropin_semantics_in_child(env_value):
+    import subprocess
+    import sys
+    code = ("import sys, ctypes; sys.path.insert(0, %r); import __graft_entry__ as g; "
+            "yp = g.load_package(); s = ctypes.c_int(-1); "
+            "assert yp._lib.load().ypdq_dropin_semantics(ctypes.byref(s)) == 0; print(s.value)"
+            % ROOT)
+    env = dict(os.environ)
+    env.pop("YUME_PDQ_DIHEDRAL_SEMANTICS", None)
+    if env_value is not None:
+        env["YUME_PDQ_DIHEDRAL_SEMANTICS"] = env_value
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    return int(r.stdout.strip())
+
+
+def test_dropin_semantics_default_follows_host():
+    """The drop-in symbols derive dihedrals with the sign convention the replaced library
+    uses on the same host, and the environment variable overrides it."""
+    assert _dropin_semantics_in_child(None) == _host_dropin_semantics()
+    for name, want in (("exact", 0), ("avx2", 1), ("scalar", 2)):
+        assert _dropin_semantics_in_child(name) == want
+    assert _dropin_semantics_in_child("bogus") == _host_dropin_semantics()

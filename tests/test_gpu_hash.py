@@ -177,10 +177,15 @@ def test_dropin_hash_symbol(yp, oracle):
 
 
 def test_dropin_visit_symbol(yp, oracle):
+    """yume_pdq_visit_dihedrals_smart_kernel derives the dihedrals with the sign convention
+    of the kernel the reference's smart_kernel() picks on this host (the trait default on an
+    aarch64 host, Avx2F32Kernel's on x86_64 with AVX2 and FMA)."""
     lib = yp._lib.load()
+    sem = ctypes.c_int(-1)
+    assert lib.ypdq_dropin_semantics(ctypes.byref(sem)) == 0
     img = yp.synth.blob_images(1, seed=56)[0]
     h0, t0, q0, b0, p0 = oracle.hash_get_threshold(img)
-    dh, dt, dq, dp = oracle.dihedrals(p0, t0, "exact")
+    dh, dt, dq, dp = oracle.dihedrals(p0, t0, ["exact", "avx2", "scalar"][sem.value])
     out = np.zeros(32, np.uint8)
     pdqf = p0.copy()
     calls = []

@@ -39,7 +39,8 @@ def test_luma8_stream_all_dihedrals(yp, oracle):
     pipe = load_pipe()
     frames = yp.synth.to_u8(yp.synth.blob_images(3, seed=501))
     out = run(["-f", "q+hex+lf", "--dihedrals", "--batch", "2"], frames.tobytes())
-    h, q, t, _ = oracle.hash_batch(frames)
+    # the CLI's default: the sign convention of the reference's smart_kernel on this host
+    h, q, t, _ = oracle.hash_batch(frames, semantics=yp.kernel.host_semantics())
     assert out == expected(pipe, h, q, "q+hex+lf", 8)
     assert out.count(b"\n") == 24
 
@@ -72,7 +73,7 @@ def test_partial_frame_is_an_error(yp):
 def test_screening_stream_with_database(yp, oracle, tmp_path):
     pipe = load_pipe()
     frames = yp.synth.to_u8(yp.synth.blob_images(5, seed=503))
-    h, q, t, _ = oracle.hash_batch(frames)
+    h, q, t, _ = oracle.hash_batch(frames, semantics=yp.kernel.host_semantics())
     rows = yp.synth.rows_128(50_000, seed=504)
     yp.synth.plant(rows, h.reshape(-1, 32), 300, 0, 31, seed=505)
     db = tmp_path / "db.bin"

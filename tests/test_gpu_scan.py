@@ -322,3 +322,25 @@ def test_db_file_round_trip_and_scan(ctx, yp, oracle, tmp_path):
         yp.Database.from_file(ctx, bad)
     with pytest.raises(yp.YpdqError):
         yp.Database.from_file(ctx, tmp_path / "missing.bin")
+
+
+@pytest.mark.parametrize("n_q", [257, 300, 511, 512, 513, 1025])
+def test_pair_kernel_matches_oracle(ctx, yp, oracle, n_q):
+    """More than 256 queries at t <= 36 run passes of 512 queries, two per f32 accumulator
+    column (the second scaled by 512). Odd counts leave a pair with one query; rows equal or
+    complementary to a query on the 128-bit prefix put d = +-128 in either half of a column;
+    thresholds cover 0..36 at one size and the range's edges at the others."""
+    rows = yp.synth.rows_128(6000, seed=n_q)
+    q = yp.synth.rows_128(n_q, seed=n_q + 1)
+    yp.synth.plant(rows, q, 300, 0, 40, seed=3)
+    rows[10], rows[11] = q[0], ~q[1]
+    rows[12], rows[13] = q[n_q - 1], ~q[n_q - 1]
+    rows[14, :16], rows[14, 16:] = q[2, :16], ~q[2, 16:]   # prefix equal, distance 128
+    rows[15, :16], rows[15, 16:] = ~q[3, :16], q[3, 16:]   # prefix complement, distance 128
+    rows[16] = q[n_q - 2]
+    ts = range(37) if n_q == 513 else (0, 1, 16, 31, 35, 36)
+    for t in ts:
+        want = oracle.find_all(rows, q, t)
+        for algo in (3, 0):  # YPDQ_SCAN_TC, YPDQ_SCAN_AUTO
+            got = yp.scan(ctx, rows, q, t, algo=algo)
+            assert np.array_equal(as_tuples(got), as_tuples(want)), (t, algo, len(got), len(want))

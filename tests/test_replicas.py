@@ -126,3 +126,29 @@ def test_shard_rows_partition_and_merge():
         raise AssertionError("rank out of range accepted")
     except ValueError:
         pass
+
+
+def test_bench_gpus_flag_starts_n_ranks():
+    """`bench.py --gpus 2` outside torchrun starts two replica processes that join one gloo
+    group (world 2, local ranks 0 and 1) and agree on the slowest rank's time."""
+    import json
+    import subprocess
+    import sys
+    env = {k: v for k, v in os.environ.items()
+           if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT")}
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2",
+                        "--ranks-only"], capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert sorted((d["rank"], d["local_rank"]) for d in lines) == [(0, 0), (1, 1)]
+    assert all(d["world"] == 2 and d["max_ms"] == 2.0 for d in lines)
+
+
+def test_bench_rejects_rank_count_mismatch():
+    """A run whose WORLD_SIZE differs from --gpus fails instead of reporting the wrong N."""
+    import subprocess
+    import sys
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2",
+                        "--ranks-only"], capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode != 0 and "--gpus 2" in r.stderr

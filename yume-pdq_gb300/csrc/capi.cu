@@ -696,17 +696,35 @@ __attribute__((visibility("default"))) const YumePDQ_Dihedrals YUME_PDQ_DIHEDRAL
 
 namespace {
 
-std::once_flag g_dropin_once;
+std::once_flag g_dropin_once, g_dropin_sem_once;
 ypdq_ctx* g_dropin_ctx = nullptr;
-int g_dropin_semantics = YPDQ_DIHEDRAL_EXACT;
+int g_dropin_semantics = YPDQ_DIHEDRAL_SCALAR;
 
-// The drop-in symbols use one library-owned context on device 0. The dihedral sign
-// convention comes from YUME_PDQ_DIHEDRAL_SEMANTICS = exact | avx2 | scalar (default exact).
+// The dihedral sign convention of the drop-in symbols: the one yume-pdq's smart_kernel()
+// computes on this host (src/kernel/mod.rs:79-176) in its default build (without the
+// non-default `avx512` feature). On x86_64 with AVX2 and FMA that is Avx2F32Kernel (the
+// router's runtime check); on any other host the trait-default DefaultKernel. The
+// environment variable YUME_PDQ_DIHEDRAL_SEMANTICS = exact | avx2 | scalar overrides it
+// (exact = Avx512F32Kernel, what a build with `avx512` computes on an AVX-512 host).
+int dropin_semantics() {
+  std::call_once(g_dropin_sem_once, [] {
+    int sem = YPDQ_DIHEDRAL_SCALAR;
+#if defined(__x86_64__)
+    if (__builtin_cpu_supports("avx2") && __builtin_cpu_supports("fma")) sem = YPDQ_DIHEDRAL_AVX2;
+#endif
+    const char* env = getenv("YUME_PDQ_DIHEDRAL_SEMANTICS");
+    if (env && !strcmp(env, "exact")) sem = YPDQ_DIHEDRAL_EXACT;
+    if (env && !strcmp(env, "avx2")) sem = YPDQ_DIHEDRAL_AVX2;
+    if (env && !strcmp(env, "scalar")) sem = YPDQ_DIHEDRAL_SCALAR;
+    g_dropin_semantics = sem;
+  });
+  return g_dropin_semantics;
+}
+
+// The drop-in symbols use one library-owned context on device 0.
 ypdq_ctx* dropin_ctx() {
+  dropin_semantics();
   std::call_once(g_dropin_once, [] {
-    const char* sem = getenv("YUME_PDQ_DIHEDRAL_SEMANTICS");
-    if (sem && !strcmp(sem, "avx2")) g_dropin_semantics = YPDQ_DIHEDRAL_AVX2;
-    if (sem && !strcmp(sem, "scalar")) g_dropin_semantics = YPDQ_DIHEDRAL_SCALAR;
     ypdq_ctx* c = nullptr;
     if (ypdq_ctx_create(0, &c) == YPDQ_OK) g_dropin_ctx = c;
     else fprintf(stderr, "yume_pdq (gb300): %s\n", ypdq_last_error());
@@ -836,6 +854,12 @@ __attribute__((visibility("default"))) bool yume_pdq_visit_dihedrals_smart_kerne
     if (!callback(cb_ctx, kSlotDihedral[v], threshold, q[v])) return false;
   }
   return true;
+}
+
+ypdq_status ypdq_dropin_semantics(int* semantics) {
+  if (!semantics) return YPDQ_ERR_INVALID;
+  *semantics = dropin_semantics();
+  return YPDQ_OK;
 }
 
 }  // extern "C"

@@ -153,7 +153,9 @@ __host__ __device__ constexpr uint32_t idesc_f8(uint32_t n) {
 // of packed word p holds bit 8i + 7 - m of that word, which `<< m` moves to the byte's sign
 // bit. Output word (p, m) goes to K chunk p / 4, 16-byte unit 2 (p % 4) + m / 4.
 // kWords < 8: only packed words 0 .. kWords - 1 (the first 32 * kWords bits).
-template <int kWords = 8>
+// kOne: the magnitude's byte, repeated (e4m3 1.0 = 0x38; the pair kernel below uses e5m2
+// 1.0 = 0x3C and 512.0 = 0x60); the data bit becomes the sign bit.
+template <int kWords = 8, uint32_t kOne = 0x38383838u>
 __device__ __forceinline__ void expand_row(const uint4 w0, const uint4 w1, uint8_t* chunk0,
                                            uint8_t* chunk1, int row) {
   const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
@@ -165,10 +167,10 @@ __device__ __forceinline__ void expand_row(const uint4 w0, const uint4 w1, uint8
     for (int h = 0; h < 2; ++h) {
       const uint32_t w = words[p];
       uint4 out;
-      out.x = ((w << (4 * h + 0)) & 0x80808080u) | 0x38383838u;
-      out.y = ((w << (4 * h + 1)) & 0x80808080u) | 0x38383838u;
-      out.z = ((w << (4 * h + 2)) & 0x80808080u) | 0x38383838u;
-      out.w = ((w << (4 * h + 3)) & 0x80808080u) | 0x38383838u;
+      out.x = ((w << (4 * h + 0)) & 0x80808080u) | kOne;
+      out.y = ((w << (4 * h + 1)) & 0x80808080u) | kOne;
+      out.z = ((w << (4 * h + 2)) & 0x80808080u) | kOne;
+      out.w = ((w << (4 * h + 3)) & 0x80808080u) | kOne;
       const int unit = 2 * (p & 3) + h;
       *reinterpret_cast<uint4*>(base + ((unit ^ sw) << 4)) = out;
     }
@@ -628,6 +630,346 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// scan_pair_kernel: two queries per f32 accumulator column (passes of 512 queries, t <= 36).
+//
+// The 128-bit prefix bound of scan_tc_kernel<false, 4>, with a pass's queries taken in pairs
+// (2j, 2j+1). The operands are e5m2: a database row's prefix bits become +-1 (A), query 2j's
+// +-1 (B chunk 0, row j) and query 2j+1's +-512 (B chunk 1, row j). For each 128-row tile one
+// thread issues 8 MMAs of M = 128, N = 256 (pairs), K = 32 into one f32 accumulator stage:
+//   MMA k     (k < 4): A K-chunk k x B0 K-chunk k  ->  d1 = 128 - 2 * (prefix distance of 2j)
+//   MMA 4 + k        : A K-chunk k x B1 K-chunk k  ->  512 * d2 (the same for query 2j + 1)
+// Column j then holds v = d1 + 512 d2, an integer of magnitude <= 65,664: every product is
+// +-1 or +-512 and every partial sum an integer below 2^24, so f32 accumulation is exact
+// (checked on the GPU for all three orders of the 8 MMAs, including d = +-128).
+//
+// Decoding both halves at once. With f = d + 128 in [0, 256] (even, as d is),
+// v + 65,664 = f1 + 512 f2. A pair member is a candidate when d >= dot_min = 128 - 2t.
+// Adding c = 384 - dot_min to each 9-bit field makes it carry out exactly then, so with
+// MAGIC = 2^23 + 65,664 + 513 c (an integer below 2^24, exact in f32) the sum v + MAGIC lies
+// in [2^23, 2^24), where the f32 mantissa is the integer itself, and
+//   bit 9 of its bits   <=>  query 2j   is a candidate
+//   bit 18 of its bits  <=>  query 2j+1 is a candidate
+// (field 2 + c is even, so field 1's carry lands in a clear bit 9 and cannot change whether
+// field 2 carries). A 32-column chunk costs 32 FADD and 16 three-input ORs; a chunk with a
+// candidate becomes a 64-query mask that emit_candidates re-checks over all 256 bits.
+//
+// Why pairs: reading the accumulator costs about the same per byte whatever its type, so f32
+// pairs read no more than f16 singles per query, but a pass of 512 queries puts twice the
+// MMA work behind each accumulator stage. The two stages of 256 columns then give the
+// readout and the barrier handoffs a whole tile of MMAs (~1,060 clk) to hide behind, where
+// passes of 256 f16 queries gave them ~540 clk and left the tensor pipe ~40 % idle. Eight
+// MMAs per commit also keep the issuing thread (~60 clk per MMA) off the critical path.
+// Roles and barriers are those of scan_tc_kernel<false, 4>.
+constexpr int kPairN = 256;                 // pairs per pass (MMA N)
+constexpr int kPairQueries = 2 * kPairN;    // queries per pass
+constexpr int kPairAStages = 4;             // A tiles in shared memory (16 KiB each)
+
+// Instruction descriptor: D f32, A and B e5m2, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_e5m2_f32(uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_pair_issue(uint32_t d, uint32_t a0, uint32_t b0,
+                                               uint32_t b1, uint32_t idesc) {
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks)
+    mma_f8(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 32 * ks), idesc, ks > 0 ? 1u : 0u);
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks)
+    mma_f8(d, sw128_desc(a0 + 32 * ks), sw128_desc(b1 + 32 * ks), idesc, 1u);
+}
+
+__global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const Params prm) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* const smem_base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  Smem& sm = *reinterpret_cast<Smem*>(smem_base);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t n_pack = prm.pack_stages;
+  const uint32_t n_queries = prm.nq_dev ? min(*prm.nq_dev, prm.n_queries) : prm.n_queries;
+  uint8_t* const a_smem = smem_base + kFixedBytes;    // [kPairAStages][kChunkBytes]
+  uint8_t* const bchunk0 = smem_base + prm.b_offset;  // 256 pairs x 128 B: queries 2j (+-1)
+  uint8_t* const bchunk1 = bchunk0 + kPairN * 128;    // 256 pairs x 128 B: 2j + 1 (+-512)
+  uint8_t* const packed = smem_base + prm.pack_offset;
+  const uint64_t n_tiles = (prm.n_rows + kTileRows - 1) / kTileRows;
+  const uint32_t n_passes = (n_queries + kPairQueries - 1) / kPairQueries;
+  const uint64_t my_tiles =
+      blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  volatile int* abort_flag = &sm.abort_flag;
+
+  if (tid == 0) {
+    for (uint32_t s = 0; s < n_pack; ++s) {
+      mbar_init(&sm.pk_full[s], 1);
+      mbar_init(&sm.pk_empty[s], 4);
+    }
+    for (int s = 0; s < kPairAStages; ++s) {
+      mbar_init(&sm.a_full[s], 4);
+      mbar_init(&sm.a_empty[s], 1);
+    }
+    for (int s = 0; s < kAccStages; ++s) {
+      mbar_init(&sm.acc_full[s], 1);
+      mbar_init(&sm.acc_empty[s], kEpilogueWarps);
+    }
+    mbar_init(&sm.b_full, 4);
+    mbar_init(&sm.b_empty, 1);
+    mbar_init(&sm.epi_exit, kEpilogueWarps);
+    mbar_init(&sm.exp_exit, 4);
+    mbar_init(&sm.mma_done, 1);
+    sm.abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == kMmaWarp) {
+    tmem_alloc(&sm.tmem_base, kTmemCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = sm.tmem_base;
+  if (my_tiles == 0 || n_passes == 0) {
+    if (warp == kMmaWarp) tmem_dealloc(tmem_base, kTmemCols);
+    return;
+  }
+
+  if (warp == kProducerWarp) {
+    if (lane == 0) {
+      uint32_t slot = 0, phase = 0, issued = 0;
+      bool ok = true;
+      for (uint32_t p = 0; p < n_passes && ok; ++p) {
+        for (uint64_t k = 0; k < my_tiles; ++k) {
+          const uint64_t tile = blockIdx.x + k * gridDim.x;
+          if (!mbar_wait(&sm.pk_empty[slot], phase ^ 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          const uint64_t r0 = tile * kTileRows;
+          const uint64_t nr = (prm.n_rows - r0) < kTileRows ? (prm.n_rows - r0) : kTileRows;
+          const uint32_t bytes = static_cast<uint32_t>(nr * 32);
+          mbar_arrive_expect_tx(&sm.pk_full[slot], bytes);
+          bulk_g2s(packed + slot * kPackBytes, prm.rows + r0 * 32, bytes, &sm.pk_full[slot],
+                   policy_evict_first());
+          ++issued;
+          if (++slot == n_pack) {
+            slot = 0;
+            phase ^= 1u;
+          }
+        }
+      }
+      if (!ok) {
+        raise_abort(sm, prm.dev_err);
+        // let the copies already issued land (bounded), as in scan_tc_kernel
+        for (uint32_t k = 1; k <= n_pack && k <= issued; ++k) {
+          const uint32_t sl = (slot + n_pack - k) % n_pack;
+          const uint32_t ph = (k <= slot) ? phase : (phase ^ 1u);
+          const uint64_t t0 = globaltimer_ns();
+          while (!mbar_try_wait(&sm.pk_full[sl], ph))
+            if (globaltimer_ns() - t0 > kWaitLimitNs / 4) break;
+        }
+      }
+    }
+    return;
+  }
+
+  if (warp >= kExpandWarp0 && warp < kExpandWarp0 + 4) {
+    const int e = tid - kExpandWarp0 * 32;  // 0..127: tile row; pairs e and e + 128
+    uint32_t slot = 0, phase = 0, ga = 0;
+    for (uint32_t p = 0; p < n_passes; ++p) {
+      if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag)) goto fail;
+      for (uint32_t j = e; j < static_cast<uint32_t>(kPairN); j += 128) {
+        const uint64_t q0 = static_cast<uint64_t>(p) * kPairQueries + 2 * j;
+        const uint4 zero = make_uint4(0, 0, 0, 0);
+        // a query past the end gives a zero B row: its products are all 0
+        if (q0 < n_queries) {
+          const uint4* src = reinterpret_cast<const uint4*>(prm.queries + q0 * 32);
+          expand_row<4, 0x3C3C3C3Cu>(src[0], src[1], bchunk0, nullptr, static_cast<int>(j));
+        } else {
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            *reinterpret_cast<uint4*>(bchunk0 + j * 128 + u * 16) = zero;
+        }
+        if (q0 + 1 < n_queries) {
+          const uint4* src = reinterpret_cast<const uint4*>(prm.queries + (q0 + 1) * 32);
+          expand_row<4, 0x60606060u>(src[0], src[1], bchunk1, nullptr, static_cast<int>(j));
+        } else {
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            *reinterpret_cast<uint4*>(bchunk1 + j * 128 + u * 16) = zero;
+        }
+      }
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.b_full);
+
+      for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
+        const uint32_t as = ga % kPairAStages;
+        const uint32_t aph = (ga / kPairAStages) & 1u;
+        if (!mbar_wait(&sm.pk_full[slot], phase, abort_flag)) goto fail;
+        const uint4* src = reinterpret_cast<const uint4*>(packed + slot * kPackBytes + e * 32);
+        const uint4 w0 = src[0], w1 = src[1];
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.pk_empty[slot]);
+        if (++slot == n_pack) {
+          slot = 0;
+          phase ^= 1u;
+        }
+        if (!mbar_wait(&sm.a_empty[as], aph ^ 1u, abort_flag)) goto fail;
+        expand_row<4, 0x3C3C3C3Cu>(w0, w1, a_smem + static_cast<size_t>(as) * kChunkBytes,
+                                   nullptr, e);
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.a_full[as]);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.exp_exit);
+    return;
+  fail:
+    if (lane == 0) {
+      raise_abort(sm, prm.dev_err);
+      mbar_arrive(&sm.exp_exit);
+    }
+    return;
+  }
+
+  if (warp == kMmaWarp) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_e5m2_f32(kPairN);
+      const uint32_t b0 = smem_u32(bchunk0), b1 = smem_u32(bchunk1);
+      uint32_t ga = 0;
+      bool ok = true;
+      for (uint32_t p = 0; p < n_passes && ok; ++p) {
+        if (!mbar_wait(&sm.b_full, p & 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
+          const uint32_t as = ga % kPairAStages;
+          const uint32_t ac = ga % kAccStages;
+          if (!mbar_wait(&sm.a_full[as], (ga / kPairAStages) & 1u, abort_flag) ||
+              !mbar_wait(&sm.acc_empty[ac], ((ga / kAccStages) & 1u) ^ 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          mma_pair_issue(tmem_base + ac * kPairN,
+                         smem_u32(a_smem + static_cast<size_t>(as) * kChunkBytes), b0, b1, idesc);
+          mma_commit(&sm.a_empty[as]);
+          mma_commit(&sm.acc_full[ac]);
+        }
+        if (ok) mma_commit(&sm.b_empty);
+      }
+      if (!ok) raise_abort(sm, prm.dev_err);
+      mma_commit(&sm.mma_done);
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.mma_done, 0))
+        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
+    }
+    __syncwarp();
+    // the epilogue warps arrive on epi_exit when they stop reading TMEM, the expanders on
+    // exp_exit when they stop writing shared memory the MMAs read
+    {
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.epi_exit, 0))
+        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
+      const uint64_t t1 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.exp_exit, 0))
+        if (globaltimer_ns() - t1 > kWaitLimitNs) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
+    }
+    tc_fence_after();
+    tmem_dealloc(tmem_base, kTmemCols);
+    return;
+  }
+
+  // ---- epilogue warps 0..7: rows (warp % 4) * 32 + lane; group warp / 4 reads the pair
+  // columns 128 g .. 128 g + 127 of the stage as four loads of 32, two in flight at a time
+  {
+    const float dot_min = 128.0f - 2.0f * static_cast<float>(prm.threshold);
+    const float magic = 8388608.0f + 65664.0f + 513.0f * (384.0f - dot_min);
+    const uint32_t quarter = static_cast<uint32_t>(warp & 3);
+    const uint32_t group = static_cast<uint32_t>(warp >> 2);
+    const uint32_t lane_addr = (quarter * 32) << 16;
+    uint32_t ga = 0;
+    bool ok = true;
+    for (uint32_t p = 0; p < n_passes && ok; ++p) {
+      const uint64_t pass_q = static_cast<uint64_t>(p) * kPairQueries;
+      for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
+        const uint64_t tile = blockIdx.x + k * gridDim.x;
+        const uint32_t ac = ga % kAccStages;
+        if (!mbar_wait(&sm.acc_full[ac], (ga / kAccStages) & 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint64_t row = tile * kTileRows + quarter * 32 + lane;
+        const bool row_ok = row < prm.n_rows;
+        const uint32_t col0 = ac * kPairN + 128 * group;
+        // candidate mask of 32 pair columns (64 queries; bits 2i and 2i + 1 are pair i's
+        // two queries); `need` is set for the whole warp when any lane has a candidate
+        auto chunk_mask = [&](const uint32_t (&raw)[32], bool& need) -> uint64_t {
+          uint32_t any = 0;
+#pragma unroll
+          for (int i = 0; i < 32; i += 2)
+            any |= __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic)) |
+                   __float_as_uint(__fadd_rn(__uint_as_float(raw[i + 1]), magic));
+          const bool cand = row_ok && (any & 0x40200u);
+          need = __any_sync(0xffffffffu, cand);
+          uint64_t mask = 0;
+          if (cand) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              const uint32_t x = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic));
+              mask |= static_cast<uint64_t>((x >> 9) & 1u) << (2 * i);
+              mask |= static_cast<uint64_t>((x >> 18) & 1u) << (2 * i + 1);
+            }
+          }
+          return mask;
+        };
+        uint32_t raw0[32], raw1[32];
+        float unused[32];
+        uint64_t mask[4];
+        bool need[4];
+        tmem_ld32_nowait(tmem_base + lane_addr + col0, raw0);
+        tmem_ld32_nowait(tmem_base + lane_addr + col0 + 32, raw1);
+        tmem_ld_wait();
+        tmem_take(raw0, unused);
+        tmem_take(raw1, unused);
+        mask[0] = chunk_mask(raw0, need[0]);
+        mask[1] = chunk_mask(raw1, need[1]);
+        tmem_ld32_nowait(tmem_base + lane_addr + col0 + 64, raw0);
+        tmem_ld32_nowait(tmem_base + lane_addr + col0 + 96, raw1);
+        tmem_ld_wait();
+        tmem_take(raw0, unused);
+        tmem_take(raw1, unused);
+        // the stage's last columns are in registers: hand it back before the hit reporting
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+        mask[2] = chunk_mask(raw0, need[2]);
+        mask[3] = chunk_mask(raw1, need[3]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (need[i])
+            emit_candidates(mask[i], row, pass_q + 2 * (128 * group + 32 * i), n_queries, prm,
+                            lane);
+      }
+    }
+    if (!ok && lane == 0) raise_abort(sm, prm.dev_err);
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.epi_exit);
+  }
+}
+
 }  // namespace tc
 
 cudaError_t scan_tc_init() {
@@ -635,7 +977,8 @@ cudaError_t scan_tc_init() {
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<true, 8>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 4>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 6>),
-                        reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 8>)}) {
+                        reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 8>),
+                        reinterpret_cast<const void*>(tc::scan_pair_kernel)}) {
     const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                static_cast<int>(tc::kSmemLimit));
     if (e != cudaSuccess) return e;
@@ -653,7 +996,9 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   uint32_t n = (p.n_queries + 63u) & ~63u;
   prm.n_tile = n > static_cast<uint32_t>(tc::kMaxN) ? static_cast<uint32_t>(tc::kMaxN) : n;
   if (p.n_tile) {
-    if (p.n_tile % 64u != 0 || p.n_tile > static_cast<uint32_t>(tc::kMaxN))
+    // 64..256 in steps of 64: one query per accumulator column; 512: the pair kernel
+    if ((p.n_tile % 64u != 0 || p.n_tile > static_cast<uint32_t>(tc::kMaxN)) &&
+        p.n_tile != static_cast<uint32_t>(tc::kPairQueries))
       return cudaErrorInvalidValue;
     prm.n_tile = p.n_tile;
   }
@@ -664,11 +1009,33 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   prm.dev_err = p.dev_err;
   prm.query_base = p.query_base;
   prm.nq_dev = p.nq_dev;
+  // at a small threshold the first 128 bits bound the distance (kKSteps = 4)
+  const bool half_k = p.threshold <= 36;
+  const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
+  const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
+  // more than one pass of 256 queries at t <= 36 (or n_tile = 512): passes of 512 queries,
+  // two per accumulator column (scan_pair_kernel)
+  if (half_k && (p.n_tile == static_cast<uint32_t>(tc::kPairQueries) ||
+                 (p.n_tile == 0 && p.n_queries > static_cast<uint32_t>(tc::kMaxN)))) {
+    prm.n_tile = tc::kPairQueries;
+    prm.a_stages = tc::kPairAStages;
+    // layout: [fixed Smem][A: 4 x 16 KB][B: 2 x 256 pairs x 128 B][packed ring], 1024-aligned
+    prm.b_offset = static_cast<uint32_t>(tc::kFixedBytes +
+                                         static_cast<size_t>(tc::kPairAStages) * tc::kChunkBytes);
+    const size_t b_end = prm.b_offset + 2 * static_cast<size_t>(tc::kPairN) * 128;
+    size_t stages = (tc::kSmemLimit - 1024 - b_end) / tc::kPackBytes;
+    if (stages > static_cast<size_t>(tc::kMaxPackStages)) stages = tc::kMaxPackStages;
+    prm.pack_stages = static_cast<uint32_t>(stages);
+    prm.pack_offset = static_cast<uint32_t>(b_end);
+    const size_t smem = b_end + stages * tc::kPackBytes + 1024;
+    tc::scan_pair_kernel<<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
+    return cudaGetLastError();
+  }
+  if (p.n_tile == static_cast<uint32_t>(tc::kPairQueries))
+    return cudaErrorInvalidValue;  // pairs need the 128-bit bound (t <= 36)
   // passes of <= 128 queries: two MMA issuers and A in tensor memory (the pass is bound by
   // issuing and shared-memory traffic, not by the tensor core)
   const bool dual = prm.n_tile <= 128;
-  // at a small threshold the first 128 bits bound the distance (kKSteps = 4)
-  const bool half_k = p.threshold <= 36;
   uint32_t a_stages = tc::kAStages;
   if (dual) {
     a_stages = (tc::kTmemCols - tc::kAccStages * prm.n_tile) / (half_k ? 32 : 64);
@@ -687,8 +1054,6 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   prm.pack_stages = static_cast<uint32_t>(stages);
   prm.pack_offset = static_cast<uint32_t>(b_end);
   const size_t smem = b_end + stages * tc::kPackBytes + 1024;
-  const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
-  const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
   // passes of 256 queries at t <= 62: the first 192 bits bound the distance
   const bool prefix192 = !dual && !half_k && p.threshold <= 62;
   const unsigned g = static_cast<unsigned>(grid);

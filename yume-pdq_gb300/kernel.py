@@ -36,6 +36,16 @@ class Dihedrals:
         return (b[0], b[1]), (b[2], b[3])
 
 
+def host_semantics():
+    """Name of the dihedral sign convention that yume-pdq's smart_kernel() uses on this host
+    (src/kernel/mod.rs:79-176; ypdq_dropin_semantics): "avx2" on x86_64 with AVX2 and FMA,
+    "scalar" on any other host, unless YUME_PDQ_DIHEDRAL_SEMANTICS overrides it."""
+    import ctypes
+    s = ctypes.c_int(-1)
+    _lib.check(_lib.load().ypdq_dropin_semantics(ctypes.byref(s)))
+    return ("exact", "avx2", "scalar")[s.value]
+
+
 # Slot order of every batched output: the image, then visit_dihedrals' order.
 SLOT_DIHEDRALS = [
     Dihedrals.NORMAL, Dihedrals.FLOPPED, Dihedrals.ROTATED_180, Dihedrals.FLIPPED,

@@ -104,8 +104,9 @@ def main(argv=None):
                     choices=sorted(BYTES_PER_PIXEL))
     ap.add_argument("-f", "--format", default="bin")
     ap.add_argument("--dihedrals", action="store_true", help="output all 8 hashes per frame")
-    ap.add_argument("--semantics", default="exact", choices=["exact", "avx2", "scalar"],
-                    help="dihedral sign convention (the reference's kernels differ)")
+    ap.add_argument("--semantics", default="host", choices=["host", "exact", "avx2", "scalar"],
+                    help="dihedral sign convention (the reference's kernels differ); host: "
+                         "the one the reference's smart_kernel uses on this host")
     ap.add_argument("--reference-kernel", action="store_true",
                     help="hash with ReferenceKernel<f32> (full Jarosz filter, "
                          "YPDQ_COMPRESS_JAROSZ) instead of the default kernel (an extension)")
@@ -120,6 +121,8 @@ def main(argv=None):
     import __graft_entry__ as g
     yp = g.load_package()
     ctx = yp.Context(0)
+    if a.semantics == "host":
+        a.semantics = yp.kernel.host_semantics()
     fin = sys.stdin.buffer if a.input == "-" else open(a.input, "rb")
     fout = sys.stdout.buffer if a.output == "-" else open(a.output, "wb")
     slots = 8 if a.dihedrals else 1

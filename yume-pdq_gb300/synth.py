@@ -115,5 +115,13 @@ def plant(rows, queries, n_plant, dmin, dmax, seed=0):
     return pos, qid, dist
 
 
+def plant_near_duplicates(rows, hashes, n_plant, seed, dmax=31):
+    """The screening workload's database edit, in place: n_plant rows (at most all of them)
+    replaced by copies of randomly chosen hashes ([..., 32] u8, e.g. all 8 dihedral hashes
+    of a batch) at exact distances U{0..dmax}. Returns (positions, hash ids, distances)."""
+    h = np.ascontiguousarray(hashes, np.uint8).reshape(-1, 32)
+    return plant(rows, h, min(int(n_plant), rows.shape[0]), 0, dmax, seed)
+
+
 def popcount_rows(rows):
     return np.unpackbits(np.ascontiguousarray(rows, np.uint8), axis=1).sum(axis=1)
