@@ -562,8 +562,15 @@ def run_ours(args):
         achieved = flops / (scan_avg / 1000.0) / 1e12
         fp8 = fp8_dense_burst(local) if rank == 0 else None
         peak = fp8 if fp8 else 2 * bf16_peak
-        passes = (nq + 255) // 256
-        roofline = {"bound": "tensor", "kernel": "scan_tc_kernel (tcgen05 kind::f8f6f4)",
+        # past 256 queries at t <= 36 the launch runs passes of 512 queries, two per
+        # accumulator column (mirrors launch_scan_tc)
+        pairs = args.threshold <= 36 and nq > 256
+        per_pass = 512 if pairs else 256
+        passes = (nq + per_pass - 1) // per_pass
+        roofline = {"bound": "tensor",
+                    "kernel": ("scan_pair_kernel (tcgen05 kind::f8f6f4, e5m2, two queries per f32 "
+                               "accumulator column)" if pairs else
+                               "scan_tc_kernel (tcgen05 kind::f8f6f4)"),
                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak,
                     "peak_source": ("measured fp8 burst (torch._scaled_mm e4m3 8192^3, best of "
@@ -571,13 +578,14 @@ def run_ours(args):
                                     "%s bf16 burst x 2 (fp8 dense)" % peak_kind),
                     "traffic": None,
                     "traffic_computed": passes * 32.0 * n + hits_per_step * 16.0,
-                    "traffic_note": "traffic_computed = 32 B x rows x query passes of 256 + "
-                                    "16 B per hit (the database streams once per pass), "
-                                    "computed, not a counter",
+                    "traffic_note": "traffic_computed = 32 B x rows x %d query passes of %d + 16 B "
+                                    "per hit (the database streams once per pass), computed, not "
+                                    "a counter" % (passes, per_pass),
                     "launch_ms": scan_avg, "launches_per_step": 1,
                     "mma_k_bits": k_bits,
                     "pairs_per_s": nq * n / (scan_avg / 1e3),
-                    "db_stream_gbs": (n * 32 * passes) / (scan_avg / 1e3) / 1e9}
+                    "db_stream_gbs": (n * 32 * passes) / (scan_avg / 1e3) / 1e9,
+                    "query_passes": passes}
     elif scan_avg >= hash_avg:
         # SIMT scan: one launch reads the whole database once for up to 2048 queries
         dom_ms = scan_avg / scan_launches

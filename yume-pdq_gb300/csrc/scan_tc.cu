@@ -996,9 +996,7 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   uint32_t n = (p.n_queries + 63u) & ~63u;
   prm.n_tile = n > static_cast<uint32_t>(tc::kMaxN) ? static_cast<uint32_t>(tc::kMaxN) : n;
   if (p.n_tile) {
-    // 64..256 in steps of 64: one query per accumulator column; 512: the pair kernel
-    if ((p.n_tile % 64u != 0 || p.n_tile > static_cast<uint32_t>(tc::kMaxN)) &&
-        p.n_tile != static_cast<uint32_t>(tc::kPairQueries))
+    if (p.n_tile % 64u != 0 || p.n_tile > static_cast<uint32_t>(tc::kMaxN) || p.pair_n)
       return cudaErrorInvalidValue;
     prm.n_tile = p.n_tile;
   }
@@ -1013,10 +1011,11 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   const bool half_k = p.threshold <= 36;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
-  // more than one pass of 256 queries at t <= 36 (or n_tile = 512): passes of 512 queries,
-  // two per accumulator column (scan_pair_kernel)
-  if (half_k && (p.n_tile == static_cast<uint32_t>(tc::kPairQueries) ||
-                 (p.n_tile == 0 && p.n_queries > static_cast<uint32_t>(tc::kMaxN)))) {
+  if (p.pair_n && (!half_k || p.pair_n != static_cast<uint32_t>(tc::kPairN)))
+    return cudaErrorInvalidValue;  // pairs need the 128-bit bound (t <= 36)
+  // at t <= 36, passes of 512 queries, two per accumulator column (scan_pair_kernel), when
+  // asked for or by default past one pass of 256
+  if (half_k && !p.n_tile && (p.pair_n || p.n_queries > static_cast<uint32_t>(tc::kMaxN))) {
     prm.n_tile = tc::kPairQueries;
     prm.a_stages = tc::kPairAStages;
     // layout: [fixed Smem][A: 4 x 16 KB][B: 2 x 256 pairs x 128 B][packed ring], 1024-aligned
@@ -1031,8 +1030,6 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
     tc::scan_pair_kernel<<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
     return cudaGetLastError();
   }
-  if (p.n_tile == static_cast<uint32_t>(tc::kPairQueries))
-    return cudaErrorInvalidValue;  // pairs need the 128-bit bound (t <= 36)
   // passes of <= 128 queries: two MMA issuers and A in tensor memory (the pass is bound by
   // issuing and shared-memory traffic, not by the tensor core)
   const bool dual = prm.n_tile <= 128;

@@ -63,7 +63,8 @@ struct Request {
 struct Bucket {
   uint32_t images = 0;
   int algo = YPDQ_SCAN_TC;
-  uint32_t n_tile = 0;
+  uint32_t n_tile = 0;   // tensor-core scan: queries per pass, one per accumulator column
+  uint32_t pair_n = 0;   // or query pairs per pass, two per column (t <= 36)
   float ms = 0.0f;
   uint64_t steps = 0;
 };
@@ -152,6 +153,7 @@ ypdq_status capture_bucket(ypdq_server* S, Slot& sl, const Bucket& b, cudaGraphE
   sp.n_queries = 8 * nb;
   sp.nq_dev = &sl.d_hdr->n_queries;
   sp.n_tile = b.algo == YPDQ_SCAN_TC ? b.n_tile : 0;
+  sp.pair_n = b.algo == YPDQ_SCAN_TC ? b.pair_n : 0;
   sp.threshold = S->cfg.threshold;
   sp.hits = sl.d_hits;
   sp.capacity = S->cfg.step_hit_capacity;
@@ -459,10 +461,13 @@ ypdq_status autotune(ypdq_server* S) {
   for (Bucket& b : S->buckets) {
     std::vector<Bucket> cand;
     const uint32_t nq = 8 * b.images;
-    if (nq <= 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_SIMT, 0, 0.0f, 0});
+    if (nq <= 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_SIMT, 0, 0, 0.0f, 0});
     const uint32_t nq64 = (nq + 63u) & ~63u;
     for (uint32_t nt = 64; nt <= 256; nt *= 2)
-      if (nt <= nq64 || nt == 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, nt, 0.0f, 0});
+      if (nt <= nq64 || nt == 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, nt, 0, 0.0f, 0});
+    // two queries per accumulator column (t <= 36): passes of 512 queries
+    if (S->cfg.threshold <= 36 && nq > 128)
+      cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, 256, 0.0f, 0});
     float best = 0.0f;
     for (Bucket& c : cand) {
       ypdq_status st = time_bucket(S, c, &c.ms);
@@ -471,6 +476,7 @@ ypdq_status autotune(ypdq_server* S) {
         best = c.ms;
         b.algo = c.algo;
         b.n_tile = c.n_tile;
+        b.pair_n = c.pair_n;
         b.ms = c.ms;
       }
     }
@@ -671,7 +677,10 @@ ypdq_status ypdq_server_get_stats(ypdq_server* S, ypdq_server_stats* o, int rese
   for (uint32_t i = 0; i < o->n_buckets; ++i) {
     o->bucket_images[i] = S->buckets[i].images;
     o->bucket_algo[i] = S->buckets[i].algo;
-    o->bucket_n_tile[i] = S->buckets[i].algo == YPDQ_SCAN_TC ? S->buckets[i].n_tile : 0;
+    o->bucket_n_tile[i] = S->buckets[i].algo != YPDQ_SCAN_TC ? 0
+                          : S->buckets[i].pair_n ? 2 * S->buckets[i].pair_n
+                                                 : S->buckets[i].n_tile;
+    o->bucket_pair[i] = S->buckets[i].algo == YPDQ_SCAN_TC && S->buckets[i].pair_n ? 1 : 0;
     o->bucket_ms[i] = S->buckets[i].ms;
     o->bucket_steps[i] = S->buckets[i].steps;
   }
