@@ -181,6 +181,55 @@ ypdq_status ypdq_dihedrals_batch(ypdq_ctx *ctx, const float *d_pdqf, const float
                                  float *d_thresholds_out, float *d_pdqf_out,
                                  ypdq_stream_t stream);
 
+/* --------------------------------------------------------- per-stage calls */
+
+/*
+ * The Kernel trait's per-image methods (src/kernel/mod.rs:268-497) on n items per call, on
+ * the device, bit for bit with yume-pdq's f32 implementations. ypdq_hash_batch fuses these
+ * stages; the calls below serve callers that run them one at a time, as the reference's
+ * pipeline functions (src/lib.rs:427-455) do. Kernel::quantize is ypdq_dihedrals_batch with
+ * d_thresholds NULL (slot 0); Kernel::jarosz_compress is ypdq_hash_batch's d_buf1 output.
+ */
+
+/* Kernel::dct2d (src/kernel/mod.rs:484; DefaultKernel::dct2d_impl :543-574): n compressed
+ * buffers of 127 rows of `stride` f32 each (the first 127 columns are read; stride >= 127,
+ * 128 for the reference's padded Buffer1), consecutive, -> n x 16 x 16 f32 PDQF. */
+ypdq_status ypdq_dct2d_batch(ypdq_ctx *ctx, const float *d_buf1, int64_t n, int stride,
+                             float *d_pdqf, ypdq_stream_t stream);
+
+/* Kernel::sum_of_gradients (src/kernel/mod.rs:469; DefaultKernel :617-642): the quality
+ * numerator of n PDQF matrices (n x 256 f32) -> n f32. Kernel::adjust_quality is then
+ * min(x / 180, 1). */
+ypdq_status ypdq_sum_of_gradients_batch(ypdq_ctx *ctx, const float *d_pdqf, int64_t n,
+                                        float *d_out, ypdq_stream_t stream);
+
+typedef enum {
+  YPDQ_PDQF_T = 0,                    /* Kernel::pdqf_t (src/kernel/mod.rs:345-361) */
+  YPDQ_PDQF_NEGATE_ALT_COLS = 1,      /* Kernel::pdqf_negate_alt_cols::<NEGATE> (:368-383) */
+  YPDQ_PDQF_NEGATE_ALT_ROWS = 2,      /* Kernel::pdqf_negate_alt_rows::<NEGATE> (:391-406) */
+  YPDQ_PDQF_NEGATE_OFF_DIAGONALS = 3  /* Kernel::pdqf_negate_off_diagonals (:413-427) */
+} ypdq_pdqf_op;
+
+/*
+ * A PDQF transform, in place on n matrices (n x 256 f32), as the kernel of `semantics`
+ * implements it; `negate` is the method's NEGATE parameter. yume-pdq's kernels differ:
+ *   NEGATE_ALT_ROWS  SCALAR (trait default): rows 0,2,..,14 (negate 0) or 1,3,..,15
+ *                    (negate 1); AVX2 and EXACT (x86.rs:285-327, 989-1024): the other rows.
+ *   NEGATE_ALT_COLS  SCALAR and EXACT (x86.rs:1026-1079): columns 0,2,..,14 (negate 0) or
+ *                    1,3,..,15; AVX2 (x86.rs:330-378): the same among columns 0..7 only.
+ *   T and NEGATE_OFF_DIAGONALS are the same in every kernel; negate is ignored.
+ */
+ypdq_status ypdq_pdqf_transform_batch(ypdq_ctx *ctx, float *d_pdqf, int64_t n, int op,
+                                      int negate, int semantics, ypdq_stream_t stream);
+
+/* Kernel::cvt_rgb8_to_luma8f / cvt_rgba8_to_luma8f (src/kernel/mod.rs:303-340): n pixels
+ * of `channels` bytes (3: RGB8, 4: RGBA8, alpha ignored) -> n f32 luma values
+ * (r_coeff r + g_coeff g) + b_coeff b, each product and sum rounded to f32. The reference
+ * passes the BT.601 coefficients (src/kernel/constants.rs:23). */
+ypdq_status ypdq_cvt_luma8f(ypdq_ctx *ctx, const uint8_t *d_pixels, int64_t n_pixels,
+                            int channels, float r_coeff, float g_coeff, float b_coeff,
+                            float *d_out, ypdq_stream_t stream);
+
 /* ----------------------------------------------------------------- matching */
 
 /*
@@ -236,8 +285,9 @@ ypdq_status ypdq_screen_host(ypdq_ctx *ctx, ypdq_db *db, const void *h_images, i
 
 /*
  * The chunks ypdq_screen_host cuts n images into (host-only; no device or context needed).
- * The copy of each chunk overlaps the hash and scan of the one before. Chunks grow from
- * 32 images, in whole multiples of 32, as fast as the copies stay ahead of the compute
+ * The copy of each chunk overlaps the hash and scan of the one before. Chunks grow from one
+ * granule of whole scan passes (64 images at threshold <= 36, where passes hold 512
+ * queries; 32 images otherwise), in whole granules, as fast as the copies stay ahead of the compute
  * (estimated for a GB300 from the input kind, the hash kernel's fixed cost per chunk and
  * the scan of 8 queries per image against n_rows rows at `threshold`). Writes
  * bounds[0] = 0 < bounds[1] < ... < bounds[*n_chunks] = n (at most

@@ -301,3 +301,48 @@ def dct2d_avx2_matrix(D, buf128):
     out = np.zeros((16, 16), np.float32)
     lib().ypdqo_dct2d_avx2_matrix(_p(D), _p(b), _p(out))
     return out
+
+
+def pdqf_transform(pdqf, op, negate=False, semantics="scalar"):
+    """The Kernel trait's PDQF transforms as each reference kernel implements them, on one
+    16x16 matrix (a copy is returned). op: 0 pdqf_t (src/kernel/mod.rs:345-361), 1
+    pdqf_negate_alt_cols::<NEGATE> (trait :368-383; Avx2F32Kernel src/kernel/x86.rs:330-378,
+    one 8-wide multiply per row; Avx512F32Kernel :1026-1079), 2 pdqf_negate_alt_rows::<NEGATE>
+    (trait :391-406; AVX2 :285-327 and AVX-512 :989-1024 start at the other row), 3
+    pdqf_negate_off_diagonals (:413-427, the same in every kernel)."""
+    q = np.array(pdqf, np.float32, copy=True).reshape(16, 16)
+    if op == 0:
+        for i in range(16):
+            for j in range(16):
+                if i < j:
+                    q[i, j], q[j, i] = q[j, i], q[i, j]
+    elif op == 1:
+        if semantics == "avx2":
+            coef = np.array(([1.0, -1.0] if negate else [-1.0, 1.0]) * 4, np.float32)
+            for i in range(16):
+                q[i, :8] = q[i, :8] * coef
+        else:
+            for i in range(16):
+                for j in range(1 if negate else 0, 16, 2):
+                    q[i, j] = -q[i, j]
+    elif op == 2:
+        start = (1 if negate else 0) if semantics == "scalar" else (0 if negate else 1)
+        for i in range(start, 16, 2):
+            q[i, :] = -q[i, :]
+    elif op == 3:
+        for i in range(16):
+            for j in range(16):
+                if (j - i) % 2 == 1:
+                    q[i, j] = -q[i, j]
+    else:
+        raise ValueError(op)
+    return q
+
+
+def luma_with(px, coeffs):
+    """cvt_rgb8_to_luma8f / cvt_rgba8_to_luma8f (src/kernel/mod.rs:303-340) with given
+    coefficients: (r_c r + g_c g) + b_c b, every product and sum rounded to f32."""
+    px = np.asarray(px, np.uint8)
+    r, g, b = (px[..., c].astype(np.float32) for c in range(3))
+    rc, gc, bc = (np.float32(c) for c in coeffs)
+    return ((rc * r + gc * g) + bc * b).astype(np.float32)

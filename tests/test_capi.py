@@ -110,7 +110,7 @@ def test_server_config_default_and_argument_checks(yp):
 
 def test_screen_chunk_plan(yp):
     """ypdq_screen_plan (host-only): the chunks of ypdq_screen_host cover [0, n) in order,
-    are whole multiples of 32 images except the last and number at most 32. They grow
+    are whole multiples of 32 images (64 at t <= 36) except the last and number at most 32. They grow
     geometrically when hashing and scanning an image takes longer than copying it, and
     slowly (by the hash kernel's fixed cost per chunk) when it does not."""
     lib = yp._lib.load()
@@ -129,11 +129,15 @@ def test_screen_chunk_plan(yp):
             sizes = np.diff(b)
             assert b[0] == 0 and b[-1] == n and (sizes > 0).all() and len(sizes) <= 32
             assert (sizes[:-1] % 32 == 0).all()
-    # 1,024 f32 images against 10M rows at t = 31: ~7 us of hash and scan per image against
-    # ~5 us of copy, so the chunks grow from 32 images to a few hundred
+    # 1,024 f32 images against 10M rows at t = 31: ~6 us of hash and scan per image against
+    # ~5 us of copy, so the chunks grow from 64 images (one pass of 512 queries in pairs) to
+    # a few hundred, in whole passes
     sizes = np.diff(plan(1024, 0, 10_000_000, 31))
-    assert sizes[0] == 32 and (np.diff(sizes[:-1]) >= 0).all() and sizes.max() >= 256
-    assert 6 <= len(sizes) <= 12
+    assert sizes[0] == 64 and (sizes % 64 == 0).all() and sizes.max() >= 192
+    assert 5 <= len(sizes) <= 12
+    # above t = 36 passes hold 256 queries: chunks of whole 32-image passes
+    sizes48 = np.diff(plan(1024, 0, 10_000_000, 48))
+    assert sizes48[0] == 32 and (sizes48 % 32 == 0).all()
     # a small database: copying dominates and a chunk's compute is mostly the hash kernel's
     # one round over its images, so chunks grow only by that fixed cost
     small = np.diff(plan(1024, 0, 60_000, 31))
@@ -234,3 +238,23 @@ def test_dropin_semantics_default_follows_host():
     for name, want in (("exact", 0), ("avx2", 1), ("scalar", 2)):
         assert _dropin_semantics_in_child(name) == want
     assert _dropin_semantics_in_child("bogus") == _host_dropin_semantics()
+
+
+REFERENCE_CONSUMER = "/root/reference/integration/dummy.c"  # yume-pdq's own C example
+
+
+def test_reference_c_consumer_links_unchanged(tmp_path):
+    """yume-pdq's C example (integration/dummy.c), compiled unchanged with gcc, links
+    against libyumepdq_gb300.so in place of libyume_pdq.so. Only where the reference tree is
+    present (running it needs a GPU; tests/dropin_consumer.c covers the run on one)."""
+    import pytest
+    import subprocess
+    if not os.path.exists(REFERENCE_CONSUMER):
+        pytest.skip("reference tree not present")
+    lib_dir = os.path.join(ROOT, "yume-pdq_gb300", "_build")
+    exe = str(tmp_path / "dummy")
+    r = subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", exe, REFERENCE_CONSUMER,
+                        "-L", lib_dir, "-l:libyumepdq_gb300.so"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    nm = subprocess.run(["nm", "-D", "--undefined-only", exe], capture_output=True, text=True)
+    assert "yume_pdq_hash_smart_kernel" in nm.stdout

@@ -26,6 +26,7 @@ DCT_FP32, DCT_TF32, DCT_BF16X3 = 0, 1, 2
 DIHEDRAL_EXACT, DIHEDRAL_AVX2, DIHEDRAL_SCALAR = 0, 1, 2
 SEMANTICS = {"exact": DIHEDRAL_EXACT, "avx2": DIHEDRAL_AVX2, "scalar": DIHEDRAL_SCALAR}
 SCAN_AUTO, SCAN_SIMT, SCAN_B1MMA, SCAN_TC = 0, 1, 2, 3
+PDQF_T, PDQF_NEGATE_ALT_COLS, PDQF_NEGATE_ALT_ROWS, PDQF_NEGATE_OFF_DIAGONALS = 0, 1, 2, 3
 H2D, D2H, D2D = 0, 1, 2
 
 
@@ -90,6 +91,10 @@ SIGNATURES = {
     "ypdq_hash_occupancy": (i32, [P, i32, i32, ctypes.POINTER(ctypes.c_int)]),
     "ypdq_hash_batch": (i32, [P, P, i64, i32, i32, i32, P, P, P, P, i32, P, P]),
     "ypdq_dihedrals_batch": (i32, [P, P, P, i64, i32, P, P, P, P, P]),
+    "ypdq_dct2d_batch": (i32, [P, P, i64, i32, P, P]),
+    "ypdq_sum_of_gradients_batch": (i32, [P, P, i64, P, P]),
+    "ypdq_pdqf_transform_batch": (i32, [P, P, i64, i32, i32, i32, P]),
+    "ypdq_cvt_luma8f": (i32, [P, P, i64, i32, f32, f32, f32, P, P]),
     "ypdq_scan": (i32, [P, P, u64, P, u32, u32, P, u64, P, i32, P]),
     "ypdq_sort_hits": (i32, [P, P, u64, P]),
     "ypdq_db_create": (i32, [P, P, u64, PP]),

@@ -14,7 +14,7 @@ LIB_NAME = "libyumepdq_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
 SOURCES = ["hash.cu", "scan.cu", "scan_tc.cu", "synth.cu", "capi.cu", "noalloc.cu", "serve.cu",
-           "dbfile.cu", "jarosz.cu"]
+           "dbfile.cu", "jarosz.cu", "stages.cu"]
 HEADERS = ["ypdq_internal.cuh", "ypdq_tables.h", "capi_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [

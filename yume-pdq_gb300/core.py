@@ -196,6 +196,70 @@ def dihedrals_batch(ctx, pdqf, thresholds, semantics="exact"):
     }
 
 
+def dct2d_batch(ctx, buffers):
+    """Kernel::dct2d of n compressed buffers on the GPU (ypdq_dct2d_batch): [n, 127, w] f32
+    with w >= 127 (127 or the reference's padded 128; the first 127 columns are read)
+    -> PDQF [n, 16, 16]."""
+    b = np.ascontiguousarray(buffers, np.float32)
+    if b.ndim != 3 or b.shape[1] < 127 or b.shape[2] < 127:
+        raise ValueError("buffers must be [n, 127+, 127+], got %s" % (b.shape,))
+    b = np.ascontiguousarray(b[:, :127])
+    n, w = b.shape[0], b.shape[2]
+    if n == 0:
+        return np.zeros((0, 16, 16), np.float32)
+    d_b, d_p = ctx.to_device(b), ctx.alloc(n * 1024)
+    check(ctx.lib.ypdq_dct2d_batch(ctx.handle, d_b.ptr, n, w, d_p.ptr, None))
+    ctx.sync()
+    return d_p.download((n, 16, 16), np.float32)
+
+
+def sum_of_gradients_batch(ctx, pdqf):
+    """Kernel::sum_of_gradients of n PDQF matrices [n, 16, 16] on the GPU -> [n] f32."""
+    p = np.ascontiguousarray(pdqf, np.float32).reshape(-1, 256)
+    n = p.shape[0]
+    if n == 0:
+        return np.zeros(0, np.float32)
+    d_p, d_g = ctx.to_device(p), ctx.alloc(n * 4)
+    check(ctx.lib.ypdq_sum_of_gradients_batch(ctx.handle, d_p.ptr, n, d_g.ptr, None))
+    ctx.sync()
+    return d_g.download((n,), np.float32)
+
+
+def pdqf_transform_batch(ctx, pdqf, op, negate=False, semantics="exact"):
+    """One Kernel PDQF transform (ypdq_pdqf_op: _lib.PDQF_T, PDQF_NEGATE_ALT_COLS,
+    PDQF_NEGATE_ALT_ROWS, PDQF_NEGATE_OFF_DIAGONALS) of n matrices [n, 16, 16] on the GPU,
+    as the kernel of `semantics` implements it; returns the transformed matrices."""
+    p = np.ascontiguousarray(pdqf, np.float32).reshape(-1, 256)
+    n = p.shape[0]
+    if n == 0:
+        return p.reshape(0, 16, 16).copy()
+    d_p = ctx.to_device(p)
+    check(ctx.lib.ypdq_pdqf_transform_batch(ctx.handle, d_p.ptr, n, int(op), int(bool(negate)),
+                                            _semantics(semantics), None))
+    ctx.sync()
+    return d_p.download((n, 16, 16), np.float32)
+
+
+BT601 = (0.299, 0.587, 0.114)  # src/kernel/constants.rs:23
+
+
+def cvt_luma8f(ctx, pixels, coeffs=BT601):
+    """Kernel::cvt_rgb8_to_luma8f / cvt_rgba8_to_luma8f on the GPU (ypdq_cvt_luma8f):
+    pixels [..., 3 | 4] u8 -> f32 luma [...], (r_c r + g_c g) + b_c b rounded step by step."""
+    px = np.ascontiguousarray(pixels, np.uint8)
+    ch = px.shape[-1]
+    if ch not in (3, 4):
+        raise ValueError("pixels must end in 3 (RGB8) or 4 (RGBA8) channels")
+    n = px.size // ch
+    if n == 0:
+        return np.zeros(px.shape[:-1], np.float32)
+    d_px, d_out = ctx.to_device(px), ctx.alloc(n * 4)
+    r, g, b = (float(np.float32(c)) for c in coeffs)
+    check(ctx.lib.ypdq_cvt_luma8f(ctx.handle, d_px.ptr, n, ch, r, g, b, d_out.ptr, None))
+    ctx.sync()
+    return d_out.download(px.shape[:-1], np.float32)
+
+
 def scan_device(ctx, d_rows, n_rows, d_queries, n_queries, threshold, d_hits, capacity, d_count,
                 algo=_lib.SCAN_AUTO, stream=None):
     def dp(b):

@@ -113,24 +113,26 @@ int64_t jarosz_chunk(int64_t n) { return n < 2048 ? (n > 0 ? n : 1) : 2048; }
 // time when its end S_{c+1} (images counted from the start) satisfies
 // S_{c+1} u <= S_1 u + S_c v + c h, i.e. S_{c+1} <= S_1 + (v / u) S_c + c (h / u): chunks
 // grow geometrically by the compute/copy ratio, and only the first chunk's copy is exposed.
-// `ratio` is v / u and `chunk_images` h / u. Chunks are whole multiples of 32 images (whole
-// 256-query scan passes); the first is 32 images unless more than `max_chunks` chunks would
-// be needed. When copying is the longer stage (v / u <= 1) chunks still grow by h / u each,
-// since a chunk's fixed cost is then all its compute.
+// `ratio` is v / u and `chunk_images` h / u. Chunks are whole multiples of `granule` images
+// (whole scan passes: 32 images = 256 queries, or 64 = one pass of 512 queries taken in
+// pairs); the first is one granule unless more than `max_chunks` chunks would be needed.
+// When copying is the longer stage (v / u <= 1) chunks still grow by h / u each, since a
+// chunk's fixed cost is then all its compute.
 int plan_screen_chunks(int64_t n, double ratio, double chunk_images, int max_chunks,
-                       int64_t* bounds) {
+                       int64_t granule, int64_t* bounds) {
   const double r = std::min(2.0, std::max(1.0, ratio));
   const double h = std::min(256.0, std::max(0.0, chunk_images));
   bounds[0] = 0;
   if (n <= 0) return 0;
-  for (int64_t first = 32;; first *= 2) {
+  for (int64_t first = granule;; first *= 2) {
     int nch = 0;
-    int64_t end = n < first + 32 ? n : first;
+    int64_t end = n < first + granule ? n : first;
     bounds[++nch] = end;
     while (end < n && nch < max_chunks) {
       const double limit = static_cast<double>(first) + r * static_cast<double>(end) + nch * h;
-      int64_t next = std::max<int64_t>(end + 32, static_cast<int64_t>(limit) / 32 * 32);
-      if (next + 32 > n) next = n;  // no remainder smaller than 32 images
+      int64_t next =
+          std::max<int64_t>(end + granule, static_cast<int64_t>(limit) / granule * granule);
+      if (next + granule > n) next = n;  // no remainder smaller than a granule
       end = next;
       bounds[++nch] = end;
     }
@@ -144,9 +146,10 @@ struct ChunkCost {
   double fixed_us, per_image_us;
 };
 ChunkCost screen_chunk_cost(int input_kind, bool jarosz, uint64_t n_rows, uint32_t threshold) {
-  // the tensor-core scan: 11.5 T (row, query) pairs/s with the 128-bit prefix bound, 9.5 T
-  // with the 192-bit one, 8.3 T with all 256 bits; 8 queries per image
-  const double pairs_per_us = threshold <= 36 ? 11.5e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
+  // the tensor-core scan: 13.1 T (row, query) pairs/s in passes of 512 queries taken in
+  // pairs (the 128-bit prefix bound), 9.5 T with the 192-bit bound, 8.3 T with all 256
+  // bits; 8 queries per image
+  const double pairs_per_us = threshold <= 36 ? 13.1e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
   const double scan_us = 8.0 * static_cast<double>(n_rows) / pairs_per_us;
   // the Jarosz filter: four passes, each at least one line's sequential replay (512
   // dependent steps, ~5 us) however few images the chunk holds, plus the DCT
@@ -160,12 +163,15 @@ ChunkCost screen_chunk_cost(int input_kind, bool jarosz, uint64_t n_rows, uint32
 // The chunk plan of ypdq_screen_host (and ypdq_screen_plan).
 int screen_chunks(int64_t n, int input_kind, int dct_precision, uint64_t n_rows,
                   uint32_t threshold, int64_t* bounds) {
-  // pinned host memory copies at ~200 GB/s
-  const double copy_us = static_cast<double>(image_bytes_of(input_kind)) / 2.0e5;
+  // host memory reaches the device at ~211 GB/s on a GB300 host link, for copy-engine copies
+  // and SM loads from mapped or pageable memory alike
+  const double copy_us = static_cast<double>(image_bytes_of(input_kind)) / 2.11e5;
   const ChunkCost cost =
       screen_chunk_cost(input_kind, dct_precision == YPDQ_COMPRESS_JAROSZ, n_rows, threshold);
+  // at t <= 36 chunks of 64 images fill whole passes of the pair scan (512 queries)
+  const int64_t granule = threshold <= 36 ? 64 : 32;
   return plan_screen_chunks(n, 0.95 * cost.per_image_us / copy_us, 0.95 * cost.fixed_us / copy_us,
-                            ypdq_ctx::kMaxChunks, bounds);
+                            ypdq_ctx::kMaxChunks, granule, bounds);
 }
 
 ypdq_status ensure_jarosz_scratch(ypdq_ctx* ctx, int64_t chunk) {
@@ -203,6 +209,7 @@ ypdq_status ypdq_ctx_create(int device, ypdq_ctx** out) {
   if (e == cudaSuccess) e = upload_constants();
   if (e == cudaSuccess) e = scan_init();
   if (e == cudaSuccess) e = jarosz_init();
+  if (e == cudaSuccess) e = stages_init();
   if (e == cudaSuccess) e = hash_occupancy(0, &ctx->hash_ctas_f32);
   if (e == cudaSuccess) e = hash_occupancy(1, &ctx->hash_ctas_u8);
   for (int u = 0; u < 4 && e == cudaSuccess; ++u)
@@ -331,6 +338,70 @@ ypdq_status ypdq_hash_batch(ypdq_ctx* ctx, const void* d_images, int64_t n, int 
   CK(launch_hash(p, ctx->num_sms, ctx->hash_ctas[p.input_kind][dct][sep],
                  reinterpret_cast<cudaStream_t>(stream)),
      "hash kernel launch");
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_dct2d_batch(ypdq_ctx* ctx, const float* d_buf1, int64_t n, int stride,
+                             float* d_pdqf, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (n < 0) return fail(YPDQ_ERR_INVALID, "n < 0");
+  if (stride < 127) return fail(YPDQ_ERR_INVALID, "stride %d < 127", stride);
+  if (n > 0 && (!d_buf1 || !d_pdqf)) return fail(YPDQ_ERR_INVALID, "NULL buffer");
+  if (!aligned16(d_buf1) || !aligned16(d_pdqf))
+    return fail(YPDQ_ERR_ALIGN, "buffers must be 16-byte aligned");
+  CK(launch_dct2d(d_buf1, n, stride, d_pdqf, ctx->num_sms, reinterpret_cast<cudaStream_t>(stream)),
+     "dct2d launch");
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_sum_of_gradients_batch(ypdq_ctx* ctx, const float* d_pdqf, int64_t n,
+                                        float* d_out, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (n < 0) return fail(YPDQ_ERR_INVALID, "n < 0");
+  if (n > 0 && (!d_pdqf || !d_out)) return fail(YPDQ_ERR_INVALID, "NULL buffer");
+  if (!aligned16(d_pdqf)) return fail(YPDQ_ERR_ALIGN, "d_pdqf must be 16-byte aligned");
+  CK(launch_gradients(d_pdqf, n, d_out, reinterpret_cast<cudaStream_t>(stream)),
+     "gradients launch");
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_pdqf_transform_batch(ypdq_ctx* ctx, float* d_pdqf, int64_t n, int op,
+                                      int negate, int semantics, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (n < 0) return fail(YPDQ_ERR_INVALID, "n < 0");
+  if (n > 0 && !d_pdqf) return fail(YPDQ_ERR_INVALID, "d_pdqf is NULL");
+  if (op < YPDQ_PDQF_T || op > YPDQ_PDQF_NEGATE_OFF_DIAGONALS)
+    return fail(YPDQ_ERR_INVALID, "op %d", op);
+  if (semantics < YPDQ_DIHEDRAL_EXACT || semantics > YPDQ_DIHEDRAL_SCALAR)
+    return fail(YPDQ_ERR_INVALID, "semantics %d", semantics);
+  if (!aligned16(d_pdqf)) return fail(YPDQ_ERR_ALIGN, "d_pdqf must be 16-byte aligned");
+  const bool neg = negate != 0;
+  // bit i: row / column i negated
+  uint32_t rows = 0xFFFFu, cols = 0xFFFFu;
+  if (op == YPDQ_PDQF_NEGATE_ALT_ROWS)
+    rows = (semantics == YPDQ_DIHEDRAL_SCALAR) == neg ? 0xAAAAu : 0x5555u;
+  if (op == YPDQ_PDQF_NEGATE_ALT_COLS)
+    cols = (neg ? 0xAAAAu : 0x5555u) & (semantics == YPDQ_DIHEDRAL_AVX2 ? 0x00FFu : 0xFFFFu);
+  CK(launch_pdqf_op(d_pdqf, n, op, rows, cols, ctx->num_sms,
+                    reinterpret_cast<cudaStream_t>(stream)),
+     "pdqf transform launch");
+  return YPDQ_OK;
+}
+
+ypdq_status ypdq_cvt_luma8f(ypdq_ctx* ctx, const uint8_t* d_pixels, int64_t n_pixels,
+                            int channels, float r_coeff, float g_coeff, float b_coeff,
+                            float* d_out, ypdq_stream_t stream) {
+  ypdq_status st = check_ctx(ctx);
+  if (st) return st;
+  if (n_pixels < 0) return fail(YPDQ_ERR_INVALID, "n_pixels < 0");
+  if (channels != 3 && channels != 4) return fail(YPDQ_ERR_INVALID, "channels %d", channels);
+  if (n_pixels > 0 && (!d_pixels || !d_out)) return fail(YPDQ_ERR_INVALID, "NULL buffer");
+  CK(launch_luma(d_pixels, n_pixels, channels, r_coeff, g_coeff, b_coeff, d_out, ctx->num_sms,
+                 reinterpret_cast<cudaStream_t>(stream)),
+     "luma launch");
   return YPDQ_OK;
 }
 

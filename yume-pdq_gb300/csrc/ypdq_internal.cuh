@@ -224,6 +224,16 @@ cudaError_t launch_sort_hits(ypdq_hit* hits, uint64_t n, cudaStream_t s);
 cudaError_t scan_tc_init();
 cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s);
 
+// stages.cu: the Kernel trait's per-stage methods on n items
+cudaError_t stages_init();
+cudaError_t launch_dct2d(const float* buf, int64_t n, int stride, float* pdqf, int num_sms,
+                         cudaStream_t s);
+cudaError_t launch_gradients(const float* pdqf, int64_t n, float* out, cudaStream_t s);
+cudaError_t launch_pdqf_op(float* pdqf, int64_t n, int op, uint32_t row_mask, uint32_t col_mask,
+                           int num_sms, cudaStream_t s);
+cudaError_t launch_luma(const uint8_t* px, int64_t n, int channels, float rc, float gc, float bc,
+                        float* out, int num_sms, cudaStream_t s);
+
 // synth.cu
 cudaError_t launch_synth_rows(uint8_t* rows, uint64_t n, uint64_t first, uint64_t seed,
                               cudaStream_t s);

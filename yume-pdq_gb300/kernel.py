@@ -117,14 +117,47 @@ class CudaKernel:
     def adjust_quality(gradient_sum):
         return min(float(np.float32(gradient_sum) / np.float32(QUALITY_ADJUST_DIVISOR)), 1.0)
 
-    @staticmethod
-    def pdqf_t(pdqf):
-        pdqf[:] = pdqf.T.copy()
+    def dct2d(self, buffer, tmp_row_buffer, output):
+        """Kernel::dct2d (src/kernel/mod.rs:484): the compressed buffer (127x127, or the
+        reference's 128x128 padded Buffer1, first 127 rows and columns read) -> output
+        16x16 PDQF. tmp_row_buffer is the reference's scratch row and is left untouched."""
+        output[:] = core.dct2d_batch(self.ctx, np.asarray(buffer, np.float32)[None, :127])[0]
 
-    @staticmethod
-    def pdqf_negate_off_diagonals(pdqf):
-        i, j = np.indices((16, 16))
-        pdqf[((j - i) % 2) == 1] *= -1
+    def sum_of_gradients(self, input):
+        """Kernel::sum_of_gradients (src/kernel/mod.rs:469)."""
+        return float(core.sum_of_gradients_batch(self.ctx, np.asarray(input, np.float32)[None])[0])
+
+    def _pdqf_op(self, pdqf, op, negate=False):
+        pdqf[:] = core.pdqf_transform_batch(self.ctx, np.asarray(pdqf, np.float32)[None], op,
+                                            negate, self.semantics)[0]
+
+    def pdqf_t(self, input):
+        """Kernel::pdqf_t (src/kernel/mod.rs:345): transpose in place."""
+        self._pdqf_op(input, _lib.PDQF_T)
+
+    def pdqf_negate_alt_cols(self, input, negate=False):
+        """Kernel::pdqf_negate_alt_cols::<NEGATE> (src/kernel/mod.rs:368), in place, with
+        this kernel's sign convention (the AVX2 kernel touches columns 0..7 only)."""
+        self._pdqf_op(input, _lib.PDQF_NEGATE_ALT_COLS, negate)
+
+    def pdqf_negate_alt_rows(self, input, negate=False):
+        """Kernel::pdqf_negate_alt_rows::<NEGATE> (src/kernel/mod.rs:391), in place, with
+        this kernel's sign convention (the AVX2/AVX-512 kernels negate the other rows)."""
+        self._pdqf_op(input, _lib.PDQF_NEGATE_ALT_ROWS, negate)
+
+    def pdqf_negate_off_diagonals(self, input):
+        """Kernel::pdqf_negate_off_diagonals (src/kernel/mod.rs:413), in place."""
+        self._pdqf_op(input, _lib.PDQF_NEGATE_OFF_DIAGONALS)
+
+    def cvt_rgb8_to_luma8f(self, input, output, coeffs=core.BT601):
+        """Kernel::cvt_rgb8_to_luma8f (src/kernel/mod.rs:303): a row of RGB8 pixels
+        ([..., 3] u8) -> f32 luma in output."""
+        output[...] = core.cvt_luma8f(self.ctx, np.asarray(input, np.uint8)[..., :3], coeffs)
+
+    def cvt_rgba8_to_luma8f(self, input, output, coeffs=core.BT601):
+        """Kernel::cvt_rgba8_to_luma8f (src/kernel/mod.rs:324): RGBA8 ([..., 4] u8, alpha
+        ignored) -> f32 luma in output."""
+        output[...] = core.cvt_luma8f(self.ctx, np.asarray(input, np.uint8), coeffs)
 
 
 def hash_get_threshold(kernel, input, output, buf1, tmp, pdqf):
