@@ -623,6 +623,7 @@ def run_ours(args):
                        if serve else None),
         "batch_latency_ms": {"p50": 1000 * statistics.median(lat),
                              "p99": 1000 * float(np.percentile(lat, 99)),
+                             "all": [round(1000 * x, 3) for x in lat],
                              "at": "ypdq_screen_host of %d images" % B},
         "serving": serve,
         "scan_sweep": sweep,

@@ -145,6 +145,21 @@ const char *ypdq_last_error(void);
 /* Sticky device-side error flags (timeouts) raised by kernels of this context; clears them.
  * Blocks until the device is idle. */
 ypdq_status ypdq_check_device_errors(ypdq_ctx *ctx);
+/*
+ * Longest time a barrier wait inside the tensor-core scan kernels may take (default 4 s;
+ * 0 restores the default; at most 60 s), for scans launched afterwards by any context and
+ * by ypdq_screen_noalloc. A kernel whose wait runs out stops, sets the context's sticky
+ * timeout flag and returns; ypdq_stream_sync / ypdq_check_device_errors then report
+ * YPDQ_ERR_TIMEOUT (ypdq_screen_noalloc: *d_count = UINT64_MAX) and the context stays usable.
+ */
+ypdq_status ypdq_set_scan_wait_limit(uint64_t ns);
+/*
+ * Testing the timeout path: the next n tensor-core scan launches (any context) issue no
+ * database copies, so their other roles wait until the wait limit and give up as above.
+ * Nothing faults and no wait is unbounded. 0 cancels.
+ */
+ypdq_status ypdq_debug_stall_scans(int n);
+
 /* Number of SMs and the hash kernel's resident CTAs per SM (for sizing batches). */
 ypdq_status ypdq_device_info(ypdq_ctx *ctx, int *num_sms, int *hash_ctas_per_sm);
 /* CTAs per SM the hash kernel of this input kind and DCT precision runs with (its grid is
@@ -332,7 +347,9 @@ ypdq_status ypdq_event_elapsed_ms(ypdq_ctx *ctx, ypdq_event_t start, ypdq_event_
  * 4096 (larger n returns YPDQ_ERR_INVALID) and every GPU that loads the library holds
  * that array until exit. All calls share the array: calls that overlap on the GPU race,
  * so order them. The first call on a device sets it up there (symbol address, DCT table,
- * kernel attributes); make that call before any stream capture. Asynchronous on stream.
+ * kernel attributes); make that call before any stream capture. After cudaDeviceReset the
+ * next call sets it up again in the new context. d_images and d_rows must be 16-byte
+ * aligned, d_hits and d_count 8-byte aligned (YPDQ_ERR_ALIGN). Asynchronous on stream.
  */
 ypdq_status ypdq_screen_noalloc(const void *d_images, int64_t n, int input_kind, int semantics,
                                 const uint8_t *d_rows, uint64_t n_rows, uint32_t threshold,

@@ -2,8 +2,8 @@
  * A plain C consumer of the drop-in interface (include/yume_pdq.h), built by the tests with
  * gcc and linked against libyumepdq_gb300.so: it hashes two ramp images the way yume-pdq's
  * own C example does (pixel i holds i, then i + 1), visits the dihedrals of the second
- * through a C callback that stops after `stop_after` variants, and prints everything with
- * enough digits to compare bit for bit.
+ * through a C callback that asks to stop after `stop_after` variants (0: never), and prints
+ * everything with enough digits to compare bit for bit.
  *
  * usage: dropin_consumer [stop_after]
  */
@@ -30,7 +30,7 @@ static bool on_variant(void *ctx, uint32_t dihedral, float threshold, float qual
   print_hash(st->hash);
   printf("\n");
   st->seen++;
-  return st->seen < st->stop_after;
+  return st->stop_after <= 0 || st->seen < st->stop_after;
 }
 
 int main(int argc, char **argv) {
@@ -49,7 +49,7 @@ int main(int argc, char **argv) {
     print_hash(hash);
     printf("\n");
   }
-  struct visit_state st = {hash, pdqf, 0, argc > 1 ? atoi(argv[1]) : 7};
+  struct visit_state st = {hash, pdqf, 0, argc > 1 ? atoi(argv[1]) : 0};
   const bool done = yume_pdq_visit_dihedrals_smart_kernel(&st, threshold, hash, pdqf, on_variant);
   printf("visited %d completed %d\n", st.seen, done ? 1 : 0);
   printf("version %u.%u.%u %s\n", (unsigned)YUME_PDQ_VERSION_MAJOR,

@@ -344,3 +344,33 @@ def test_pair_kernel_matches_oracle(ctx, yp, oracle, n_q):
         for algo in (3, 0):  # YPDQ_SCAN_TC, YPDQ_SCAN_AUTO
             got = yp.scan(ctx, rows, q, t, algo=algo)
             assert np.array_equal(as_tuples(got), as_tuples(want)), (t, algo, len(got), len(want))
+
+
+@pytest.mark.parametrize("n_q", [64, 256, 300])
+def test_device_wait_timeout_is_reported_and_recovered(ctx, yp, oracle, n_q):
+    """The timeout path of the tensor-core scans (64 queries: two issuers and A in tensor
+    memory; 256: one pass; 300: the pair kernel). Under a 1 ms wait limit a launch whose
+    producer issues nothing (ypdq_debug_stall_scans) stops with its waits run out: the
+    stream sync reports YPDQ_ERR_TIMEOUT, and the next scan on the same context returns the
+    oracle's hits. No trap, no fault, no unbounded wait."""
+    lib = ctx.lib
+    rows = yp.synth.rows_128(50_000, seed=n_q + 70)
+    q = yp.synth.rows_128(n_q, seed=n_q + 71)
+    yp.synth.plant(rows, q, 200, 0, 31, seed=72)
+    d_rows, d_q = ctx.to_device(rows), ctx.to_device(q)
+    cap = 1 << 14
+    d_hits, d_cnt = ctx.alloc(cap * 16), ctx.alloc(8)
+    assert lib.ypdq_set_scan_wait_limit(1_000_000) == 0
+    try:
+        assert lib.ypdq_debug_stall_scans(1) == 0
+        yp.core.scan_device(ctx, d_rows, rows.shape[0], d_q, n_q, 31, d_hits, cap, d_cnt, 3)
+        with pytest.raises(yp.YpdqError) as err:
+            ctx.sync()
+        assert err.value.status == yp._lib.ERR_TIMEOUT
+    finally:
+        lib.ypdq_debug_stall_scans(0)
+        lib.ypdq_set_scan_wait_limit(0)
+    got = yp.scan(ctx, rows, q, 31, algo=3)
+    assert np.array_equal(as_tuples(got), as_tuples(oracle.find_all(rows, q, 31)))
+    assert lib.ypdq_set_scan_wait_limit(61 * 10 ** 9) == yp._lib.ERR_INVALID
+    assert lib.ypdq_debug_stall_scans(-1) == yp._lib.ERR_INVALID

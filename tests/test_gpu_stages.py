@@ -152,7 +152,7 @@ def parse_fields(line):
     return {toks[i]: toks[i + 1] for i in range(0, len(toks) - 1, 2)}
 
 
-@pytest.mark.parametrize("stop_after", [7, 3])
+@pytest.mark.parametrize("stop_after", [0, 3, 7])
 def test_c_consumer_against_oracle(yp, oracle, tmp_path, stop_after):
     """A gcc-built C program links the drop-in symbols (functions, the bool callback ABI,
     exported data symbols), hashes two ramp images and visits the dihedrals of the second;
@@ -171,12 +171,13 @@ def test_c_consumer_against_oracle(yp, oracle, tmp_path, stop_after):
         assert np.float32(f["buf1_0"]) == b[0, 0] and np.float32(f["pdqf0"]) == p[0, 0]
     dh, dt, dq, dp = oracle.dihedrals(p, t, sem)
     variants = [parse_fields(x) for x in out if x.startswith("variant")]
-    assert len(variants) == stop_after
+    assert len(variants) == (stop_after or 7)
     for v, f in enumerate(variants):
         assert int(f["dihedral"], 16) == yp.SLOT_DIHEDRALS[v + 1]
         assert np.float32(f["threshold"]) == np.float32(t)  # the outer threshold is passed
         assert np.float32(f["quality"]) == dq[v] and np.float32(f["pdqf0"]) == dp[v][0, 0]
         assert f["hash"] == dh[v].tobytes().hex()
-    assert ("visited %d completed %d" % (stop_after, 1 if stop_after == 7 else 0)) in out
+    # a callback that returns false stops the visit, which then returns false (src/lib.rs:358-420)
+    assert ("visited %d completed %d" % (stop_after or 7, 0 if stop_after else 1)) in out
     assert any(x.startswith("version 1.") for x in out)
     assert ("flipped %08x rotated_90 %08x" % (yp.Dihedrals.FLIPPED, yp.Dihedrals.ROTATED_90)) in out

@@ -122,6 +122,8 @@ SIGNATURES = {
     "ypdq_synth_clustered_rows": (i32, [P, P, u64, u64, u64, u32, u64, P]),
     "ypdq_constants": (i32, [P, P]),
     "ypdq_dropin_semantics": (i32, [ctypes.POINTER(ctypes.c_int)]),
+    "ypdq_set_scan_wait_limit": (i32, [u64]),
+    "ypdq_debug_stall_scans": (i32, [i32]),
     "ypdq_screen_noalloc": (i32, [P, i64, i32, i32, P, u64, u32, P, u64, P, P]),
     "ypdq_server_config_default": (i32, [ctypes.POINTER(ServerConfig)]),
     "ypdq_server_create": (i32, [P, P, ctypes.POINTER(ServerConfig), PP]),

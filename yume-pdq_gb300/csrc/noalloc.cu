@@ -15,11 +15,14 @@
 //     threads without ordering) race and corrupt each other's results; order them;
 //   * the first call on a device does a one-time set-up there: it resolves the array's
 //     device address (cudaGetSymbolAddress), uploads the DCT table and sets kernel
-//     attributes. Make that first call before any stream capture;
+//     attributes. Make that first call before any stream capture. The set-up belongs to
+//     the device's CUDA context: after cudaDeviceReset the next call (in the new context)
+//     does it again;
 //   * no cudaMalloc, cudaFree or allocating library routine is called.
 #include <cstdio>
 #include <mutex>
 
+#include "capi_internal.h"
 #include "ypdq_internal.cuh"
 
 namespace ypdq {
@@ -37,6 +40,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 struct DeviceState {
   bool ready = false;
+  unsigned long long context_id = 0;  // the CUDA context the set-up was done in
   uint8_t* hashes = nullptr;  // device address of g_noalloc_scratch on this device
   int* err = nullptr;
   int num_sms = 0;
@@ -47,7 +51,7 @@ struct DeviceState {
 static std::mutex g_mu;
 static DeviceState g_state[kMaxDevices];
 
-static ypdq_status fail(ypdq_status st, const char* msg, const char* detail = nullptr) {
+static ypdq_status fail_with(ypdq_status st, const char* msg, const char* detail = nullptr) {
   char buf[256];
   if (detail)
     snprintf(buf, sizeof(buf), "%s: %s", msg, detail);
@@ -57,22 +61,54 @@ static ypdq_status fail(ypdq_status st, const char* msg, const char* detail = nu
   return st;
 }
 
-// One-time set-up on the current device; host code may not use the array's name as an
-// address, so the device address comes from cudaGetSymbolAddress with that device current.
+// Unique id of the calling thread's current CUDA context (driver cuCtxGetCurrent and
+// cuCtxGetId, reached through the runtime's entry-point query so the library needs no
+// libcuda link), or 0 when it cannot be read. A context that cudaDeviceReset destroyed and
+// the runtime created again has a new id.
+static unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault,
+                                         nullptr) == cudaSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, nullptr) ==
+        cudaSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Set-up on the current device, once per CUDA context; host code may not use the array's
+// name as an address, so the device address comes from cudaGetSymbolAddress with that
+// device current.
 static ypdq_status setup(int dev, DeviceState** out) {
   std::lock_guard<std::mutex> lock(g_mu);
   DeviceState& s = g_state[dev];
+  // a new context (the device was reset) needs its own set-up; when the context cannot be
+  // identified, every call redoes it
+  const unsigned long long cid = current_context_id();
+  if (s.ready && (cid == 0 || cid != s.context_id)) s.ready = false;
   if (!s.ready) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return fail(YPDQ_ERR_CUDA, "cudaGetSymbolAddress", cudaGetErrorString(e));
+    if (e != cudaSuccess) return fail_with(YPDQ_ERR_CUDA, "cudaGetSymbolAddress", cudaGetErrorString(e));
     if ((e = upload_constants()) != cudaSuccess || (e = scan_init()) != cudaSuccess ||
         (e = cudaDeviceGetAttribute(&s.num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
         (e = hash_occupancy(0, &s.ctas_f32)) != cudaSuccess ||
         (e = hash_occupancy(1, &s.ctas_u8)) != cudaSuccess)
-      return fail(YPDQ_ERR_CUDA, "no-alloc set-up", cudaGetErrorString(e));
+      return fail_with(YPDQ_ERR_CUDA, "no-alloc set-up", cudaGetErrorString(e));
     s.hashes = static_cast<uint8_t*>(p);
     s.err = reinterpret_cast<int*>(static_cast<uint8_t*>(p) + kHashBytes);
+    s.context_id = current_context_id();
     s.ready = true;
   }
   *out = &s;
@@ -95,20 +131,24 @@ extern "C" ypdq_status ypdq_screen_noalloc(const void* d_images, int64_t n, int 
   using namespace ypdq;
   using namespace ypdq::noalloc;
   if (n < 0 || n > kMaxImages)
-    return fail(YPDQ_ERR_INVALID, "n out of range: ypdq_screen_noalloc takes 0..4096 images");
+    return fail_with(YPDQ_ERR_INVALID, "n out of range: ypdq_screen_noalloc takes 0..4096 images");
   if (input_kind != YPDQ_INPUT_F32 && input_kind != YPDQ_INPUT_U8)
-    return fail(YPDQ_ERR_INVALID, "input_kind must be YPDQ_INPUT_F32 or YPDQ_INPUT_U8");
+    return fail_with(YPDQ_ERR_INVALID, "input_kind must be YPDQ_INPUT_F32 or YPDQ_INPUT_U8");
   if (semantics < YPDQ_DIHEDRAL_EXACT || semantics > YPDQ_DIHEDRAL_SCALAR)
-    return fail(YPDQ_ERR_INVALID, "unknown dihedral semantics");
-  if (threshold > 256) return fail(YPDQ_ERR_INVALID, "threshold > 256");
+    return fail_with(YPDQ_ERR_INVALID, "unknown dihedral semantics");
+  if (threshold > 256) return fail_with(YPDQ_ERR_INVALID, "threshold > 256");
   if (!d_count || (n > 0 && !d_images) || (n_rows > 0 && !d_rows) || (capacity > 0 && !d_hits))
-    return fail(YPDQ_ERR_INVALID, "NULL argument");
+    return fail_with(YPDQ_ERR_INVALID, "NULL argument");
   if ((reinterpret_cast<uintptr_t>(d_images) & 15u) || (reinterpret_cast<uintptr_t>(d_rows) & 15u))
-    return fail(YPDQ_ERR_ALIGN, "images and rows must be 16-byte aligned");
+    return fail_with(YPDQ_ERR_ALIGN, "images and rows must be 16-byte aligned");
+  // the count takes 64-bit atomics and a memset; hits are stored as 16-byte records
+  if ((reinterpret_cast<uintptr_t>(d_count) & 7u) ||
+      (reinterpret_cast<uintptr_t>(d_hits) % alignof(ypdq_hit)))
+    return fail_with(YPDQ_ERR_ALIGN, "d_count and d_hits must be 8-byte aligned");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(YPDQ_ERR_CUDA, "cudaGetDevice", cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fail(YPDQ_ERR_UNSUPPORTED, "device ordinal too large");
+  if (e != cudaSuccess) return fail_with(YPDQ_ERR_CUDA, "cudaGetDevice", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return fail_with(YPDQ_ERR_UNSUPPORTED, "device ordinal too large");
   DeviceState* s = nullptr;
   ypdq_status st = setup(dev, &s);
   if (st != YPDQ_OK) return st;
@@ -122,8 +162,7 @@ extern "C" ypdq_status ypdq_screen_noalloc(const void* d_images, int64_t n, int 
     hp.images = d_images;
     hp.n = n;
     hp.input_kind = input_kind;
-    hp.row_mask = semantics == YPDQ_DIHEDRAL_SCALAR ? 0xAAAAu : 0x5555u;
-    hp.col_mask = semantics == YPDQ_DIHEDRAL_AVX2 ? 0x0055u : 0x5555u;
+    semantics_masks(semantics, &hp.row_mask, &hp.col_mask);
     hp.hashes = s->hashes;
     hp.pdqf_slots = 1;
     hp.dev_err = s->err;
@@ -146,6 +185,6 @@ extern "C" ypdq_status ypdq_screen_noalloc(const void* d_images, int64_t n, int 
     report_kernel<<<1, 1, 0, cs>>>(s->err, reinterpret_cast<unsigned long long*>(d_count));
     e = cudaGetLastError();
   }
-  if (e != cudaSuccess) return fail(YPDQ_ERR_CUDA, "ypdq_screen_noalloc", cudaGetErrorString(e));
+  if (e != cudaSuccess) return fail_with(YPDQ_ERR_CUDA, "ypdq_screen_noalloc", cudaGetErrorString(e));
   return YPDQ_OK;
 }

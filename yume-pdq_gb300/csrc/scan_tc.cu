@@ -46,6 +46,9 @@
 // scan's.
 #include <cuda_fp16.h>
 
+#include <atomic>
+
+#include "capi_internal.h"
 #include "ypdq_internal.cuh"
 
 namespace ypdq {
@@ -215,6 +218,8 @@ struct Params {
   uint32_t pack_offset;   // byte offset of the packed ring in shared memory
   uint32_t a_stages;      // expanded tiles in flight
   uint32_t b_offset;      // byte offset of the expanded queries
+  uint64_t wait_ns;       // longest barrier wait before the kernel gives up (timeout flag)
+  int stall;              // testing: the producer issues no copies, so the waits run out
 };
 
 __device__ __forceinline__ uint32_t popc256(uint4 a0, uint4 a1, uint4 b0, uint4 b1) {
@@ -361,13 +366,13 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
   }
 
   if (warp == kProducerWarp) {
-    if (lane == 0) {
+    if (lane == 0 && !prm.stall) {
       uint32_t slot = 0, phase = 0, issued = 0;
       bool ok = true;
       for (uint32_t p = 0; p < n_passes && ok; ++p) {
         for (uint64_t k = 0; k < my_tiles; ++k) {
           const uint64_t tile = blockIdx.x + k * gridDim.x;
-          if (!mbar_wait(&sm.pk_empty[slot], phase ^ 1u, abort_flag)) {
+          if (!mbar_wait(&sm.pk_empty[slot], phase ^ 1u, abort_flag, prm.wait_ns)) {
             ok = false;
             break;
           }
@@ -393,7 +398,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           const uint32_t ph = (k <= slot) ? phase : (phase ^ 1u);
           const uint64_t t0 = globaltimer_ns();
           while (!mbar_try_wait(&sm.pk_full[sl], ph))
-            if (globaltimer_ns() - t0 > kWaitLimitNs / 4) break;
+            if (globaltimer_ns() - t0 > prm.wait_ns / 4) break;
         }
       }
     }
@@ -408,7 +413,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
     uint32_t slot = 0, phase = 0, ga = 0, as_t = 0, aph_t = 0;  // as_t, aph_t: kDual stages
     for (uint32_t p = 0; p < n_passes; ++p) {
       // queries of this pass into B (N rows; padding rows are zero = contributes nothing)
-      if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag)) goto fail;
+      if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag, prm.wait_ns)) goto fail;
       for (uint32_t qr = e; qr < N; qr += 128) {
         const uint64_t qi = static_cast<uint64_t>(p) * N + qr;
         if (qi < n_queries) {
@@ -429,7 +434,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
       for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
         const uint32_t as = kDual ? as_t : ga % kAStages;
         const uint32_t aph = kDual ? aph_t : (ga / kAStages) & 1u;
-        if (!mbar_wait(&sm.pk_full[slot], phase, abort_flag)) goto fail;
+        if (!mbar_wait(&sm.pk_full[slot], phase, abort_flag, prm.wait_ns)) goto fail;
         const uint4* src = reinterpret_cast<const uint4*>(packed + slot * kPackBytes + arow * 32);
         const uint4 w0 = src[0], w1 = src[1];
         __syncwarp();
@@ -438,7 +443,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           slot = 0;
           phase ^= 1u;
         }
-        if (!mbar_wait(&sm.a_empty[as], aph ^ 1u, abort_flag)) goto fail;
+        if (!mbar_wait(&sm.a_empty[as], aph ^ 1u, abort_flag, prm.wait_ns)) goto fail;
         if constexpr (kDual) {
           __syncwarp();  // tcgen05.st is .sync.aligned: the lanes leave the wait one by one
           expand_row_tmem<kKSteps == 4>(w0, w1, tmem_base + a_lane + a_col0 + kACols * as);
@@ -476,7 +481,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
     bool ok = true;
     if (lane == 0) {
       for (uint32_t p = 0; p < n_passes && ok; ++p) {
-        if (!mbar_wait(&sm.b_full, p & 1u, abort_flag)) {
+        if (!mbar_wait(&sm.b_full, p & 1u, abort_flag, prm.wait_ns)) {
           ok = false;
           break;
         }
@@ -491,8 +496,8 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
           }
           if (kDual && (ga & 1u) != issuer) continue;
           const uint32_t ac = ga % kAccStages;
-          if (!mbar_wait(&sm.a_full[as], aph, abort_flag) ||
-              !mbar_wait(&sm.acc_empty[ac], ((ga / kAccStages) & 1u) ^ 1u, abort_flag)) {
+          if (!mbar_wait(&sm.a_full[as], aph, abort_flag, prm.wait_ns) ||
+              !mbar_wait(&sm.acc_empty[ac], ((ga / kAccStages) & 1u) ^ 1u, abort_flag, prm.wait_ns)) {
             ok = false;
             break;
           }
@@ -526,7 +531,10 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
       mma_commit(&sm.mma_done);
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(&sm.mma_done, 0))
-        if (globaltimer_ns() - t0 > kWaitLimitNs) break;
+        if (globaltimer_ns() - t0 > prm.wait_ns) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
     }
     __syncwarp();
     if (kDual && warp == kMmaWarp2) return;
@@ -535,10 +543,16 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
     {
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(&sm.epi_exit, 0))
-        if (globaltimer_ns() - t0 > kWaitLimitNs) break;
+        if (globaltimer_ns() - t0 > prm.wait_ns) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
       const uint64_t t1 = globaltimer_ns();
       while (!mbar_try_wait(&sm.exp_exit, 0))
-        if (globaltimer_ns() - t1 > kWaitLimitNs) break;
+        if (globaltimer_ns() - t1 > prm.wait_ns) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
     }
     tc_fence_after();
     tmem_dealloc(tmem_base, tmem_cols);
@@ -563,7 +577,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
         if (by_tile && (ga & 1u) != group) continue;
         const uint64_t tile = blockIdx.x + k * gridDim.x;
         const uint32_t ac = ga % kAccStages;
-        if (!mbar_wait(&sm.acc_full[ac], (ga / kAccStages) & 1u, abort_flag)) {
+        if (!mbar_wait(&sm.acc_full[ac], (ga / kAccStages) & 1u, abort_flag, prm.wait_ns)) {
           ok = false;
           break;
         }
@@ -732,13 +746,13 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
   }
 
   if (warp == kProducerWarp) {
-    if (lane == 0) {
+    if (lane == 0 && !prm.stall) {
       uint32_t slot = 0, phase = 0, issued = 0;
       bool ok = true;
       for (uint32_t p = 0; p < n_passes && ok; ++p) {
         for (uint64_t k = 0; k < my_tiles; ++k) {
           const uint64_t tile = blockIdx.x + k * gridDim.x;
-          if (!mbar_wait(&sm.pk_empty[slot], phase ^ 1u, abort_flag)) {
+          if (!mbar_wait(&sm.pk_empty[slot], phase ^ 1u, abort_flag, prm.wait_ns)) {
             ok = false;
             break;
           }
@@ -763,7 +777,7 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
           const uint32_t ph = (k <= slot) ? phase : (phase ^ 1u);
           const uint64_t t0 = globaltimer_ns();
           while (!mbar_try_wait(&sm.pk_full[sl], ph))
-            if (globaltimer_ns() - t0 > kWaitLimitNs / 4) break;
+            if (globaltimer_ns() - t0 > prm.wait_ns / 4) break;
         }
       }
     }
@@ -774,7 +788,7 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
     const int e = tid - kExpandWarp0 * 32;  // 0..127: tile row; pairs e and e + 128
     uint32_t slot = 0, phase = 0, ga = 0;
     for (uint32_t p = 0; p < n_passes; ++p) {
-      if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag)) goto fail;
+      if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag, prm.wait_ns)) goto fail;
       for (uint32_t j = e; j < static_cast<uint32_t>(kPairN); j += 128) {
         const uint64_t q0 = static_cast<uint64_t>(p) * kPairQueries + 2 * j;
         const uint4 zero = make_uint4(0, 0, 0, 0);
@@ -803,7 +817,7 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
       for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
         const uint32_t as = ga % kPairAStages;
         const uint32_t aph = (ga / kPairAStages) & 1u;
-        if (!mbar_wait(&sm.pk_full[slot], phase, abort_flag)) goto fail;
+        if (!mbar_wait(&sm.pk_full[slot], phase, abort_flag, prm.wait_ns)) goto fail;
         const uint4* src = reinterpret_cast<const uint4*>(packed + slot * kPackBytes + e * 32);
         const uint4 w0 = src[0], w1 = src[1];
         __syncwarp();
@@ -812,7 +826,7 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
           slot = 0;
           phase ^= 1u;
         }
-        if (!mbar_wait(&sm.a_empty[as], aph ^ 1u, abort_flag)) goto fail;
+        if (!mbar_wait(&sm.a_empty[as], aph ^ 1u, abort_flag, prm.wait_ns)) goto fail;
         expand_row<4, 0x3C3C3C3Cu>(w0, w1, a_smem + static_cast<size_t>(as) * kChunkBytes,
                                    nullptr, e);
         fence_proxy_async_smem();
@@ -838,7 +852,7 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
       uint32_t ga = 0;
       bool ok = true;
       for (uint32_t p = 0; p < n_passes && ok; ++p) {
-        if (!mbar_wait(&sm.b_full, p & 1u, abort_flag)) {
+        if (!mbar_wait(&sm.b_full, p & 1u, abort_flag, prm.wait_ns)) {
           ok = false;
           break;
         }
@@ -846,8 +860,8 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
         for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
           const uint32_t as = ga % kPairAStages;
           const uint32_t ac = ga % kAccStages;
-          if (!mbar_wait(&sm.a_full[as], (ga / kPairAStages) & 1u, abort_flag) ||
-              !mbar_wait(&sm.acc_empty[ac], ((ga / kAccStages) & 1u) ^ 1u, abort_flag)) {
+          if (!mbar_wait(&sm.a_full[as], (ga / kPairAStages) & 1u, abort_flag, prm.wait_ns) ||
+              !mbar_wait(&sm.acc_empty[ac], ((ga / kAccStages) & 1u) ^ 1u, abort_flag, prm.wait_ns)) {
             ok = false;
             break;
           }
@@ -863,7 +877,7 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
       mma_commit(&sm.mma_done);
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(&sm.mma_done, 0))
-        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+        if (globaltimer_ns() - t0 > prm.wait_ns) {
           raise_abort(sm, prm.dev_err);
           break;
         }
@@ -874,13 +888,13 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
     {
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(&sm.epi_exit, 0))
-        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+        if (globaltimer_ns() - t0 > prm.wait_ns) {
           raise_abort(sm, prm.dev_err);
           break;
         }
       const uint64_t t1 = globaltimer_ns();
       while (!mbar_try_wait(&sm.exp_exit, 0))
-        if (globaltimer_ns() - t1 > kWaitLimitNs) {
+        if (globaltimer_ns() - t1 > prm.wait_ns) {
           raise_abort(sm, prm.dev_err);
           break;
         }
@@ -905,7 +919,7 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
       for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
         const uint64_t tile = blockIdx.x + k * gridDim.x;
         const uint32_t ac = ga % kAccStages;
-        if (!mbar_wait(&sm.acc_full[ac], (ga / kAccStages) & 1u, abort_flag)) {
+        if (!mbar_wait(&sm.acc_full[ac], (ga / kAccStages) & 1u, abort_flag, prm.wait_ns)) {
           ok = false;
           break;
         }
@@ -1007,6 +1021,8 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   prm.dev_err = p.dev_err;
   prm.query_base = p.query_base;
   prm.nq_dev = p.nq_dev;
+  prm.wait_ns = scan_wait_limit_ns();
+  prm.stall = take_scan_stall() ? 1 : 0;
   // at a small threshold the first 128 bits bound the distance (kKSteps = 4)
   const bool half_k = p.threshold <= 36;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
@@ -1067,4 +1083,31 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+namespace {
+std::atomic<uint64_t> g_scan_wait_ns{kWaitLimitNs};
+std::atomic<int> g_scan_stalls{0};
+}  // namespace
+
+uint64_t scan_wait_limit_ns() { return g_scan_wait_ns.load(std::memory_order_relaxed); }
+
+bool take_scan_stall() {
+  int n = g_scan_stalls.load();
+  while (n > 0)
+    if (g_scan_stalls.compare_exchange_weak(n, n - 1)) return true;
+  return false;
+}
+
 }  // namespace ypdq
+
+extern "C" ypdq_status ypdq_set_scan_wait_limit(uint64_t ns) {
+  if (ns > 60ull * 1000 * 1000 * 1000)
+    return ypdq::fail(YPDQ_ERR_INVALID, "wait limit %llu ns > 60 s", (unsigned long long)ns);
+  ypdq::g_scan_wait_ns.store(ns ? ns : ypdq::kWaitLimitNs);
+  return YPDQ_OK;
+}
+
+extern "C" ypdq_status ypdq_debug_stall_scans(int n) {
+  if (n < 0) return ypdq::fail(YPDQ_ERR_INVALID, "n < 0");
+  ypdq::g_scan_stalls.store(n);
+  return YPDQ_OK;
+}

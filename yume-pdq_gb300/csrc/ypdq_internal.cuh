@@ -58,15 +58,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Wait for the phase with the given parity. Gives up (returns false) when *abort_flag is
-// set by another warp or when kWaitLimitNs passes; the caller then raises the error.
+// set by another warp or when limit_ns passes; the caller then raises the error.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
-                                          const volatile int* abort_flag) {
+                                          const volatile int* abort_flag,
+                                          uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
-    if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    if (globaltimer_ns() - t0 > limit_ns) return false;
   }
 }
 
@@ -222,6 +223,10 @@ cudaError_t launch_sort_hits(ypdq_hit* hits, uint64_t n, cudaStream_t s);
 
 // scan_tc.cu
 cudaError_t scan_tc_init();
+// Wait limit of the tensor-core scan kernels and the number of their next launches whose
+// producer issues nothing (ypdq_set_scan_wait_limit, ypdq_debug_stall_scans)
+uint64_t scan_wait_limit_ns();
+bool take_scan_stall();
 cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s);
 
 // stages.cu: the Kernel trait's per-stage methods on n items
