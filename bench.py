@@ -167,6 +167,11 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+# DRAM bytes (read + write) per 512-query pass of the pair scan over 10M rows: an ncu
+# capture of one launch of 4 passes (2,048 queries, t = 31) read 1.2797 GB and wrote 3.4 MB.
+NCU_DRAM_BYTES_PER_PASS_10M = (1.2797e9 + 3.4e6) / 4
+
+
 def fp8_dense_burst(device=0, n=8192, reps=10):
     """Dense FP8 (e4m3) tensor-core rate of this GPU in TFLOP/s: torch._scaled_mm of two
     n x n e4m3 matrices (per-tensor unit scales, bf16 out), best of `reps` launches timed
@@ -576,7 +581,11 @@ def run_ours(args):
                     "peak_source": ("measured fp8 burst (torch._scaled_mm e4m3 8192^3, best of "
                                     "10, this GPU, this run)" if fp8 else
                                     "%s bf16 burst x 2 (fp8 dense)" % peak_kind),
-                    "traffic": None,
+                    "traffic": (passes * NCU_DRAM_BYTES_PER_PASS_10M * (n / 1e7)
+                                + hits_per_step * 16.0 if pairs else None),
+                    "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a "
+                                       "4-pass launch over 10M rows (1.283 GB) per pass, scaled "
+                                       "by this launch's passes and rows" if pairs else None),
                     "traffic_computed": passes * 32.0 * n + hits_per_step * 16.0,
                     "traffic_note": "traffic_computed = 32 B x rows x %d query passes of %d + 16 B "
                                     "per hit (the database streams once per pass), computed, not "
