@@ -60,6 +60,20 @@ def parse():
                     help="1: time and check the FP32 / TF32 / BF16x3 hash variants")
     ap.add_argument("--peaks", action="store_true",
                     help="only measure the dense FP8 burst of GPU 0 and print it as JSON")
+    ap.add_argument("--kernel", choices=["hash", "scan"],
+                    help="only time one kernel configuration with CUDA events and print one "
+                         "line per repetition (for profiling): `hash` runs ypdq_hash_batch on "
+                         "--images device-resident images of --input kind with --dct (plus "
+                         "--separable / --jarosz); `scan` runs ypdq_scan of --queries random "
+                         "hashes against --db-rows generated rows with --algo at --threshold")
+    ap.add_argument("--input", choices=["f32", "u8", "rgb8", "rgba8"], default="f32")
+    ap.add_argument("--images", type=int, default=4096)
+    ap.add_argument("--separable", action="store_true",
+                    help="with --kernel hash: YPDQ_COMPRESS_SEPARABLE (not bit-exact)")
+    ap.add_argument("--jarosz", action="store_true",
+                    help="with --kernel hash: YPDQ_COMPRESS_JAROSZ (ReferenceKernel<f32>)")
+    ap.add_argument("--queries", type=int, default=64)
+    ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--ranks-only", action="store_true",
                     help="only join the replicas' process group and print this rank's view "
                          "(tests the multi-process launch without a GPU)")
@@ -775,8 +789,68 @@ def run_reference(args):
     }))
 
 
+def kernel_mode(args):
+    """One kernel configuration timed with CUDA events, one line per repetition (the first
+    includes first-launch costs). Hash: 64 distinct seeded images repeated to --images;
+    scan: --queries random 128-bit hashes against ypdq_synth_rows(seed 1)."""
+    import ctypes
+    import __graft_entry__ as g
+    yp = g.load_package()
+    ctx = yp.Context(0)
+    stream = ctx.stream()
+    e0, e1 = ctx.event(), ctx.event()
+    if args.kernel == "hash":
+        kind = {"f32": yp._lib.INPUT_F32, "u8": yp._lib.INPUT_U8, "rgb8": yp._lib.INPUT_RGB8,
+                "rgba8": yp._lib.INPUT_RGBA8}[args.input]
+        if kind in (yp._lib.INPUT_RGB8, yp._lib.INPUT_RGBA8):
+            ch = 3 if kind == yp._lib.INPUT_RGB8 else 4
+            base = np.concatenate([yp.synth.color_images(16, seed=3, channels=ch)] * 4)
+        else:
+            base = yp.synth.blob_images(64, seed=3)
+            if kind == yp._lib.INPUT_U8:
+                base = yp.synth.to_u8(base)
+        d_img = ctx.to_device(np.concatenate([base] * ((args.images + 63) // 64))[: args.images])
+        d_h, d_q = ctx.alloc(args.images * 256), ctx.alloc(args.images * 32)
+        prec = 0x200 if args.jarosz else args.dct | (0x100 if args.separable else 0)
+        if not args.jarosz:
+            c = ctypes.c_int()
+            yp._lib.check(ctx.lib.ypdq_hash_occupancy(ctx.handle, kind, prec, ctypes.byref(c)))
+            print("hash_kernel input %s dct %d separable %d: %d CTAs per SM"
+                  % (args.input, args.dct, args.separable, c.value))
+        for _ in range(args.reps):
+            ctx.record(e0, stream)
+            yp.core.hash_batch_device(ctx, d_img, args.images, kind, d_h, d_q, dct=prec,
+                                      stream=stream)
+            ctx.record(e1, stream)
+            ctx.sync(stream)
+            ms = ctx.elapsed_ms(e0, e1)
+            print("images %d ms %.4f Mimg/s %.3f" % (args.images, ms, args.images / ms / 1e3),
+                  flush=True)
+    else:
+        n = args.db_rows
+        d_rows = ctx.alloc(n * 32)
+        yp._lib.check(ctx.lib.ypdq_synth_rows(ctx.handle, d_rows.ptr, n, 0, 1, None))
+        d_q = ctx.to_device(yp.synth.rows_128(args.queries, seed=5))
+        cap = 1 << 20
+        d_hits, d_cnt = ctx.alloc(cap * 16), ctx.alloc(8)
+        for _ in range(args.reps):
+            ctx.record(e0, stream)
+            yp.core.scan_device(ctx, d_rows, n, d_q, args.queries, args.threshold, d_hits, cap,
+                                d_cnt, args.algo, stream)
+            ctx.record(e1, stream)
+            ctx.sync(stream)
+            ms = ctx.elapsed_ms(e0, e1)
+            print("rows %d queries %d ms %.4f Gpairs/s %.1f DB GB/s %.1f"
+                  % (n, args.queries, ms, n * args.queries / ms / 1e6, n * 32 / ms / 1e6),
+                  flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.kernel:
+        kernel_mode(args)
+        return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     if args.peaks:
         print(json.dumps({"fp8_e4m3_dense_tflops": fp8_dense_burst(),

@@ -2,122 +2,30 @@
 """Generate ``oracle/ypdq_constants.h``: the PDQ constant tables at 128-bit precision.
 
 TEST INFRASTRUCTURE. Only the oracle and the tests use the header this script writes.
-The CUDA library derives its own tables at context creation (FP64 cosine, f32 tent
-weights). A CPU test checks that those tables equal the ones below bit for bit.
 
-This restates the constant generation in yume-pdq's build script, which runs in
-MPFR at 128 bits and rounds once to f32/f64:
-
-* DCT matrix ``D[i-1][j] = sqrt(2/127) * cos(pi / (2*127) * i * (2j + 1))`` for i in 1..=16,
-  j in 0..127. The order of operations follows ``d_value`` in build.rs:316-325. The rows are
-  written out for ``i = 1..=16`` in build.rs:591-602 (f32) and build.rs:625-637 (f64).
-* Tent filter: the 7x7 impulse response of two passes of the 3-wide pdqhash box filter.
-  The filter truncates its window at the edges, as ``mean_box::box_one_d_float`` does in
-  build.rs:203-261. It is measured at the centre pixel, following
-  ``tent_filter_weights`` (build.rs:334-381, asserted 7x7 with offset 3 at build.rs:652).
-* Sample offsets ``round(4 * (i + 1))`` from ``lerp(0, 512, i, 127)``
-  (build.rs:383-387, build.rs:771-773).
-
-mpmath stands in for MPFR: both round each operation to nearest at a 128-bit mantissa.
-Each value is then rounded once, directly from 128 bits to 24 or 53 bits, so no value
-is rounded twice.
+The tables come from the library's one generator, ``yume-pdq_gb300/csrc/gen_tables.py``
+(imported here), which restates the 128-bit MPFR construction of yume-pdq's build script
+(build.rs:203-387, 557-643): the DCT matrix rounded once to f32 and f64, the 7x7 tent
+weights and the 127 sample offsets. This script adds the f64 DCT matrix the FP64 oracle
+needs and writes the oracle's header format. Generating both headers from one
+implementation means the equality of the two f32 tables (test_constants_pinned) is a
+check of the build, not of the construction; what checks the construction independently
+is the closed-form comparison (test_constants_closed_form) and the README known-answer
+vector, which the oracle reproduces to 0 bits.
 """
+import importlib.util
 import os
 import sys
 
-import mpmath
-from mpmath import mp, mpf
+from mpmath import mp
 
-PREC = 128
-
-
-def round_to_bits(x, bits):
-    """Round an mpf once to a ``bits``-bit mantissa (round to nearest even) and return a float."""
-    with mpmath.workprec(bits):
-        y = +x
-    return float(y)
-
-
-def f32_bits(x):
-    import struct
-    v = round_to_bits(x, 24)
-    return struct.unpack("<I", struct.pack("<f", v))[0], v
-
-
-def f64_bits(x):
-    import struct
-    v = round_to_bits(x, 53)
-    return struct.unpack("<Q", struct.pack("<d", v))[0], v
-
-
-def d_value(i, j, n):
-    # build.rs:316-325: (two / n).sqrt() * (pi / (two * n) * i * (two * j + one)).cos()
-    n1, i1, j1 = mpf(n), mpf(i), mpf(j)
-    one = mpf(1)
-    two = one + one
-    pi = mp.pi
-    return mpmath.sqrt(two / n1) * mpmath.cos(pi / (two * n1) * i1 * (two * j1 + one))
-
-
-def box_one_d(invec, start, outvec, length, stride, full_window):
-    """Restates the edge-truncated running box mean of build.rs:203-261."""
-    half = (full_window + 2) // 2
-    p1 = half - 1
-    p2 = full_window - half + 1
-    oi_off = p1 * stride
-    li_off = p2 * stride
-    s = mpf(0)
-    cur = mpf(0)
-    p1_end = oi_off + start
-    for ri in range(start, p1_end, stride):
-        s += invec[ri]
-        cur += 1
-    p2_end = full_window * stride + start
-    for ri in range(p1_end, p2_end, stride):
-        oi = ri - oi_off
-        s += invec[ri]
-        cur += 1
-        outvec[oi] = s / cur
-    p3_end = length * stride + start
-    for ri in range(p2_end, p3_end, stride):
-        oi = ri - oi_off
-        li = oi - li_off
-        s += invec[ri]
-        s -= invec[li]
-        outvec[oi] = s / cur
-    p4_start = (length - half + 1) * stride + start
-    for oi in range(p4_start, p3_end, stride):
-        li = oi - li_off
-        s -= invec[li]
-        cur -= 1
-        outvec[oi] = s / cur
-
-
-def jarosz(buf, rows, cols, wr, wc, nreps):
-    """build.rs:283-303: nreps x (box along rows, then box along columns)."""
-    tmp = [mpf(0)] * len(buf)
-    for _ in range(nreps):
-        for i in range(rows):
-            box_one_d(buf, i * cols, tmp, cols, 1, wr)
-        for j in range(cols):
-            box_one_d(tmp, j, buf, rows, cols, wc)
-
-
-def tent_weights(old_dim=512, new_dim=127):
-    window = -(-old_dim // (2 * new_dim))  # div_ceil, build.rs:310-312
-    er = ec = 2 * window + 1
-    out = [mpf(0)] * (er * ec)
-    for di in range(er):
-        for dj in range(ec):
-            tmp = [mpf(0)] * (er * ec)
-            tmp[di * ec + dj] = mpf(1)
-            total = sum(tmp, mpf(0))
-            tmp = [x / total for x in tmp]
-            jarosz(tmp, er, ec, window, window, 2)
-            mid = tmp[window * ec + window]
-            if float(mid) > 0.0:
-                out[di * ec + dj] = mid
-    return (ec - 1) // 2, er, ec, out
+_GEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), os.pardir, "yume-pdq_gb300",
+                    "csrc", "gen_tables.py")
+_spec = importlib.util.spec_from_file_location("ypdq_gen_tables", _GEN)
+gen = importlib.util.module_from_spec(_spec)
+_spec.loader.exec_module(gen)
+PREC, d_value, f32_bits, f64_bits, tent_weights = (gen.PREC, gen.d_value, gen.f32_bits,
+                                                   gen.f64_bits, gen.tent_weights)
 
 
 def main(path):

@@ -73,7 +73,8 @@ def test_avx2_kernel_agrees_with_default(oracle, yp):
 
 
 def test_constants_pinned(oracle, yp):
-    """The oracle's 128-bit tables equal the tables compiled into the library."""
+    """The oracle's tables equal the ones compiled into the library (both headers come from
+    one generator: this checks that library and oracle were built from the same tables)."""
     import ctypes
     lib = yp._lib.load()
     dct = np.empty(16 * 127, np.float32)

@@ -2,8 +2,10 @@
 """Generate ``ypdq_tables.h``: the f32 constant tables compiled into the CUDA library.
 
 This is a build step of the library. Its output is committed because the build
-machines have no arbitrary-precision package. A CPU test checks the tables bit for bit
-against the oracle's independently generated copy.
+machines have no arbitrary-precision package. The oracle's header (oracle/ypdq_constants.h,
+with the f64 matrix too) is generated from the same functions by oracle/gen_constants.py;
+the construction itself is checked against the closed form and the README known-answer
+vector.
 
 This restates the constant generation in yume-pdq's build script, which runs in
 MPFR at 128 bits and rounds once to f32/f64:
