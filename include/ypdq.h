@@ -425,7 +425,9 @@ typedef struct {
   uint32_t bucket_n_tile[YPDQ_SERVER_MAX_BUCKETS];  /* tensor-core queries per pass (0: SIMT) */
   float bucket_ms[YPDQ_SERVER_MAX_BUCKETS];         /* step time measured by the autotuner */
   uint64_t bucket_steps[YPDQ_SERVER_MAX_BUCKETS];   /* steps launched per bucket */
-  uint32_t bucket_pair[YPDQ_SERVER_MAX_BUCKETS];    /* 1: two queries per accumulator column */
+  uint32_t bucket_kernel[YPDQ_SERVER_MAX_BUCKETS];  /* tensor-core scan form: 0 one query per
+                                                       accumulator column, 1 two per column,
+                                                       2 queries as the MMA's A operand */
 } ypdq_server_stats;
 
 /* Fills cfg with the defaults above (threshold 31, f32 input, FP32 DCT, exact semantics). */

@@ -374,3 +374,20 @@ def test_device_wait_timeout_is_reported_and_recovered(ctx, yp, oracle, n_q):
     assert np.array_equal(as_tuples(got), as_tuples(oracle.find_all(rows, q, 31)))
     assert lib.ypdq_set_scan_wait_limit(61 * 10 ** 9) == yp._lib.ERR_INVALID
     assert lib.ypdq_debug_stall_scans(-1) == yp._lib.ERR_INVALID
+
+
+@pytest.mark.parametrize("n_q", [1, 2, 31, 33, 64, 100, 127, 128])
+def test_rows_kernel_matches_oracle(ctx, yp, oracle, n_q):
+    """Up to 128 queries the tensor-core scan takes the queries as the MMA's A operand and
+    256 database rows per MMA. Row counts that end mid-tile, rows equal or complementary to
+    a query, several planted rows per 64-row chunk, and thresholds on both sides of each
+    prefix-bound switch (36 / 37, 62 / 63) and at the range's ends."""
+    rows = yp.synth.rows_128(6001, seed=n_q + 500)
+    q = yp.synth.rows_128(n_q, seed=n_q + 501)
+    yp.synth.plant(rows, q, min(600, 6001), 0, 70, seed=n_q)
+    rows[5996], rows[5997] = q[0], ~q[n_q - 1]   # the last, partial tile
+    rows[300:310] = q[np.arange(10) % n_q]       # ten hits in one 64-row chunk
+    for t in (0, 1, 16, 31, 36, 37, 48, 62, 63, 90, 128, 255, 256):
+        want = oracle.find_all(rows, q, t)
+        got = yp.scan(ctx, rows, q, t, algo=3, capacity=1 << 20)
+        assert np.array_equal(as_tuples(got), as_tuples(want)), (t, len(got), len(want))

@@ -74,7 +74,7 @@ class ServerStats(ctypes.Structure):
                 ("bucket_n_tile", ctypes.c_uint32 * SERVER_MAX_BUCKETS),
                 ("bucket_ms", ctypes.c_float * SERVER_MAX_BUCKETS),
                 ("bucket_steps", ctypes.c_uint64 * SERVER_MAX_BUCKETS),
-                ("bucket_pair", ctypes.c_uint32 * SERVER_MAX_BUCKETS)]
+                ("bucket_kernel", ctypes.c_uint32 * SERVER_MAX_BUCKETS)]
 
 
 # name -> (restype, argtypes); the exported surface of include/*.h

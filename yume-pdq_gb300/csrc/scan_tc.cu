@@ -984,6 +984,323 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// scan_rows_kernel: narrow passes (<= 128 queries) with the operands swapped.
+//
+// The queries are the MMA's A operand (M = 128 rows; a query past the end is a zero row,
+// whose dot products are 0 and never reach dot_min) and the database tiles its B operand,
+// N = 256 rows per MMA. An M = 128, K = 32 MMA costs ~120 clk whatever its N up to 128 and
+// ~128 clk at N = 256, so scan_tc_kernel's narrow passes (N = 64 queries, 128 rows per MMA)
+// pay four times the MMA instructions per database row that these do. The accumulator of a
+// tile is 128 lanes (queries) x 256 columns (rows), f16 as in scan_tc_kernel (two stages);
+// epilogue warp w reads queries 32 (w % 4) .. + 31 (its lanes) and rows 128 (w / 4) .. + 127
+// as two 64-column loads. A candidate column becomes a 64-row mask per lane, re-checked with
+// popcounts of the packed row and the lane's query (emit_rows). The queries are expanded
+// once per launch; each 256-row tile is expanded once (two rows per expander thread).
+// Roles: warps 0-7 epilogue, 8 producer (bulk copies of 8 KiB packed tiles), 9 MMA and
+// TMEM allocation, 10-13 expanders.
+constexpr int kRowsN = 256;                  // database rows per tile (MMA N)
+// expanded tiles in shared memory: 3 of 32 KiB (128-bit prefix) or 2 of 64 KiB
+__host__ __device__ constexpr int rows_b_stages(int k_steps) { return k_steps > 4 ? 2 : 3; }
+constexpr int kRowsPackBytes = kRowsN * 32;  // one packed tile
+constexpr int kRowsChunkBytes = kRowsN * 128;  // one 128-byte K-chunk of an expanded tile
+constexpr int kRowsMaxQueries = kTileRows;   // queries per launch (MMA M)
+
+// Report the candidate rows of one lane (bit j of cand: row row0 + j against the lane's
+// query q): the exact distance of each from popcounts, hits within the threshold written at
+// positions taken with one atomic per warp. Called by all 32 lanes; a lane without
+// candidates passes cand = 0.
+__device__ __forceinline__ void emit_rows(uint64_t cand, uint64_t row0, uint32_t q,
+                                          const Params& prm, int lane) {
+  if (row0 >= prm.n_rows) {
+    cand = 0;
+  } else if (prm.n_rows - row0 < 64) {
+    cand &= (1ull << (prm.n_rows - row0)) - 1;
+  }
+  uint4 q0 = make_uint4(0, 0, 0, 0), q1 = q0;
+  if (cand) {
+    const uint4* qp = reinterpret_cast<const uint4*>(prm.queries + static_cast<uint64_t>(q) * 32);
+    q0 = __ldg(qp);
+    q1 = __ldg(qp + 1);
+  }
+  uint64_t hits = 0;
+  for (uint64_t m = cand; m; m &= m - 1) {
+    const int j = __ffsll(static_cast<long long>(m)) - 1;
+    const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + (row0 + j) * 32);
+    if (popc256(__ldg(rp), __ldg(rp + 1), q0, q1) <= prm.threshold) hits |= 1ull << j;
+  }
+  const uint32_t mine = static_cast<uint32_t>(__popcll(hits));
+  uint32_t incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total == 0) return;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(prm.count, static_cast<unsigned long long>(total));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  uint64_t pos = base + incl - mine;
+  for (uint64_t m = hits; m; m &= m - 1, ++pos) {
+    if (pos >= prm.capacity) break;
+    const int j = __ffsll(static_cast<long long>(m)) - 1;
+    const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + (row0 + j) * 32);
+    ypdq_hit h;
+    h.index = row0 + j;
+    h.query = q + prm.query_base;
+    h.distance = popc256(__ldg(rp), __ldg(rp + 1), q0, q1);
+    prm.hits[pos] = h;
+  }
+}
+
+template <int kKSteps>
+__global__ void __launch_bounds__(threads_of(false), 1) scan_rows_kernel(const Params prm) {
+  static_assert(kKSteps == 4 || kKSteps == 6 || kKSteps == 8, "K steps");
+  constexpr int kChunks = kKSteps > 4 ? 2 : 1;  // 128-byte K-chunks per expanded row
+  constexpr int kRowsBStages = rows_b_stages(kKSteps);
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* const smem_base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  Smem& sm = *reinterpret_cast<Smem*>(smem_base);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t n_pack = prm.pack_stages;
+  const uint32_t n_queries = prm.nq_dev ? min(*prm.nq_dev, prm.n_queries) : prm.n_queries;
+  uint8_t* const q_smem = smem_base + kFixedBytes;                  // [kChunks][128 x 128 B]
+  uint8_t* const b_smem = q_smem + kChunks * kChunkBytes;           // [stages][kChunks][32 KB]
+  uint8_t* const packed = smem_base + prm.pack_offset;
+  const uint64_t n_tiles = (prm.n_rows + kRowsN - 1) / kRowsN;
+  const uint64_t my_tiles =
+      blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  volatile int* abort_flag = &sm.abort_flag;
+
+  if (tid == 0) {
+    for (uint32_t s = 0; s < n_pack; ++s) {
+      mbar_init(&sm.pk_full[s], 1);
+      mbar_init(&sm.pk_empty[s], 4);
+    }
+    for (int s = 0; s < kRowsBStages; ++s) {
+      mbar_init(&sm.a_full[s], 4);   // expanded tile stage s is ready
+      mbar_init(&sm.a_empty[s], 1);  // the MMAs reading it have completed
+    }
+    for (int s = 0; s < kAccStages; ++s) {
+      mbar_init(&sm.acc_full[s], 1);
+      mbar_init(&sm.acc_empty[s], kEpilogueWarps);
+    }
+    mbar_init(&sm.b_full, 4);  // the queries are expanded
+    mbar_init(&sm.epi_exit, kEpilogueWarps);
+    mbar_init(&sm.exp_exit, 4);
+    mbar_init(&sm.mma_done, 1);
+    sm.abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == kMmaWarp) {
+    tmem_alloc(&sm.tmem_base, kTmemCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = sm.tmem_base;
+  if (my_tiles == 0 || n_queries == 0) {
+    if (warp == kMmaWarp) tmem_dealloc(tmem_base, kTmemCols);
+    return;
+  }
+
+  if (warp == kProducerWarp) {
+    if (lane == 0 && !prm.stall) {
+      uint32_t slot = 0, phase = 0, issued = 0;
+      bool ok = true;
+      for (uint64_t k = 0; k < my_tiles; ++k) {
+        const uint64_t tile = blockIdx.x + k * gridDim.x;
+        if (!mbar_wait(&sm.pk_empty[slot], phase ^ 1u, abort_flag, prm.wait_ns)) {
+          ok = false;
+          break;
+        }
+        const uint64_t r0 = tile * kRowsN;
+        const uint64_t nr = (prm.n_rows - r0) < kRowsN ? (prm.n_rows - r0) : kRowsN;
+        const uint32_t bytes = static_cast<uint32_t>(nr * 32);
+        mbar_arrive_expect_tx(&sm.pk_full[slot], bytes);
+        bulk_g2s(packed + slot * kRowsPackBytes, prm.rows + r0 * 32, bytes, &sm.pk_full[slot],
+                 policy_evict_first());
+        ++issued;
+        if (++slot == n_pack) {
+          slot = 0;
+          phase ^= 1u;
+        }
+      }
+      if (!ok) {
+        raise_abort(sm, prm.dev_err);
+        // let the copies already issued land (bounded), as in scan_tc_kernel
+        for (uint32_t k = 1; k <= n_pack && k <= issued; ++k) {
+          const uint32_t sl = (slot + n_pack - k) % n_pack;
+          const uint32_t ph = (k <= slot) ? phase : (phase ^ 1u);
+          const uint64_t t0 = globaltimer_ns();
+          while (!mbar_try_wait(&sm.pk_full[sl], ph))
+            if (globaltimer_ns() - t0 > prm.wait_ns / 4) break;
+        }
+      }
+    }
+    return;
+  }
+
+  if (warp >= kExpandWarp0 && warp < kExpandWarp0 + 4) {
+    const int e = tid - kExpandWarp0 * 32;  // 0..127: query e; tile rows e and e + 128
+    uint8_t* const q1 = q_smem + (kChunks > 1 ? kChunkBytes : 0);
+    if (static_cast<uint32_t>(e) < n_queries) {
+      const uint4* src = reinterpret_cast<const uint4*>(prm.queries + static_cast<uint64_t>(e) * 32);
+      expand_row<kKSteps>(src[0], src[1], q_smem, q1, e);
+    } else {
+      for (int c = 0; c < kChunks; ++c)
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          *reinterpret_cast<uint4*>(q_smem + c * kChunkBytes + e * 128 + u * 16) =
+              make_uint4(0, 0, 0, 0);
+    }
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.b_full);
+    uint32_t slot = 0, phase = 0;
+    for (uint64_t k = 0; k < my_tiles; ++k) {
+      const uint32_t bs = static_cast<uint32_t>(k % kRowsBStages);
+      const uint32_t bph = static_cast<uint32_t>(k / kRowsBStages) & 1u;
+      if (!mbar_wait(&sm.pk_full[slot], phase, abort_flag, prm.wait_ns)) goto fail;
+      const uint4* src0 = reinterpret_cast<const uint4*>(packed + slot * kRowsPackBytes + e * 32);
+      const uint4* src1 = src0 + 2 * 128;  // row e + 128
+      const uint4 a0 = src0[0], a1 = src0[1], c0 = src1[0], c1 = src1[1];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.pk_empty[slot]);
+      if (++slot == n_pack) {
+        slot = 0;
+        phase ^= 1u;
+      }
+      if (!mbar_wait(&sm.a_empty[bs], bph ^ 1u, abort_flag, prm.wait_ns)) goto fail;
+      uint8_t* const b0 = b_smem + static_cast<size_t>(bs) * kChunks * kRowsChunkBytes;
+      uint8_t* const b1 = b0 + (kChunks > 1 ? kRowsChunkBytes : 0);
+      expand_row<kKSteps>(a0, a1, b0, b1, e);
+      expand_row<kKSteps>(c0, c1, b0, b1, e + 128);
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.a_full[bs]);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.exp_exit);
+    return;
+  fail:
+    if (lane == 0) {
+      raise_abort(sm, prm.dev_err);
+      mbar_arrive(&sm.exp_exit);
+    }
+    return;
+  }
+
+  if (warp == kMmaWarp) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_f8(kRowsN);
+      bool ok = mbar_wait(&sm.b_full, 0, abort_flag, prm.wait_ns);
+      tc_fence_after();
+      const uint32_t qa0 = smem_u32(q_smem), qa1 = qa0 + kChunkBytes;
+      for (uint64_t k = 0; k < my_tiles && ok; ++k) {
+        const uint32_t bs = static_cast<uint32_t>(k % kRowsBStages);
+        const uint32_t ac = static_cast<uint32_t>(k % kAccStages);
+        if (!mbar_wait(&sm.a_full[bs], static_cast<uint32_t>(k / kRowsBStages) & 1u, abort_flag,
+                       prm.wait_ns) ||
+            !mbar_wait(&sm.acc_empty[ac], (static_cast<uint32_t>(k / kAccStages) & 1u) ^ 1u,
+                       abort_flag, prm.wait_ns)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t b0 = smem_u32(b_smem + static_cast<size_t>(bs) * kChunks * kRowsChunkBytes);
+        const uint32_t b1 = b0 + kRowsChunkBytes;
+        const uint32_t d = tmem_base + ac * kRowsN;
+#pragma unroll
+        for (int ks = 0; ks < kKSteps; ++ks) {
+          const uint32_t off = (ks & 3) * 32;
+          mma_f8(d, sw128_desc((ks < 4 ? qa0 : qa1) + off), sw128_desc((ks < 4 ? b0 : b1) + off),
+                 idesc, ks > 0 ? 1u : 0u);
+        }
+        mma_commit(&sm.a_empty[bs]);
+        mma_commit(&sm.acc_full[ac]);
+      }
+      if (!ok) raise_abort(sm, prm.dev_err);
+      mma_commit(&sm.mma_done);
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.mma_done, 0))
+        if (globaltimer_ns() - t0 > prm.wait_ns) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
+    }
+    __syncwarp();
+    {
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.epi_exit, 0))
+        if (globaltimer_ns() - t0 > prm.wait_ns) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
+      const uint64_t t1 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.exp_exit, 0))
+        if (globaltimer_ns() - t1 > prm.wait_ns) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
+    }
+    tc_fence_after();
+    tmem_dealloc(tmem_base, kTmemCols);
+    return;
+  }
+
+  // ---- epilogue warps 0..7: queries (warp % 4) * 32 + lane; group warp / 4 reads the tile's
+  // rows 128 g .. 128 g + 127 as two 64-column loads
+  {
+    const float dot_min = 32.0f * kKSteps - 2.0f * static_cast<float>(prm.threshold);
+    const uint32_t quarter = static_cast<uint32_t>(warp & 3);
+    const uint32_t group = static_cast<uint32_t>(warp >> 2);
+    const uint32_t lane_addr = (quarter * 32) << 16;
+    const uint32_t q = quarter * 32 + lane;
+    const bool q_ok = q < n_queries;
+    bool ok = true;
+    for (uint64_t k = 0; k < my_tiles && ok; ++k) {
+      const uint64_t tile = blockIdx.x + k * gridDim.x;
+      const uint32_t ac = static_cast<uint32_t>(k % kAccStages);
+      if (!mbar_wait(&sm.acc_full[ac], static_cast<uint32_t>(k / kAccStages) & 1u, abort_flag,
+                     prm.wait_ns)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t c0 = 128 * group;
+      uint32_t raw0[32], raw1[32];
+      float unused[32];
+      tmem_ld64_pack16_nowait(tmem_base + lane_addr + ac * kRowsN + c0, raw0);
+      tmem_ld64_pack16_nowait(tmem_base + lane_addr + ac * kRowsN + c0 + 64, raw1);
+      tmem_ld_wait();
+      tmem_take(raw0, unused);
+      tmem_take(raw1, unused);
+      // both chunks are in registers: hand the stage back before the hit reporting
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+      const uint64_t row0 = tile * kRowsN + c0;
+      auto scan_chunk = [&](const uint32_t (&raw)[32], uint64_t r0) {
+        __half2 mh = *reinterpret_cast<const __half2*>(&raw[0]);
+#pragma unroll
+        for (int i = 1; i < 32; ++i) mh = __hmax2(mh, *reinterpret_cast<const __half2*>(&raw[i]));
+        const float m = fmaxf(__low2float(mh), __high2float(mh));
+        if (__any_sync(0xffffffffu, q_ok && m >= dot_min))
+          emit_rows(q_ok && m >= dot_min ? candidate_mask(raw, dot_min) : 0, r0, q, prm, lane);
+      };
+      scan_chunk(raw0, row0);
+      scan_chunk(raw1, row0 + 64);
+    }
+    if (!ok && lane == 0) raise_abort(sm, prm.dev_err);
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.epi_exit);
+  }
+}
+
 }  // namespace tc
 
 cudaError_t scan_tc_init() {
@@ -992,7 +1309,10 @@ cudaError_t scan_tc_init() {
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 4>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 6>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 8>),
-                        reinterpret_cast<const void*>(tc::scan_pair_kernel)}) {
+                        reinterpret_cast<const void*>(tc::scan_pair_kernel),
+                        reinterpret_cast<const void*>(tc::scan_rows_kernel<4>),
+                        reinterpret_cast<const void*>(tc::scan_rows_kernel<6>),
+                        reinterpret_cast<const void*>(tc::scan_rows_kernel<8>)}) {
     const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                static_cast<int>(tc::kSmemLimit));
     if (e != cudaSuccess) return e;
@@ -1027,6 +1347,30 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   const bool half_k = p.threshold <= 36;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
+  // at most 128 queries and no pass width asked for: queries as A, 256 database rows per
+  // MMA (scan_rows_kernel)
+  if (!p.n_tile && !p.pair_n && p.n_queries <= static_cast<uint32_t>(tc::kRowsMaxQueries)) {
+    const int ks = half_k ? 4 : (p.threshold <= 62 ? 6 : 8);
+    const int chunks = ks > 4 ? 2 : 1;
+    const size_t b_end = tc::kFixedBytes + static_cast<size_t>(chunks) * tc::kChunkBytes +
+                         static_cast<size_t>(tc::rows_b_stages(ks)) * chunks * tc::kRowsChunkBytes;
+    size_t stages = (tc::kSmemLimit - 1024 - b_end) / tc::kRowsPackBytes;
+    if (stages > static_cast<size_t>(tc::kMaxPackStages)) stages = tc::kMaxPackStages;
+    if (stages < 2) return cudaErrorInvalidConfiguration;
+    prm.n_tile = tc::kRowsMaxQueries;
+    prm.pack_stages = static_cast<uint32_t>(stages);
+    prm.pack_offset = static_cast<uint32_t>(b_end);
+    const size_t smem = b_end + stages * tc::kRowsPackBytes + 1024;
+    const uint64_t rtiles = (p.n_rows + tc::kRowsN - 1) / tc::kRowsN;
+    const unsigned g = static_cast<unsigned>(rtiles < static_cast<uint64_t>(num_sms) ? rtiles : num_sms);
+    if (ks == 4)
+      tc::scan_rows_kernel<4><<<g, tc::threads_of(false), smem, s>>>(prm);
+    else if (ks == 6)
+      tc::scan_rows_kernel<6><<<g, tc::threads_of(false), smem, s>>>(prm);
+    else
+      tc::scan_rows_kernel<8><<<g, tc::threads_of(false), smem, s>>>(prm);
+    return cudaGetLastError();
+  }
   if (p.pair_n && (!half_k || p.pair_n != static_cast<uint32_t>(tc::kPairN)))
     return cudaErrorInvalidValue;  // pairs need the 128-bit bound (t <= 36)
   // at t <= 36, passes of 512 queries, two per accumulator column (scan_pair_kernel), when

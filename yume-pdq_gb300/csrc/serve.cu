@@ -462,6 +462,8 @@ ypdq_status autotune(ypdq_server* S) {
     std::vector<Bucket> cand;
     const uint32_t nq = 8 * b.images;
     if (nq <= 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_SIMT, 0, 0, 0.0f, 0});
+    // up to 128 queries: the launcher's choice, queries as A and 256 rows per MMA
+    if (nq <= 128) cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, 0, 0.0f, 0});
     const uint32_t nq64 = (nq + 63u) & ~63u;
     for (uint32_t nt = 64; nt <= 256; nt *= 2)
       if (nt <= nq64 || nt == 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, nt, 0, 0.0f, 0});
@@ -677,10 +679,11 @@ ypdq_status ypdq_server_get_stats(ypdq_server* S, ypdq_server_stats* o, int rese
   for (uint32_t i = 0; i < o->n_buckets; ++i) {
     o->bucket_images[i] = S->buckets[i].images;
     o->bucket_algo[i] = S->buckets[i].algo;
-    o->bucket_n_tile[i] = S->buckets[i].algo != YPDQ_SCAN_TC ? 0
-                          : S->buckets[i].pair_n ? 2 * S->buckets[i].pair_n
-                                                 : S->buckets[i].n_tile;
-    o->bucket_pair[i] = S->buckets[i].algo == YPDQ_SCAN_TC && S->buckets[i].pair_n ? 1 : 0;
+    const Bucket& b = S->buckets[i];
+    const bool tc = b.algo == YPDQ_SCAN_TC;
+    // tensor-core kernel: 0 one query per column (n_tile), 1 pairs, 2 queries as A
+    o->bucket_kernel[i] = !tc ? 0 : b.pair_n ? 1 : b.n_tile ? 0 : 2;
+    o->bucket_n_tile[i] = !tc ? 0 : b.pair_n ? 2 * b.pair_n : b.n_tile ? b.n_tile : 128;
     o->bucket_ms[i] = S->buckets[i].ms;
     o->bucket_steps[i] = S->buckets[i].steps;
   }
