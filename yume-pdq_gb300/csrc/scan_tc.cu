@@ -1260,6 +1260,9 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_rows_kernel(const P
     const uint32_t lane_addr = (quarter * 32) << 16;
     const uint32_t q = quarter * 32 + lane;
     const bool q_ok = q < n_queries;
+    // a lane quarter that holds no query (fewer than 97, 65 or 33 queries) has nothing to
+    // read: its warps only hand each stage back
+    const bool active = quarter * 32 < n_queries;
     bool ok = true;
     for (uint64_t k = 0; k < my_tiles && ok; ++k) {
       const uint64_t tile = blockIdx.x + k * gridDim.x;
@@ -1270,6 +1273,12 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_rows_kernel(const P
         break;
       }
       tc_fence_after();
+      if (!active) {
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+        continue;
+      }
       const uint32_t c0 = 128 * group;
       uint32_t raw0[32], raw1[32];
       float unused[32];
