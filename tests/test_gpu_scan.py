@@ -10,7 +10,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-ALGOS = [1, 2, 3]  # YPDQ_SCAN_SIMT, YPDQ_SCAN_B1MMA, YPDQ_SCAN_TC
+ALGOS = [1, 2, 3, 4]  # YPDQ_SCAN_SIMT, YPDQ_SCAN_B1MMA, YPDQ_SCAN_TC, YPDQ_SCAN_TC_FP4
 
 
 def as_tuples(h):
@@ -346,10 +346,32 @@ def test_pair_kernel_matches_oracle(ctx, yp, oracle, n_q):
             assert np.array_equal(as_tuples(got), as_tuples(want)), (t, algo, len(got), len(want))
 
 
-@pytest.mark.parametrize("n_q", [64, 256, 300])
-def test_device_wait_timeout_is_reported_and_recovered(ctx, yp, oracle, n_q):
-    """The timeout path of the tensor-core scans (64 queries: two issuers and A in tensor
-    memory; 256: one pass; 300: the pair kernel). Under a 1 ms wait limit a launch whose
+@pytest.mark.parametrize("n_q", [1, 2, 239, 240, 241, 479, 480, 481, 961])
+def test_fp4_pair_kernel_matches_oracle(ctx, yp, oracle, n_q):
+    """YPDQ_SCAN_TC_FP4: the pair kernel with block-scaled e2m1 operands (K = 64 per MMA,
+    the second query of a pair scaled by 2^9 through its scale factors), passes of 480
+    queries. Pass boundaries, a pair with one query, rows equal or complementary to a
+    query on the 128-bit prefix (d = +-128 in either half of a column), every threshold
+    0..36 at one size; above 36 the call runs the FP8 scan."""
+    rows = yp.synth.rows_128(6000, seed=n_q + 900)
+    q = yp.synth.rows_128(n_q, seed=n_q + 901)
+    yp.synth.plant(rows, q, 300, 0, 40, seed=9)
+    rows[10], rows[11] = q[0], ~q[n_q - 1]
+    rows[14, :16], rows[14, 16:] = q[n_q // 2, :16], ~q[n_q // 2, 16:]
+    rows[15, :16], rows[15, 16:] = ~q[n_q - 1, :16], q[n_q - 1, 16:]
+    rows[5999] = q[0]                                  # the last, partial tile
+    rows[200:264] = q[np.arange(64) % n_q]             # many hits in one tile
+    ts = range(37) if n_q == 481 else (0, 1, 16, 31, 35, 36, 40)
+    for t in ts:
+        want = oracle.find_all(rows, q, t)
+        got = yp.scan(ctx, rows, q, t, algo=yp._lib.SCAN_TC_FP4)
+        assert np.array_equal(as_tuples(got), as_tuples(want)), (t, len(got), len(want))
+
+
+@pytest.mark.parametrize("n_q,algo", [(64, 3), (256, 3), (300, 3), (300, 4)])
+def test_device_wait_timeout_is_reported_and_recovered(ctx, yp, oracle, n_q, algo):
+    """The timeout path of the tensor-core scans (64 queries: queries as A; 256: one pass;
+    300: the pair kernel, FP8 and FP4). Under a 1 ms wait limit a launch whose
     producer issues nothing (ypdq_debug_stall_scans) stops with its waits run out: the
     stream sync reports YPDQ_ERR_TIMEOUT, and the next scan on the same context returns the
     oracle's hits. No trap, no fault, no unbounded wait."""
@@ -363,14 +385,14 @@ def test_device_wait_timeout_is_reported_and_recovered(ctx, yp, oracle, n_q):
     assert lib.ypdq_set_scan_wait_limit(1_000_000) == 0
     try:
         assert lib.ypdq_debug_stall_scans(1) == 0
-        yp.core.scan_device(ctx, d_rows, rows.shape[0], d_q, n_q, 31, d_hits, cap, d_cnt, 3)
+        yp.core.scan_device(ctx, d_rows, rows.shape[0], d_q, n_q, 31, d_hits, cap, d_cnt, algo)
         with pytest.raises(yp.YpdqError) as err:
             ctx.sync()
         assert err.value.status == yp._lib.ERR_TIMEOUT
     finally:
         lib.ypdq_debug_stall_scans(0)
         lib.ypdq_set_scan_wait_limit(0)
-    got = yp.scan(ctx, rows, q, 31, algo=3)
+    got = yp.scan(ctx, rows, q, 31, algo=algo)
     assert np.array_equal(as_tuples(got), as_tuples(oracle.find_all(rows, q, 31)))
     assert lib.ypdq_set_scan_wait_limit(61 * 10 ** 9) == yp._lib.ERR_INVALID
     assert lib.ypdq_debug_stall_scans(-1) == yp._lib.ERR_INVALID

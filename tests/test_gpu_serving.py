@@ -157,10 +157,12 @@ def test_autotune_table_and_target(ctx, yp, workload):
     with yp.Server(ctx, db, max_step_images=64, autotune=True) as srv:
         st = srv.stats()
         assert [b["images"] for b in st["buckets"]] == [1, 2, 4, 8, 16, 32, 64]
-        assert all(b["ms"] > 0 and b["algo"] in ("simt", "tc", "tc pairs", "tc rows")
+        assert all(b["ms"] > 0 and b["algo"] in ("simt", "tc", "tc pairs", "tc rows",
+                                                 "tc fp4 pairs")
                    for b in st["buckets"])
-        # passes of 512 queries (two per accumulator column) are timed from 17 images up
-        assert all(b["algo"] != "tc pairs" or b["images"] > 16 for b in st["buckets"])
+        # passes of 512 or 480 queries (two per accumulator column) are timed from 17 images
+        assert all(b["algo"] not in ("tc pairs", "tc fp4 pairs") or b["images"] > 16
+                   for b in st["buckets"])
         # queries as the MMA's A operand are timed up to 16 images (128 queries)
         assert all(b["algo"] != "tc rows" or b["images"] <= 16 for b in st["buckets"])
         srv.submit(imgs[:50], tag=0)

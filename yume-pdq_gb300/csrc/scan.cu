@@ -277,6 +277,11 @@ cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t
   if (e != cudaSuccess || p.n_rows == 0 || p.n_queries == 0) return e;
   if (algo == YPDQ_SCAN_AUTO) algo = auto_scan_algo(p.n_queries, p.threshold);
   if (algo == YPDQ_SCAN_TC) return launch_scan_tc(p, num_sms, s);
+  if (algo == YPDQ_SCAN_TC_FP4) {
+    ScanLaunch q = p;
+    if (p.threshold <= 36) q.pair_n = 240;  // the FP4 pair kernel's pairs per pass
+    return launch_scan_tc(q, num_sms, s);
+  }
   // a device-side query count needs the whole query set in one launch
   if (p.nq_dev && (algo != YPDQ_SCAN_SIMT || p.n_queries > kMaxSmemQueries))
     return cudaErrorInvalidValue;

@@ -47,6 +47,7 @@
 #include <cuda_fp16.h>
 
 #include <atomic>
+#include <type_traits>
 
 #include "capi_internal.h"
 #include "ypdq_internal.cuh"
@@ -679,9 +680,91 @@ constexpr int kPairN = 256;                 // pairs per pass (MMA N)
 constexpr int kPairQueries = 2 * kPairN;    // queries per pass
 constexpr int kPairAStages = 4;             // A tiles in shared memory (16 KiB each)
 
+// The FP4 form (kFp4): block-scaled e2m1 operands, K = 64 per MMA. Scale factors live in
+// tensor memory beside the accumulators, so a stage holds 240 pairs (480 queries per pass):
+// stage s at columns 256 s .. 256 s + 239, scale factor 2^0 in columns 496-503 and 2^9 in
+// 504-511 (every byte of each region the same E8M0 value).
+constexpr int kPair4N = 240;
+constexpr uint32_t kPairStageCols = 256;
+constexpr uint32_t kSfOneCol = 496, kSfBigCol = 504, kSfCols = 8;
+constexpr uint32_t kE8m0One = 0x7F7F7F7Fu;  // 2^(127 - 127) in each byte
+constexpr uint32_t kE8m0Big = 0x88888888u;  // 2^(136 - 127) = 512 in each byte
+__host__ __device__ constexpr int pair_n_of(bool fp4) { return fp4 ? kPair4N : kPairN; }
+// The FP4 form reads its 240 accumulator columns with 12 epilogue warps (three per TMEM lane
+// quarter, 80 columns each, all loads of a tile in flight before one wait); the FP8 form with
+// 8 (two per quarter, 128 columns each as two rounds of two loads).
+__host__ __device__ constexpr int pair_epilogue_warps(bool fp4) { return fp4 ? 12 : 8; }
+__host__ __device__ constexpr int pair_threads(bool fp4) {
+  return (pair_epilogue_warps(fp4) + 6) * 32;
+}
+
 // Instruction descriptor: D f32, A and B e5m2, both K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t idesc_e5m2_f32(uint32_t n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+// Instruction descriptor of the block-scaled kind::mxf4 (D is f32): A and B e2m1 (format 1,
+// bits 7-9 and 10-12), both K-major, scale factors UE8M0 (bit 23), N >> 3 at bits 17-22,
+// M >> 4 at bits 24-28, scale-factor IDs 0 (bits 4-5 for B, 29-30 for A), dense K = 64
+// (bit 31 clear).
+__host__ __device__ constexpr uint32_t idesc_mxf4(uint32_t n) {
+  return (1u << 7) | (1u << 10) | ((n >> 3) << 17) | (1u << 23) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_mxf4(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t tmem_sfa, uint32_t tmem_sfb,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %6, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], "
+      "[%5], p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(tmem_sfa), "r"(tmem_sfb), "r"(accumulate)
+      : "memory");
+}
+
+// Store 8 consecutive 32-bit columns of this warp's 32 TMEM lanes, all with the value v.
+__device__ __forceinline__ void tmem_st8_fill(uint32_t taddr, uint32_t v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr),
+      "r"(v)
+      : "memory");
+}
+
+// Issue a load of 16 consecutive columns of this warp's 32 TMEM lanes into r[0..15].
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+
+// tmem_take for the 16 registers of tmem_ld16_nowait.
+__device__ __forceinline__ void tmem_take16(uint32_t (&r)[16]) {
+  asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
+}
+
+// The 128-bit prefix of a packed row as e2m1 (two per byte), +1.0 (0x2) for a clear bit and
+// -1.0 (0xA) for a set bit, into the 128B-swizzled K-major operand (bytes 0-63 of the row;
+// one MMA of K = 64 reads 32 of them). Packed word p becomes 16-byte unit p; its output word
+// m (m = 0..3) holds bits m, m + 4, ..., m + 28 of the word in nibbles 0..7, which `<< (3 - m)`
+// moves to each nibble's sign bit. Rows and queries share the bijection, so the dot product
+// of two expanded rows is 128 - 2 * (prefix distance).
+__device__ __forceinline__ void expand_row_fp4(const uint4 w0, uint8_t* chunk, int row) {
+  const uint32_t words[4] = {w0.x, w0.y, w0.z, w0.w};
+  uint8_t* const base = chunk + row * 128;
+  const int sw = row & 7;
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const uint32_t w = words[p];
+    uint4 out;
+    out.x = ((w << 3) & 0x88888888u) | 0x22222222u;
+    out.y = ((w << 2) & 0x88888888u) | 0x22222222u;
+    out.z = ((w << 1) & 0x88888888u) | 0x22222222u;
+    out.w = (w & 0x88888888u) | 0x22222222u;
+    *reinterpret_cast<uint4*>(base + ((p ^ sw) << 4)) = out;
+  }
 }
 
 __device__ __forceinline__ void mma_pair_issue(uint32_t d, uint32_t a0, uint32_t b0,
@@ -694,7 +777,26 @@ __device__ __forceinline__ void mma_pair_issue(uint32_t d, uint32_t a0, uint32_t
     mma_f8(d, sw128_desc(a0 + 32 * ks), sw128_desc(b1 + 32 * ks), idesc, 1u);
 }
 
-__global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const Params prm) {
+// FP4: two MMAs of K = 64 per query of the pair; query 2j + 1's B scale is 2^9.
+__device__ __forceinline__ void mma_pair4_issue(uint32_t d, uint32_t a0, uint32_t b0,
+                                                uint32_t b1, uint32_t idesc, uint32_t sf_one,
+                                                uint32_t sf_big) {
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks)
+    mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 32 * ks), idesc, sf_one, sf_one,
+             ks > 0 ? 1u : 0u);
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks)
+    mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b1 + 32 * ks), idesc, sf_one, sf_big, 1u);
+}
+
+template <bool kFp4>
+__global__ void __launch_bounds__(pair_threads(kFp4), 1) scan_pair_kernel(const Params prm) {
+  constexpr int kN = pair_n_of(kFp4);       // pairs per pass
+  constexpr int kQueries = 2 * kN;          // queries per pass
+  // roles: epilogue warps 0 .. kEpi - 1, then the producer, the MMA issuer, four expanders
+  constexpr int kEpi = pair_epilogue_warps(kFp4);
+  constexpr int kProducerWarp = kEpi, kMmaWarp = kEpi + 1, kExpandWarp0 = kEpi + 2;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* const smem_base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   Smem& sm = *reinterpret_cast<Smem*>(smem_base);
@@ -702,11 +804,11 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
   const uint32_t n_pack = prm.pack_stages;
   const uint32_t n_queries = prm.nq_dev ? min(*prm.nq_dev, prm.n_queries) : prm.n_queries;
   uint8_t* const a_smem = smem_base + kFixedBytes;    // [kPairAStages][kChunkBytes]
-  uint8_t* const bchunk0 = smem_base + prm.b_offset;  // 256 pairs x 128 B: queries 2j (+-1)
-  uint8_t* const bchunk1 = bchunk0 + kPairN * 128;    // 256 pairs x 128 B: 2j + 1 (+-512)
+  uint8_t* const bchunk0 = smem_base + prm.b_offset;  // 256 pair rows x 128 B: queries 2j
+  uint8_t* const bchunk1 = bchunk0 + kPairN * 128;    // 256 pair rows x 128 B: 2j + 1 (x512)
   uint8_t* const packed = smem_base + prm.pack_offset;
   const uint64_t n_tiles = (prm.n_rows + kTileRows - 1) / kTileRows;
-  const uint32_t n_passes = (n_queries + kPairQueries - 1) / kPairQueries;
+  const uint32_t n_passes = (n_queries + kQueries - 1) / kQueries;
   const uint64_t my_tiles =
       blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   volatile int* abort_flag = &sm.abort_flag;
@@ -722,11 +824,11 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
     }
     for (int s = 0; s < kAccStages; ++s) {
       mbar_init(&sm.acc_full[s], 1);
-      mbar_init(&sm.acc_empty[s], kEpilogueWarps);
+      mbar_init(&sm.acc_empty[s], kEpi);
     }
     mbar_init(&sm.b_full, 4);
     mbar_init(&sm.b_empty, 1);
-    mbar_init(&sm.epi_exit, kEpilogueWarps);
+    mbar_init(&sm.epi_exit, kEpi);
     mbar_init(&sm.exp_exit, 4);
     mbar_init(&sm.mma_done, 1);
     sm.abort_flag = 0;
@@ -743,6 +845,19 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
   if (my_tiles == 0 || n_passes == 0) {
     if (warp == kMmaWarp) tmem_dealloc(tmem_base, kTmemCols);
     return;
+  }
+  if constexpr (kFp4) {
+    // the scale-factor regions: epilogue warp w writes its lane quarter w % 4, group 0 the
+    // 2^0 region and group 1 the 2^9 region, before any MMA is issued
+    if (warp < 8) {
+      const uint32_t taddr = tmem_base + ((static_cast<uint32_t>(warp & 3) * 32) << 16) +
+                             (warp < 4 ? kSfOneCol : kSfBigCol);
+      tmem_st8_fill(taddr, warp < 4 ? kE8m0One : kE8m0Big);
+      tmem_st_wait();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
   }
 
   if (warp == kProducerWarp) {
@@ -789,13 +904,16 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
     uint32_t slot = 0, phase = 0, ga = 0;
     for (uint32_t p = 0; p < n_passes; ++p) {
       if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag, prm.wait_ns)) goto fail;
-      for (uint32_t j = e; j < static_cast<uint32_t>(kPairN); j += 128) {
-        const uint64_t q0 = static_cast<uint64_t>(p) * kPairQueries + 2 * j;
+      for (uint32_t j = e; j < static_cast<uint32_t>(kN); j += 128) {
+        const uint64_t q0 = static_cast<uint64_t>(p) * kQueries + 2 * j;
         const uint4 zero = make_uint4(0, 0, 0, 0);
         // a query past the end gives a zero B row: its products are all 0
         if (q0 < n_queries) {
           const uint4* src = reinterpret_cast<const uint4*>(prm.queries + q0 * 32);
-          expand_row<4, 0x3C3C3C3Cu>(src[0], src[1], bchunk0, nullptr, static_cast<int>(j));
+          if constexpr (kFp4)
+            expand_row_fp4(src[0], bchunk0, static_cast<int>(j));
+          else
+            expand_row<4, 0x3C3C3C3Cu>(src[0], src[1], bchunk0, nullptr, static_cast<int>(j));
         } else {
 #pragma unroll
           for (int u = 0; u < 8; ++u)
@@ -803,7 +921,10 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
         }
         if (q0 + 1 < n_queries) {
           const uint4* src = reinterpret_cast<const uint4*>(prm.queries + (q0 + 1) * 32);
-          expand_row<4, 0x60606060u>(src[0], src[1], bchunk1, nullptr, static_cast<int>(j));
+          if constexpr (kFp4)
+            expand_row_fp4(src[0], bchunk1, static_cast<int>(j));
+          else
+            expand_row<4, 0x60606060u>(src[0], src[1], bchunk1, nullptr, static_cast<int>(j));
         } else {
 #pragma unroll
           for (int u = 0; u < 8; ++u)
@@ -827,8 +948,11 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
           phase ^= 1u;
         }
         if (!mbar_wait(&sm.a_empty[as], aph ^ 1u, abort_flag, prm.wait_ns)) goto fail;
-        expand_row<4, 0x3C3C3C3Cu>(w0, w1, a_smem + static_cast<size_t>(as) * kChunkBytes,
-                                   nullptr, e);
+        if constexpr (kFp4)
+          expand_row_fp4(w0, a_smem + static_cast<size_t>(as) * kChunkBytes, e);
+        else
+          expand_row<4, 0x3C3C3C3Cu>(w0, w1, a_smem + static_cast<size_t>(as) * kChunkBytes,
+                                     nullptr, e);
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.a_full[as]);
@@ -847,7 +971,7 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
 
   if (warp == kMmaWarp) {
     if (lane == 0) {
-      const uint32_t idesc = idesc_e5m2_f32(kPairN);
+      const uint32_t idesc = kFp4 ? idesc_mxf4(kN) : idesc_e5m2_f32(kN);
       const uint32_t b0 = smem_u32(bchunk0), b1 = smem_u32(bchunk1);
       uint32_t ga = 0;
       bool ok = true;
@@ -866,8 +990,12 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
             break;
           }
           tc_fence_after();
-          mma_pair_issue(tmem_base + ac * kPairN,
-                         smem_u32(a_smem + static_cast<size_t>(as) * kChunkBytes), b0, b1, idesc);
+          const uint32_t a0 = smem_u32(a_smem + static_cast<size_t>(as) * kChunkBytes);
+          if constexpr (kFp4)
+            mma_pair4_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc,
+                            tmem_base + kSfOneCol, tmem_base + kSfBigCol);
+          else
+            mma_pair_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc);
           mma_commit(&sm.a_empty[as]);
           mma_commit(&sm.acc_full[ac]);
         }
@@ -904,18 +1032,21 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
     return;
   }
 
-  // ---- epilogue warps 0..7: rows (warp % 4) * 32 + lane; group warp / 4 reads the pair
-  // columns 128 g .. 128 g + 127 of the stage as four loads of 32, two in flight at a time
+  // ---- epilogue warps: rows (warp % 4) * 32 + lane; group warp / 4 reads its columns of the
+  // stage. FP8: group g reads pairs 128 g .. 128 g + 127 as four loads of 32, two in flight at
+  // a time. FP4: group g (0..2) reads pairs 80 g .. 80 g + 79 as loads of 32, 32 and 16, all
+  // in flight before one wait.
   {
     const float dot_min = 128.0f - 2.0f * static_cast<float>(prm.threshold);
     const float magic = 8388608.0f + 65664.0f + 513.0f * (384.0f - dot_min);
     const uint32_t quarter = static_cast<uint32_t>(warp & 3);
     const uint32_t group = static_cast<uint32_t>(warp >> 2);
     const uint32_t lane_addr = (quarter * 32) << 16;
+    constexpr uint32_t kGroupCols = kFp4 ? 80 : 128;
     uint32_t ga = 0;
     bool ok = true;
     for (uint32_t p = 0; p < n_passes && ok; ++p) {
-      const uint64_t pass_q = static_cast<uint64_t>(p) * kPairQueries;
+      const uint64_t pass_q = static_cast<uint64_t>(p) * kQueries;
       for (uint64_t k = 0; k < my_tiles; ++k, ++ga) {
         const uint64_t tile = blockIdx.x + k * gridDim.x;
         const uint32_t ac = ga % kAccStages;
@@ -926,13 +1057,15 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
         tc_fence_after();
         const uint64_t row = tile * kTileRows + quarter * 32 + lane;
         const bool row_ok = row < prm.n_rows;
-        const uint32_t col0 = ac * kPairN + 128 * group;
-        // candidate mask of 32 pair columns (64 queries; bits 2i and 2i + 1 are pair i's
-        // two queries); `need` is set for the whole warp when any lane has a candidate
-        auto chunk_mask = [&](const uint32_t (&raw)[32], bool& need) -> uint64_t {
+        const uint32_t col0 = ac * kPairStageCols + kGroupCols * group;
+        const uint64_t q_first = pass_q + 2 * static_cast<uint64_t>(kGroupCols * group);
+        // candidate mask of kCols pair columns (2 kCols queries; bits 2i and 2i + 1 are pair
+        // i's two queries); `need` is set for the whole warp when any lane has a candidate
+        auto chunk_mask = [&](const uint32_t* raw, auto cols, bool& need) -> uint64_t {
+          constexpr int kCols = decltype(cols)::value;
           uint32_t any = 0;
 #pragma unroll
-          for (int i = 0; i < 32; i += 2)
+          for (int i = 0; i < kCols; i += 2)
             any |= __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic)) |
                    __float_as_uint(__fadd_rn(__uint_as_float(raw[i + 1]), magic));
           const bool cand = row_ok && (any & 0x40200u);
@@ -940,7 +1073,7 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
           uint64_t mask = 0;
           if (cand) {
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
+            for (int i = 0; i < kCols; ++i) {
               const uint32_t x = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic));
               mask |= static_cast<uint64_t>((x >> 9) & 1u) << (2 * i);
               mask |= static_cast<uint64_t>((x >> 18) & 1u) << (2 * i + 1);
@@ -948,33 +1081,56 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_pair_kernel(const P
           }
           return mask;
         };
+        using C32 = std::integral_constant<int, 32>;
+        using C16 = std::integral_constant<int, 16>;
         uint32_t raw0[32], raw1[32];
         float unused[32];
-        uint64_t mask[4];
-        bool need[4];
-        tmem_ld32_nowait(tmem_base + lane_addr + col0, raw0);
-        tmem_ld32_nowait(tmem_base + lane_addr + col0 + 32, raw1);
-        tmem_ld_wait();
-        tmem_take(raw0, unused);
-        tmem_take(raw1, unused);
-        mask[0] = chunk_mask(raw0, need[0]);
-        mask[1] = chunk_mask(raw1, need[1]);
-        tmem_ld32_nowait(tmem_base + lane_addr + col0 + 64, raw0);
-        tmem_ld32_nowait(tmem_base + lane_addr + col0 + 96, raw1);
-        tmem_ld_wait();
-        tmem_take(raw0, unused);
-        tmem_take(raw1, unused);
-        // the stage's last columns are in registers: hand it back before the hit reporting
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
-        mask[2] = chunk_mask(raw0, need[2]);
-        mask[3] = chunk_mask(raw1, need[3]);
+        if constexpr (kFp4) {
+          uint32_t raw2[16];
+          tmem_ld32_nowait(tmem_base + lane_addr + col0, raw0);
+          tmem_ld32_nowait(tmem_base + lane_addr + col0 + 32, raw1);
+          tmem_ld16_nowait(tmem_base + lane_addr + col0 + 64, raw2);
+          tmem_ld_wait();
+          tmem_take(raw0, unused);
+          tmem_take(raw1, unused);
+          tmem_take16(raw2);
+          // the whole stage is in registers: hand it back before decoding
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+          bool need[3];
+          uint64_t mask[3];
+          mask[0] = chunk_mask(raw0, C32{}, need[0]);
+          mask[1] = chunk_mask(raw1, C32{}, need[1]);
+          mask[2] = chunk_mask(raw2, C16{}, need[2]);
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-          if (need[i])
-            emit_candidates(mask[i], row, pass_q + 2 * (128 * group + 32 * i), n_queries, prm,
-                            lane);
+          for (int i = 0; i < 3; ++i)
+            if (need[i]) emit_candidates(mask[i], row, q_first + 64 * i, n_queries, prm, lane);
+        } else {
+          uint64_t mask[4];
+          bool need[4];
+          tmem_ld32_nowait(tmem_base + lane_addr + col0, raw0);
+          tmem_ld32_nowait(tmem_base + lane_addr + col0 + 32, raw1);
+          tmem_ld_wait();
+          tmem_take(raw0, unused);
+          tmem_take(raw1, unused);
+          mask[0] = chunk_mask(raw0, C32{}, need[0]);
+          mask[1] = chunk_mask(raw1, C32{}, need[1]);
+          tmem_ld32_nowait(tmem_base + lane_addr + col0 + 64, raw0);
+          tmem_ld32_nowait(tmem_base + lane_addr + col0 + 96, raw1);
+          tmem_ld_wait();
+          tmem_take(raw0, unused);
+          tmem_take(raw1, unused);
+          // the stage's last columns are in registers: hand it back before the hit reporting
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+          mask[2] = chunk_mask(raw0, C32{}, need[2]);
+          mask[3] = chunk_mask(raw1, C32{}, need[3]);
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (need[i]) emit_candidates(mask[i], row, q_first + 64 * i, n_queries, prm, lane);
+        }
       }
     }
     if (!ok && lane == 0) raise_abort(sm, prm.dev_err);
@@ -1318,7 +1474,8 @@ cudaError_t scan_tc_init() {
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 4>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 6>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 8>),
-                        reinterpret_cast<const void*>(tc::scan_pair_kernel),
+                        reinterpret_cast<const void*>(tc::scan_pair_kernel<false>),
+                        reinterpret_cast<const void*>(tc::scan_pair_kernel<true>),
                         reinterpret_cast<const void*>(tc::scan_rows_kernel<4>),
                         reinterpret_cast<const void*>(tc::scan_rows_kernel<6>),
                         reinterpret_cast<const void*>(tc::scan_rows_kernel<8>)}) {
@@ -1380,12 +1537,14 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
       tc::scan_rows_kernel<8><<<g, tc::threads_of(false), smem, s>>>(prm);
     return cudaGetLastError();
   }
-  if (p.pair_n && (!half_k || p.pair_n != static_cast<uint32_t>(tc::kPairN)))
+  if (p.pair_n && (!half_k || (p.pair_n != static_cast<uint32_t>(tc::kPairN) &&
+                                p.pair_n != static_cast<uint32_t>(tc::kPair4N))))
     return cudaErrorInvalidValue;  // pairs need the 128-bit bound (t <= 36)
   // at t <= 36, passes of 512 queries, two per accumulator column (scan_pair_kernel), when
-  // asked for or by default past one pass of 256
+  // asked for or by default past one pass of 256; pair_n = 240: the FP4 form, passes of 480
   if (half_k && !p.n_tile && (p.pair_n || p.n_queries > static_cast<uint32_t>(tc::kMaxN))) {
-    prm.n_tile = tc::kPairQueries;
+    const bool fp4 = p.pair_n == static_cast<uint32_t>(tc::kPair4N);
+    prm.n_tile = 2u * static_cast<uint32_t>(tc::pair_n_of(fp4));
     prm.a_stages = tc::kPairAStages;
     // layout: [fixed Smem][A: 4 x 16 KB][B: 2 x 256 pairs x 128 B][packed ring], 1024-aligned
     prm.b_offset = static_cast<uint32_t>(tc::kFixedBytes +
@@ -1396,7 +1555,10 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
     prm.pack_stages = static_cast<uint32_t>(stages);
     prm.pack_offset = static_cast<uint32_t>(b_end);
     const size_t smem = b_end + stages * tc::kPackBytes + 1024;
-    tc::scan_pair_kernel<<<static_cast<unsigned>(grid), tc::threads_of(false), smem, s>>>(prm);
+    if (fp4)
+      tc::scan_pair_kernel<true><<<static_cast<unsigned>(grid), tc::pair_threads(true), smem, s>>>(prm);
+    else
+      tc::scan_pair_kernel<false><<<static_cast<unsigned>(grid), tc::pair_threads(false), smem, s>>>(prm);
     return cudaGetLastError();
   }
   // passes of <= 128 queries: two MMA issuers and A in tensor memory (the pass is bound by

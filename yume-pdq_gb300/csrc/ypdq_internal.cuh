@@ -197,8 +197,9 @@ struct ScanLaunch {
   uint32_t n_tile;         // tensor-core scan: queries per pass (multiple of 64, <= 256);
                            // 0 picks min(256, n_queries rounded up to 64)
   uint32_t pair_n;         // tensor-core scan at t <= 36: 256 = passes of 256 query pairs,
-                           // two per accumulator column; with n_tile and pair_n both 0 the
-                           // launcher takes pairs past 256 queries
+                           // two per accumulator column (FP8 operands); 240 = passes of 240
+                           // pairs with block-scaled FP4 operands; with n_tile and pair_n
+                           // both 0 the launcher takes pairs past 256 queries
 };
 
 // hash.cu
