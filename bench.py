@@ -220,17 +220,17 @@ def fp8_dense_burst(device=0, n=8192, reps=10):
 
 
 def fp4_dense_burst(device=0, n=8192, reps=10):
-    """Dense block-scaled FP4 (MXFP4: e2m1 operands, one E8M0 scale per 32 elements along K)
-    tensor-core rate of this GPU in TFLOP/s: torch._scaled_mm of two n x n e2m1 matrices
-    with unit scales (bf16 out), best of `reps` launches timed with CUDA events, 2 n^3 FLOP
-    each. None if this torch build has no FP4 GEMM."""
+    """Dense block-scaled FP4 tensor-core rate of this GPU in TFLOP/s: torch._scaled_mm of two
+    n x n e2m1 matrices with unit e4m3 scales per 16 elements along K (the block-scaled FP4
+    GEMM this torch build offers; bf16 out), best of `reps` launches timed with CUDA events,
+    2 n^3 FLOP each. None if this torch build has no FP4 GEMM."""
     try:
         import torch
         dev = torch.device("cuda", device)
         x4 = torch.float4_e2m1fn_x2
         a = torch.randint(0, 256, (n, n // 2), dtype=torch.uint8, device=dev).view(x4)
         b = torch.randint(0, 256, (n, n // 2), dtype=torch.uint8, device=dev).view(x4).t()
-        scale = torch.ones(n * (n // 32), device=dev).to(torch.float8_e8m0fnu)
+        scale = torch.ones(n * (n // 16), device=dev).to(torch.float8_e4m3fn)
 
         def mm():
             return torch._scaled_mm(a, b, scale, scale, out_dtype=torch.bfloat16)
@@ -888,9 +888,9 @@ def main():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     if args.peaks:
         print(json.dumps({"fp8_e4m3_dense_tflops": fp8_dense_burst(),
-                          "fp4_mxfp4_dense_tflops": fp4_dense_burst(),
+                          "fp4_dense_tflops": fp4_dense_burst(),
                           "how": "torch._scaled_mm 8192^3 (e4m3 with unit per-tensor scales; "
-                                 "e2m1 with unit E8M0 scales per 32 elements), bf16 out, best "
+                                 "e2m1 with unit e4m3 scales per 16 elements), bf16 out, best "
                                  "of 10, CUDA events"}))
         return
     if args.impl == "ours" and args.gpus > 1 and "WORLD_SIZE" not in os.environ:

@@ -94,3 +94,22 @@ def test_screening_stream_with_database(yp, oracle, tmp_path):
     assert got_hashes == [bytes(x).hex().encode() for x in h[:, 0]]
     assert sorted(got_hits) == sorted(zip(want["index"].tolist(), want["query"].tolist(),
                                           want["distance"].tolist()))
+
+
+def test_diagnostic_stream(yp, oracle):
+    """The diagnostic format end to end: each slot's quality, threshold, hash and PDQF (as the
+    reference's buffer holds it at that visit) equal the oracle's, printed as the reference
+    prints them."""
+    pipe = load_pipe()
+    frames = yp.synth.to_u8(yp.synth.blob_images(2, seed=507))
+    sem = yp.kernel.host_semantics()
+    out = run(["-f", "diagnostic", "--dihedrals"], frames.tobytes())
+    h, q, t, p = oracle.hash_batch(frames, semantics=sem, want_pdqf=True)
+    want = []
+    for f in range(len(frames)):
+        dh, dt, dq, dp = oracle.dihedrals(p[f], t[f, 0], sem)
+        pdqfs = [p[f]] + list(dp)
+        for s in range(8):
+            want.append(pipe.format_diagnostic(s, s, h[f, s], q[f, s], t[f, s], pdqfs[s], b""))
+    assert out == b"".join(want)
+    assert out.count(b"Index: 0\n") == 2 and out.count(b"[Dihedrals") == 14

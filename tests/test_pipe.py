@@ -50,3 +50,28 @@ def test_read_frames(pipe):
     with pytest.raises(EOFError):
         pipe.read_frames(io.BytesIO(data[:-1]), 3, 8)
     assert pipe.read_frames(io.BytesIO(b""), 1, 8) is None
+
+
+def test_diagnostic_format(pipe):
+    """The reference's diagnostic output (src/main.rs:738-773): header, index, quality x 100
+    with 3 decimals, threshold with 7, the 256 bits on one line, the PDQF rows with '*' on
+    values above the threshold, each value with 5 decimals."""
+    h = bytes(range(0, 256, 8))
+    pdqf = np.arange(256, dtype=np.float32).reshape(16, 16) / np.float32(7.0) - np.float32(10.0)
+    out = pipe.format_diagnostic(0, 0, h, np.float32(0.5), np.float32(1.25), pdqf, b"\n").decode()
+    lines = out.split("\n")
+    assert lines[:5] == ['["original"]', "Index: 0", "Quality: 50.000", "Threshold: 1.2500000",
+                         "Hash:"]
+    assert lines[5] == "".join(format(b, "08b") for b in h)
+    assert lines[6] == "PDQF:"
+    rows = lines[7:23]
+    assert len(rows) == 16 and lines[23] == "" and out.endswith("\n\n")
+    first = rows[0].split("\t")
+    assert first[0] == "%.5f" % float(pdqf[0, 0]) and not first[0].startswith("*")
+    assert rows[15].split("\t")[15] == "*%.5f" % float(pdqf[15, 15])
+    assert sum(v.startswith("*") for r in rows for v in r.split("\t")) == int(np.sum(pdqf > 1.25))
+    # derived hashes are named by their Dihedrals value (four big-endian i8 matrix entries)
+    assert pipe.format_diagnostic(1, 1, h, 0.5, 1.25, pdqf, b"").startswith(
+        b"[Dihedrals { packed: 4278190081 }]\nIndex: 1\n")
+    assert pipe.slot_name(7) == "Dihedrals { packed: %d }" % 0x0001FF00
+    assert pipe.parse_format("diagnostic+lf") == ("diagnostic", False, False, b"\n")

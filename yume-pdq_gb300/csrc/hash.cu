@@ -759,12 +759,24 @@ __global__ void __launch_bounds__(hash_threads<kDct>(), (hash_min_blocks<Tin, kD
         mma_commit(&sm.mma_done);
         const uint64_t t0 = globaltimer_ns();
         while (!mbar_try_wait(&sm.mma_done, 0))
-          if (globaltimer_ns() - t0 > kWaitLimitNs) break;
+          if (globaltimer_ns() - t0 > kWaitLimitNs) {
+            // the MMAs did not drain: the results are not trustworthy, so flag the launch
+            *abort_flag = 1;
+            atomicOr(prm.dev_err, kDevErrTimeout);
+            break;
+          }
       }
       __syncwarp();
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(&sm.tc_exit, 0))
-        if (globaltimer_ns() - t0 > kWaitLimitNs) break;
+        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+          // the compute warps did not report that they stopped reading tensor memory
+          if (lane == 0) {
+            *abort_flag = 1;
+            atomicOr(prm.dev_err, kDevErrTimeout);
+          }
+          break;
+        }
       tc_fence_after();
       tmem_dealloc(tmem, 32);
       return;

@@ -296,6 +296,14 @@ __device__ __forceinline__ void emit_candidates(uint64_t cand, uint64_t row, uin
   }
 }
 
+// emit_candidates as a call: the pair kernel's epilogue reaches it only on the rare tiles with a
+// candidate, and inlined at each of its chunks it would crowd the registers of the common path.
+__device__ __noinline__ void emit_candidates_call(uint64_t cand, uint64_t row, uint64_t q_first,
+                                                  uint32_t n_queries, const Params* prm,
+                                                  int lane) {
+  emit_candidates(cand, row, q_first, n_queries, *prm, lane);
+}
+
 __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
   *reinterpret_cast<volatile int*>(&sm.abort_flag) = 1;
   atomicOr(dev_err, kDevErrTimeout);
@@ -676,8 +684,7 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
 // passes of 256 f16 queries gave them ~540 clk and left the tensor pipe ~40 % idle. Eight
 // MMAs per commit also keep the issuing thread (~60 clk per MMA) off the critical path.
 // Roles and barriers are those of scan_tc_kernel<false, 4>.
-constexpr int kPairN = 256;                 // pairs per pass (MMA N)
-constexpr int kPairQueries = 2 * kPairN;    // queries per pass
+constexpr int kPairN = 256;                 // pairs per pass (MMA N), 512 queries
 constexpr int kPairAStages = 4;             // A tiles in shared memory (16 KiB each)
 
 // The FP4 form (kFp4): block-scaled e2m1 operands, K = 64 per MMA. Scale factors live in
@@ -686,14 +693,13 @@ constexpr int kPairAStages = 4;             // A tiles in shared memory (16 KiB 
 // 504-511 (every byte of each region the same E8M0 value).
 constexpr int kPair4N = 240;
 constexpr uint32_t kPairStageCols = 256;
-constexpr uint32_t kSfOneCol = 496, kSfBigCol = 504, kSfCols = 8;
+constexpr uint32_t kSfOneCol = 496, kSfBigCol = 504;  // 8 columns each
 constexpr uint32_t kE8m0One = 0x7F7F7F7Fu;  // 2^(127 - 127) in each byte
 constexpr uint32_t kE8m0Big = 0x88888888u;  // 2^(136 - 127) = 512 in each byte
 __host__ __device__ constexpr int pair_n_of(bool fp4) { return fp4 ? kPair4N : kPairN; }
-// The FP4 form reads its 240 accumulator columns with 12 epilogue warps (three per TMEM lane
-// quarter, 80 columns each, all loads of a tile in flight before one wait); the FP8 form with
-// 8 (two per quarter, 128 columns each as two rounds of two loads).
-__host__ __device__ constexpr int pair_epilogue_warps(bool fp4) { return fp4 ? 12 : 8; }
+// Both forms read their accumulator stage with 8 epilogue warps, two per TMEM lane quarter,
+// each warp half the stage's columns (128 for FP8, 120 for FP4) in two rounds.
+__host__ __device__ constexpr int pair_epilogue_warps(bool) { return 8; }
 __host__ __device__ constexpr int pair_threads(bool fp4) {
   return (pair_epilogue_warps(fp4) + 6) * 32;
 }
@@ -723,6 +729,13 @@ __device__ __forceinline__ void mma_mxf4(uint32_t tmem_d, uint64_t adesc, uint64
       : "memory");
 }
 
+// Store 16 consecutive 32-bit columns of this warp's 32 TMEM lanes, all with the value v.
+__device__ __forceinline__ void tmem_st16_fill(uint32_t taddr, uint32_t v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr),
+      "r"(v)
+      : "memory");
+}
 // Store 8 consecutive 32-bit columns of this warp's 32 TMEM lanes, all with the value v.
 __device__ __forceinline__ void tmem_st8_fill(uint32_t taddr, uint32_t v) {
   asm volatile(
@@ -738,6 +751,30 @@ __device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[1
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr)
       : "memory");
+}
+
+// Two f32 additions in one instruction (add.rn.f32x2): (a + m.lo, b + m.hi) as bit patterns,
+// a in the low half of the result.
+__device__ __forceinline__ uint64_t fadd2_rn(uint32_t a, uint32_t b, uint64_t m2) {
+  uint64_t r;
+  asm("{\n\t.reg .b64 t;\n\tmov.b64 t, {%1, %2};\n\tadd.rn.f32x2 %0, t, %3;\n\t}"
+      : "=l"(r)
+      : "r"(a), "r"(b), "l"(m2));
+  return r;
+}
+
+// Issue a load of 8 consecutive columns of this warp's 32 TMEM lanes into r[0..7].
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+}
+
+// tmem_take for the 8 registers of tmem_ld8_nowait.
+__device__ __forceinline__ void tmem_take8(uint32_t (&r)[8]) {
+  asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]));
 }
 
 // tmem_take for the 16 registers of tmem_ld16_nowait.
@@ -767,11 +804,12 @@ __device__ __forceinline__ void expand_row_fp4(const uint4 w0, uint8_t* chunk, i
   }
 }
 
+// All MMAs accumulate: the stage holds the decoding constant when the tile's MMAs start.
 __device__ __forceinline__ void mma_pair_issue(uint32_t d, uint32_t a0, uint32_t b0,
                                                uint32_t b1, uint32_t idesc) {
 #pragma unroll
   for (int ks = 0; ks < 4; ++ks)
-    mma_f8(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 32 * ks), idesc, ks > 0 ? 1u : 0u);
+    mma_f8(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 32 * ks), idesc, 1u);
 #pragma unroll
   for (int ks = 0; ks < 4; ++ks)
     mma_f8(d, sw128_desc(a0 + 32 * ks), sw128_desc(b1 + 32 * ks), idesc, 1u);
@@ -783,15 +821,15 @@ __device__ __forceinline__ void mma_pair4_issue(uint32_t d, uint32_t a0, uint32_
                                                 uint32_t sf_big) {
 #pragma unroll
   for (int ks = 0; ks < 2; ++ks)
-    mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 32 * ks), idesc, sf_one, sf_one,
-             ks > 0 ? 1u : 0u);
+    mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 32 * ks), idesc, sf_one, sf_one, 1u);
 #pragma unroll
   for (int ks = 0; ks < 2; ++ks)
     mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b1 + 32 * ks), idesc, sf_one, sf_big, 1u);
 }
 
 template <bool kFp4>
-__global__ void __launch_bounds__(pair_threads(kFp4), 1) scan_pair_kernel(const Params prm) {
+__global__ void __launch_bounds__(pair_threads(kFp4), 1)
+    scan_pair_kernel(const __grid_constant__ Params prm) {
   constexpr int kN = pair_n_of(kFp4);       // pairs per pass
   constexpr int kQueries = 2 * kN;          // queries per pass
   // roles: epilogue warps 0 .. kEpi - 1, then the producer, the MMA issuer, four expanders
@@ -846,19 +884,36 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1) scan_pair_kernel(const 
     if (warp == kMmaWarp) tmem_dealloc(tmem_base, kTmemCols);
     return;
   }
-  if constexpr (kFp4) {
-    // the scale-factor regions: epilogue warp w writes its lane quarter w % 4, group 0 the
-    // 2^0 region and group 1 the 2^9 region, before any MMA is issued
-    if (warp < 8) {
-      const uint32_t taddr = tmem_base + ((static_cast<uint32_t>(warp & 3) * 32) << 16) +
-                             (warp < 4 ? kSfOneCol : kSfBigCol);
-      tmem_st8_fill(taddr, warp < 4 ? kE8m0One : kE8m0Big);
-      tmem_st_wait();
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
+  // The decoding constant (see the epilogue) goes into every accumulator column, of both
+  // stages, before any MMA is issued; each epilogue warp writes its own columns. The FP4 form
+  // also fills its scale-factor regions: group 0 the 2^0 region, group 1 the 2^9 one.
+  const float dot_min = 128.0f - 2.0f * static_cast<float>(prm.threshold);
+  const uint32_t magic_bits =
+      __float_as_uint(8388608.0f + 65664.0f + 513.0f * (384.0f - dot_min));
+  constexpr uint32_t kGroupCols = kFp4 ? 120 : 128;
+  // (16 columns per store: a store's source is a block of consecutive registers)
+  auto fill_cols = [&](uint32_t taddr, auto cols) {
+    constexpr int kCols = decltype(cols)::value;
+#pragma unroll
+    for (int c = 0; c + 16 <= kCols; c += 16) tmem_st16_fill(taddr + c, magic_bits);
+    if constexpr (kCols % 16 == 8) tmem_st8_fill(taddr + kCols - 8, magic_bits);
+  };
+  auto fill_group = [&](uint32_t taddr) {
+    fill_cols(taddr, std::integral_constant<int, static_cast<int>(kGroupCols)>{});
+  };
+  if (warp < kEpi) {
+    const uint32_t lanes = (static_cast<uint32_t>(warp & 3) * 32) << 16;
+    const uint32_t g = static_cast<uint32_t>(warp >> 2);
+    for (uint32_t st = 0; st < kAccStages; ++st)
+      fill_group(tmem_base + lanes + st * kPairStageCols + kGroupCols * g);
+    if (kFp4 && warp < 8)
+      tmem_st8_fill(tmem_base + lanes + (warp < 4 ? kSfOneCol : kSfBigCol),
+                    warp < 4 ? kE8m0One : kE8m0Big);
+    tmem_st_wait();
   }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
 
   if (warp == kProducerWarp) {
     if (lane == 0 && !prm.stall) {
@@ -1032,17 +1087,38 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1) scan_pair_kernel(const 
     return;
   }
 
-  // ---- epilogue warps: rows (warp % 4) * 32 + lane; group warp / 4 reads its columns of the
-  // stage. FP8: group g reads pairs 128 g .. 128 g + 127 as four loads of 32, two in flight at
-  // a time. FP4: group g (0..2) reads pairs 80 g .. 80 g + 79 as loads of 32, 32 and 16, all
-  // in flight before one wait.
+  // ---- epilogue warps 0..7: rows (warp % 4) * 32 + lane; group g = warp / 4 reads pairs
+  // kGroupCols g .. + kGroupCols - 1 of the stage in two rounds: 64 columns (two loads of 32),
+  // then the rest (FP8: two loads of 32; FP4: loads of 32, 16 and 8). Each column holds
+  // v + MAGIC (the stage was filled with MAGIC before its MMAs), so the common case (no
+  // candidate in the round's columns) costs one three-input OR per two columns and one vote;
+  // the warp writes MAGIC back into its columns before it hands the stage to the MMA issuer.
   {
-    const float dot_min = 128.0f - 2.0f * static_cast<float>(prm.threshold);
-    const float magic = 8388608.0f + 65664.0f + 513.0f * (384.0f - dot_min);
     const uint32_t quarter = static_cast<uint32_t>(warp & 3);
     const uint32_t group = static_cast<uint32_t>(warp >> 2);
     const uint32_t lane_addr = (quarter * 32) << 16;
-    constexpr uint32_t kGroupCols = kFp4 ? 80 : 128;
+    auto chunk_any = [&](const uint32_t* raw, auto cols) -> uint32_t {
+      constexpr int kCols = decltype(cols)::value;
+      uint32_t any = 0;
+#pragma unroll
+      for (int i = 0; i < kCols; i += 2) any |= raw[i] | raw[i + 1];
+      return any;
+    };
+    // the rare path: the 2 kCols-query candidate mask of one chunk (bits 2i and 2i + 1 are pair
+    // i's two queries)
+    auto chunk_mask = [&](const uint32_t* raw, auto cols) -> uint64_t {
+      constexpr int kCols = decltype(cols)::value;
+      uint64_t mask = 0;
+#pragma unroll
+      for (int i = 0; i < kCols; ++i) {
+        mask |= static_cast<uint64_t>((raw[i] >> 9) & 1u) << (2 * i);
+        mask |= static_cast<uint64_t>((raw[i] >> 18) & 1u) << (2 * i + 1);
+      }
+      return mask;
+    };
+    using C8 = std::integral_constant<int, 8>;
+    using C16 = std::integral_constant<int, 16>;
+    using C32 = std::integral_constant<int, 32>;
     uint32_t ga = 0;
     bool ok = true;
     for (uint32_t p = 0; p < n_passes && ok; ++p) {
@@ -1057,79 +1133,74 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1) scan_pair_kernel(const 
         tc_fence_after();
         const uint64_t row = tile * kTileRows + quarter * 32 + lane;
         const bool row_ok = row < prm.n_rows;
-        const uint32_t col0 = ac * kPairStageCols + kGroupCols * group;
+        const uint32_t cols = tmem_base + lane_addr + ac * kPairStageCols + kGroupCols * group;
         const uint64_t q_first = pass_q + 2 * static_cast<uint64_t>(kGroupCols * group);
-        // candidate mask of kCols pair columns (2 kCols queries; bits 2i and 2i + 1 are pair
-        // i's two queries); `need` is set for the whole warp when any lane has a candidate
-        auto chunk_mask = [&](const uint32_t* raw, auto cols, bool& need) -> uint64_t {
-          constexpr int kCols = decltype(cols)::value;
-          uint32_t any = 0;
-#pragma unroll
-          for (int i = 0; i < kCols; i += 2)
-            any |= __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic)) |
-                   __float_as_uint(__fadd_rn(__uint_as_float(raw[i + 1]), magic));
-          const bool cand = row_ok && (any & 0x40200u);
-          need = __any_sync(0xffffffffu, cand);
-          uint64_t mask = 0;
-          if (cand) {
-#pragma unroll
-            for (int i = 0; i < kCols; ++i) {
-              const uint32_t x = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic));
-              mask |= static_cast<uint64_t>((x >> 9) & 1u) << (2 * i);
-              mask |= static_cast<uint64_t>((x >> 18) & 1u) << (2 * i + 1);
-            }
-          }
-          return mask;
-        };
-        using C32 = std::integral_constant<int, 32>;
-        using C16 = std::integral_constant<int, 16>;
         uint32_t raw0[32], raw1[32];
         float unused[32];
+        // round 1: pairs 0..63 of the group
+        tmem_ld32_nowait(cols, raw0);
+        tmem_ld32_nowait(cols + 32, raw1);
+        tmem_ld_wait();
+        tmem_take(raw0, unused);
+        tmem_take(raw1, unused);
+        const bool mine1 = row_ok && ((chunk_any(raw0, C32{}) | chunk_any(raw1, C32{})) & 0x40200u);
+        const bool need1 = __any_sync(0xffffffffu, mine1);
+        uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0;
+        if (need1 && mine1) {
+          m0 = chunk_mask(raw0, C32{});
+          m1 = chunk_mask(raw1, C32{});
+        }
+        // round 2: pairs 64.. of the group
+        bool mine2;
         if constexpr (kFp4) {
-          uint32_t raw2[16];
-          tmem_ld32_nowait(tmem_base + lane_addr + col0, raw0);
-          tmem_ld32_nowait(tmem_base + lane_addr + col0 + 32, raw1);
-          tmem_ld16_nowait(tmem_base + lane_addr + col0 + 64, raw2);
+          uint32_t raw2[16], raw3[8];
+          tmem_ld32_nowait(cols + 64, raw0);
+          tmem_ld16_nowait(cols + 96, raw2);
+          tmem_ld8_nowait(cols + 112, raw3);
           tmem_ld_wait();
           tmem_take(raw0, unused);
-          tmem_take(raw1, unused);
           tmem_take16(raw2);
-          // the whole stage is in registers: hand it back before decoding
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
-          bool need[3];
-          uint64_t mask[3];
-          mask[0] = chunk_mask(raw0, C32{}, need[0]);
-          mask[1] = chunk_mask(raw1, C32{}, need[1]);
-          mask[2] = chunk_mask(raw2, C16{}, need[2]);
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-            if (need[i]) emit_candidates(mask[i], row, q_first + 64 * i, n_queries, prm, lane);
+          tmem_take8(raw3);
+          mine2 = row_ok && ((chunk_any(raw0, C32{}) | chunk_any(raw2, C16{}) |
+                              chunk_any(raw3, C8{})) & 0x40200u);
+          if (mine2) {
+            m2 = chunk_mask(raw0, C32{});
+            m3 = chunk_mask(raw2, C16{});
+            m4 = chunk_mask(raw3, C8{});
+          }
         } else {
-          uint64_t mask[4];
-          bool need[4];
-          tmem_ld32_nowait(tmem_base + lane_addr + col0, raw0);
-          tmem_ld32_nowait(tmem_base + lane_addr + col0 + 32, raw1);
+          tmem_ld32_nowait(cols + 64, raw0);
+          tmem_ld32_nowait(cols + 96, raw1);
           tmem_ld_wait();
           tmem_take(raw0, unused);
           tmem_take(raw1, unused);
-          mask[0] = chunk_mask(raw0, C32{}, need[0]);
-          mask[1] = chunk_mask(raw1, C32{}, need[1]);
-          tmem_ld32_nowait(tmem_base + lane_addr + col0 + 64, raw0);
-          tmem_ld32_nowait(tmem_base + lane_addr + col0 + 96, raw1);
-          tmem_ld_wait();
-          tmem_take(raw0, unused);
-          tmem_take(raw1, unused);
-          // the stage's last columns are in registers: hand it back before the hit reporting
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
-          mask[2] = chunk_mask(raw0, C32{}, need[2]);
-          mask[3] = chunk_mask(raw1, C32{}, need[3]);
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (need[i]) emit_candidates(mask[i], row, q_first + 64 * i, n_queries, prm, lane);
+          mine2 = row_ok && ((chunk_any(raw0, C32{}) | chunk_any(raw1, C32{})) & 0x40200u);
+          if (mine2) {
+            m2 = chunk_mask(raw0, C32{});
+            m3 = chunk_mask(raw1, C32{});
+          }
+        }
+        // decoded: reset the warp's columns (one wait for all stores: a store's source
+        // registers stay reserved until then) and hand the stage back before any hit reporting
+        fill_group(cols);
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+        // each chunk's candidates re-checked exactly (all lanes take part); the chunk starts
+        // at pair `pair` of the group
+        auto report = [&](uint64_t m, uint32_t pair) {
+          if (__any_sync(0xffffffffu, m != 0))
+            emit_candidates_call(m, row, q_first + 2 * pair, n_queries, &prm, lane);
+        };
+        if (need1) {
+          report(m0, 0);
+          report(m1, 32);
+        }
+        if (__any_sync(0xffffffffu, mine2)) {
+          report(m2, 64);
+          report(m3, 96);
+          if constexpr (kFp4) report(m4, 112);
         }
       }
     }

@@ -13,6 +13,9 @@ reference's formats (src/main.rs:683-773):
   hex / HEX            64 hex digits, lower / upper case
   bin / BIN            256 '0'/'1' characters, byte by byte, most significant bit first
   q+hex, q+HEX, q+bin  prefixed with the quality x 100 as "{:02.3}" and ':'
+  diagnostic           per hash: its dihedral, its index in the frame, quality, threshold,
+                       the 256 bits and the 16 x 16 PDQF with '*' on coefficients above the
+                       threshold (src/main.rs:738-773)
   ...+lf / +crlf / +cr / +nul / +nl   a separator after every hash
 With --db the frames go through the continuous-batching server (ypdq_server_*), which also
 matches all 8 hashes of each frame against the database; after a frame's hashes one line
@@ -39,7 +42,17 @@ FORMATS = {  # name -> (kind, upper, quality prefix)
     "bin": ("bin", False, False), "BIN": ("bin", False, False),
     "q+hex": ("hex", False, True), "q+HEX": ("hex", True, True),
     "q+bin": ("bin", False, True), "q+BIN": ("bin", False, True),
+    "diagnostic": ("diagnostic", False, False),
 }
+# The diagnostic header of each slot: the reference prints `{:?}` of its name, "original"
+# for the hash itself and the Dihedrals value (a u32 of four big-endian i8 matrix entries,
+# src/lib.rs:85-134) for each derived hash, in visit order (src/lib.rs:358-420).
+DIHEDRAL_PACKED = (None, 0xFF000001, 0xFF0000FF, 0x010000FF, 0x00FFFF00, 0x00010100, 0x00FF0100,
+                   0x0001FF00)
+
+
+def slot_name(slot):
+    return '"original"' if slot == 0 else "Dihedrals { packed: %d }" % DIHEDRAL_PACKED[slot]
 
 
 def parse_format(spec):
@@ -75,6 +88,22 @@ def format_hash(hash32, quality, kind, upper, with_quality, sep):
         else:
             out = pre + "".join(format(b, "08b") for b in h).encode()
     return out + sep
+
+
+def format_diagnostic(slot, index, hash32, quality, threshold, pdqf, sep):
+    """One hash in the reference's diagnostic format: `[name]`, `Index: i` (the hash's position
+    among the frame's outputs), `Quality: {0:02.3}` of quality x 100, `Threshold: {0:.7}`,
+    `Hash:` and its 256 bits on one line, `PDQF:` and 16 rows of 16 tab-separated `{:.5}`
+    values, each prefixed by '*' when it exceeds the threshold (all f32)."""
+    t = np.float32(threshold)
+    q100 = float(np.float32(quality) * np.float32(100.0))
+    bits = "".join(format(b, "08b") for b in bytes(hash32))
+    rows = []
+    for row in np.asarray(pdqf, np.float32).reshape(16, 16):
+        rows.append("\t".join(("*" if v > t else "") + "%.5f" % float(v) for v in row))
+    text = ("[%s]\nIndex: %d\nQuality: %.3f\nThreshold: %.7f\nHash:\n%s\nPDQF:\n%s\n"
+            % (slot_name(slot), index, q100, float(t), bits, "\n".join(rows)))
+    return text.encode() + sep
 
 
 def read_frames(stream, bpp, max_frames):
@@ -127,11 +156,21 @@ def main(argv=None):
     fout = sys.stdout.buffer if a.output == "-" else open(a.output, "wb")
     slots = 8 if a.dihedrals else 1
     text = kind != "raw"
+    diag = kind == "diagnostic"
     dct = 0x200 if a.reference_kernel else 0  # YPDQ_COMPRESS_JAROSZ or the FP32 default
 
-    def emit(hashes, quality, hits_per_frame):
+    def hash_frames(frames):
+        return yp.hash_batch(ctx, frames, semantics=a.semantics, dct=dct, want_pdqf=diag,
+                             pdqf_slots=8 if diag else 1)
+
+    def emit(hashes, quality, hits_per_frame, extra=None):
         for f in range(hashes.shape[0]):
             for s in range(slots):
+                if diag:
+                    fout.write(format_diagnostic(s, s, hashes[f, s], quality[f, s],
+                                                 extra["thresholds"][f, s], extra["pdqf"][f, s],
+                                                 sep))
+                    continue
                 fout.write(format_hash(hashes[f, s], quality[f, s], kind, upper, with_quality, sep))
             if hits_per_frame is not None and text:
                 for h in hits_per_frame[f]:
@@ -142,8 +181,8 @@ def main(argv=None):
             frames = read_frames(fin, bpp, a.batch)
             if frames is None:
                 break
-            out = yp.hash_batch(ctx, frames, semantics=a.semantics, dct=dct)
-            emit(out["hashes"], out["quality"], None)
+            out = hash_frames(frames)
+            emit(out["hashes"], out["quality"], None, out)
             fout.flush()
     else:
         db = yp.Database.from_file(ctx, a.db)
@@ -151,7 +190,7 @@ def main(argv=None):
         batch = 1 << max(0, (a.batch - 1).bit_length())
         with yp.Server(ctx, db, threshold=a.threshold, input_kind=in_kind, dct=dct,
                        semantics=a.semantics, max_step_images=batch) as srv:
-            pending, done = [], {}
+            pending, done, frames_of = [], {}, {}
 
             def flush_ready():
                 # results in stream order: emit the oldest requests that have completed
@@ -161,7 +200,10 @@ def main(argv=None):
                         raise RuntimeError("request %d failed with status %d"
                                            % (r.request_id, r.status))
                     per_frame = [r.hits[(r.hits["query"] >> 3) == f] for f in range(r.n_images)]
-                    emit(r.hashes, r.quality, per_frame)
+                    # the server returns hashes and qualities; the diagnostic format also
+                    # needs each slot's threshold and PDQF, from the hash path
+                    fr = frames_of.pop(r.request_id)
+                    emit(r.hashes, r.quality, per_frame, hash_frames(fr) if diag else None)
 
             while True:
                 frames = read_frames(fin, bpp, batch)
@@ -174,6 +216,7 @@ def main(argv=None):
                     done.update((r.request_id, r) for r in srv.poll(timeout_us=1000))
                     flush_ready()
                 pending.append(rid)
+                frames_of[rid] = frames if diag else None
                 done.update((r.request_id, r) for r in srv.poll(timeout_us=0))
                 flush_ready()
             done.update((r.request_id, r) for r in srv.drain())
