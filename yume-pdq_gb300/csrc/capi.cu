@@ -146,10 +146,10 @@ struct ChunkCost {
   double fixed_us, per_image_us;
 };
 ChunkCost screen_chunk_cost(int input_kind, bool jarosz, uint64_t n_rows, uint32_t threshold) {
-  // the tensor-core scan: 13.1 T (row, query) pairs/s in passes of 512 queries taken in
+  // the tensor-core scan: 14.0 T (row, query) pairs/s in passes of 512 queries taken in
   // pairs (the 128-bit prefix bound), 9.5 T with the 192-bit bound, 8.3 T with all 256
   // bits; 8 queries per image
-  const double pairs_per_us = threshold <= 36 ? 13.1e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
+  const double pairs_per_us = threshold <= 36 ? 14.0e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
   const double scan_us = 8.0 * static_cast<double>(n_rows) / pairs_per_us;
   // the Jarosz filter: four passes, each at least one line's sequential replay (512
   // dependent steps, ~5 us) however few images the chunk holds, plus the DCT

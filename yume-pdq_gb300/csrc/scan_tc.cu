@@ -691,7 +691,7 @@ constexpr int kPairAStages = 4;             // A tiles in shared memory (16 KiB 
 // tensor memory beside the accumulators, so a stage holds 240 pairs (480 queries per pass):
 // stage s at columns 256 s .. 256 s + 239, scale factor 2^0 in columns 496-503 and 2^9 in
 // 504-511 (every byte of each region the same E8M0 value).
-constexpr int kPair4N = 240;
+constexpr int kPair4N = static_cast<int>(kPairFp4N);
 constexpr uint32_t kPairStageCols = 256;
 constexpr uint32_t kSfOneCol = 496, kSfBigCol = 504;  // 8 columns each
 constexpr uint32_t kE8m0One = 0x7F7F7F7Fu;  // 2^(127 - 127) in each byte
@@ -1609,12 +1609,13 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
     return cudaGetLastError();
   }
   if (p.pair_n && (!half_k || (p.pair_n != static_cast<uint32_t>(tc::kPairN) &&
-                                p.pair_n != static_cast<uint32_t>(tc::kPair4N))))
+                                p.pair_n != kPairFp4N)))
     return cudaErrorInvalidValue;  // pairs need the 128-bit bound (t <= 36)
   // at t <= 36, passes of 512 queries, two per accumulator column (scan_pair_kernel), when
-  // asked for or by default past one pass of 256; pair_n = 240: the FP4 form, passes of 480
+  // asked for or by default past one pass of 256; pair_n = kPairFp4N: the FP4 form (passes of
+  // 480 queries)
   if (half_k && !p.n_tile && (p.pair_n || p.n_queries > static_cast<uint32_t>(tc::kMaxN))) {
-    const bool fp4 = p.pair_n == static_cast<uint32_t>(tc::kPair4N);
+    const bool fp4 = p.pair_n == kPairFp4N;
     prm.n_tile = 2u * static_cast<uint32_t>(tc::pair_n_of(fp4));
     prm.a_stages = tc::kPairAStages;
     // layout: [fixed Smem][A: 4 x 16 KB][B: 2 x 256 pairs x 128 B][packed ring], 1024-aligned

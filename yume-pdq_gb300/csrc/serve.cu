@@ -468,10 +468,10 @@ ypdq_status autotune(ypdq_server* S) {
     for (uint32_t nt = 64; nt <= 256; nt *= 2)
       if (nt <= nq64 || nt == 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, nt, 0, 0.0f, 0});
     // two queries per accumulator column (t <= 36): passes of 512 queries (FP8 operands)
-    // and of 480 (block-scaled FP4 operands)
+    // and of 2 kPairFp4N (block-scaled FP4 operands)
     if (S->cfg.threshold <= 36 && nq > 128) {
       cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, 256, 0.0f, 0});
-      cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, 240, 0.0f, 0});
+      cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, kPairFp4N, 0.0f, 0});
     }
     float best = 0.0f;
     for (Bucket& c : cand) {
@@ -686,7 +686,7 @@ ypdq_status ypdq_server_get_stats(ypdq_server* S, ypdq_server_stats* o, int rese
     const bool tc = b.algo == YPDQ_SCAN_TC;
     // tensor-core kernel: 0 one query per column (n_tile), 1 pairs, 2 queries as A, 3 FP4
     // pairs
-    o->bucket_kernel[i] = !tc ? 0 : b.pair_n == 240 ? 3 : b.pair_n ? 1 : b.n_tile ? 0 : 2;
+    o->bucket_kernel[i] = !tc ? 0 : b.pair_n == kPairFp4N ? 3 : b.pair_n ? 1 : b.n_tile ? 0 : 2;
     o->bucket_n_tile[i] = !tc ? 0 : b.pair_n ? 2 * b.pair_n : b.n_tile ? b.n_tile : 128;
     o->bucket_ms[i] = S->buckets[i].ms;
     o->bucket_steps[i] = S->buckets[i].steps;

@@ -11,6 +11,9 @@ namespace ypdq {
 // Device-side error bits, OR-ed into the context's error word by a kernel that gives up.
 constexpr int kDevErrTimeout = 1;
 
+// Pairs per pass of the FP4 pair scan (pair_n of its launches): 2 queries per pair.
+constexpr uint32_t kPairFp4N = 240;
+
 // Longest time a device-side wait spins before the kernel reports a timeout and returns.
 constexpr uint64_t kWaitLimitNs = 4ull * 1000 * 1000 * 1000;
 
@@ -197,8 +200,8 @@ struct ScanLaunch {
   uint32_t n_tile;         // tensor-core scan: queries per pass (multiple of 64, <= 256);
                            // 0 picks min(256, n_queries rounded up to 64)
   uint32_t pair_n;         // tensor-core scan at t <= 36: 256 = passes of 256 query pairs,
-                           // two per accumulator column (FP8 operands); 240 = passes of 240
-                           // pairs with block-scaled FP4 operands; with n_tile and pair_n
+                           // two per accumulator column (FP8 operands); kPairFp4N = passes of
+                           // that many pairs with block-scaled FP4 operands; with n_tile and pair_n
                            // both 0 the launcher takes pairs past 256 queries
 };
 
