@@ -287,7 +287,12 @@ def serve_run(yp, srv, pool, rate, seconds, rng, hit_cap=4096):
     """Open-loop Poisson arrivals at `rate` req/s (rate None: submit whenever the queue has
     room, i.e. saturation) of log-uniform 1..64-image requests sliced from `pool`. Returns
     the server's window statistics once every accepted request has completed."""
+    import gc
     n_pool = pool.shape[0]
+    # the arrivals come from this loop: a collector pause would submit the requests it owes
+    # at once, a burst the arrival process does not have
+    gc.collect()
+    gc.disable()
     srv.stats(reset=True)
     t0 = time.perf_counter()
     t_next = t0
@@ -310,6 +315,7 @@ def serve_run(yp, srv, pool, rate, seconds, rng, hit_cap=4096):
             srv.poll(timeout_us=200)
         srv.poll(timeout_us=0)
     srv.drain()
+    gc.enable()
     st = srv.stats()
     return {"offered_req_s": rate, "seconds": round(st["elapsed_s"], 3),
             "completed_req_s": st["completed"] / st["elapsed_s"],
