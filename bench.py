@@ -4,8 +4,10 @@
 One step screens a batch of B synthetic 512x512 f32 images: hash each (FP32, bit-exact with
 yume-pdq's scalar kernel), derive its 8 dihedral hashes, and scan all 8B hashes exactly
 against a device-resident 10,000,000-row database at Hamming threshold 31. `value` is
-images/s with inputs already in HBM. `e2e` is the same metric through ypdq_screen_host:
-host (pinned) images in, sorted hits out, copies inside the timed region.
+images/s with inputs already in HBM. `e2e` is the same metric for a stream of such batches
+from pinned host memory through the C ABI's serving loop (ypdq_server_*), sorted hits back
+in host memory, every copy inside the timed region; `e2e_blocking` through one blocking
+ypdq_screen_host call per batch.
 
 --impl reference times yume-pdq's CPU path (the CPU oracle, a restatement of its scalar
 kernel and scalar matcher) on this host's cores on a bounded sample of the same workload.
@@ -598,6 +600,7 @@ def run_ours(args):
                                         B * args.steps)
     e2e_hits = h_hits[:min(nh.value, len(h_hits))].copy()
     ctx.lib.ypdq_free_host(ctx.handle, h_img)
+    stream_e2e = e2e_stream(yp, ctx, db, batch, args, pg, world, hits_per_step)
     # the serving sweep, the heavy-hit database and the precision variants describe one GPU:
     # rank 0 runs them (the other replicas wait at the final barrier)
     serve = serving(yp, ctx, db, batch, args) if rank == 0 else None
@@ -692,8 +695,18 @@ def run_ours(args):
         "scan_sweep": sweep,
         "large_db": large,
         "dct_variants": dctv,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": B * 512 * 512 * 4,
-                "d2h_bytes_per_step": hits_per_step * 16 + 8},
+        "e2e": {"value": stream_e2e["value"], "unit": UNIT,
+                "h2d_bytes_per_step": B * 512 * 512 * 4,
+                "d2h_bytes_per_step": hits_per_step * 16 + 8,
+                "path": "ypdq_server_* (the C ABI's serving loop, 3 slots): %d requests of %d "
+                        "pinned host f32 images each, hits back to host memory; the copies of "
+                        "one step overlap the hash and scan of another" % (args.steps, B),
+                "ms_per_step": stream_e2e["ms_per_step"],
+                "request_latency_ms": stream_e2e["latency_ms"]},
+        "e2e_blocking": {"value": e2e_value, "unit": UNIT,
+                         "path": "one blocking ypdq_screen_host call per batch of %d pinned "
+                                 "host images (copies and compute overlap inside the call "
+                                 "only)" % B},
         "roofline": roofline,
         "hash_kernel": {"ms": hash_avg, "GB/s": hash_gbs, "frac_hbm": hash_gbs / hbm_peak},
         "gpu_launches": args.steps * (1 + scan_launches),
@@ -702,7 +715,8 @@ def run_ours(args):
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline(args, args.cpu_sample,
                                            workload=(batch[:args.cpu_sample], rows))
-        out["parity"] = parity_check(args, batch, rows, gpu_step_hits, step_hits, e2e_hits)
+        out["parity"] = parity_check(args, batch, rows, gpu_step_hits, step_hits, e2e_hits,
+                                     stream_e2e["hits"])
         print(json.dumps(out))
     if pg:
         pg.barrier()
@@ -725,7 +739,49 @@ def cpu_workload(args, sample):
     return imgs[:sample], rows
 
 
-def parity_check(args, imgs, rows, gpu_hits, gpu_count, e2e_hits):
+def e2e_stream(yp, ctx, db, batch, args, pg, world, hits_per_step):
+    """The same metric for a stream of batches through the serving loop (ypdq_server_*):
+    --steps requests of the step's B pinned host images each, hashed and matched exactly at
+    the bench threshold. Every request's 1 GiB image copy and its hit list's copy back are
+    inside the timed region; the server overlaps one step's copies with another step's
+    hash and scan (3 slots), which one blocking ypdq_screen_host call per batch cannot do.
+    Returns images/s (all ranks' images over the slowest rank's time), the request
+    latencies and the last request's hits (sorted, query numbers local to the request)."""
+    B = batch.shape[0]
+    pin = yp.PinnedArray(ctx, batch.shape, np.float32)
+    pin.array[:] = batch
+    cap = max(hits_per_step, 1) * 2
+    srv = yp.Server(ctx, db, threshold=args.threshold, dct=args.dct, max_step_images=B,
+                    slots=3, max_queued_images=3 * B)
+
+    def run(k):
+        done, sent = [], 0
+        while sent < k:
+            if srv.try_submit(pin.array, hit_capacity=cap) is not None:
+                sent += 1
+            else:
+                done.extend(srv.poll(timeout_us=-1))
+        done.extend(srv.drain())
+        return done
+
+    run(max(1, args.warmup))
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    res = run(args.steps)
+    wall_ms = (time.perf_counter() - t0) * 1e3
+    _, value = aggregate_over_ranks(pg, wall_ms, world, B * args.steps)
+    assert all(r.ok for r in res) and len(res) == args.steps
+    last = max(res, key=lambda r: r.request_id)
+    lat = sorted(r.latency_us / 1e3 for r in res)
+    srv.close()
+    pin.free()
+    return {"value": value, "ms_per_step": wall_ms / args.steps,
+            "latency_ms": {"p50": statistics.median(lat), "max": lat[-1]},
+            "hits": last.hits.copy()}
+
+
+def parity_check(args, imgs, rows, gpu_hits, gpu_count, e2e_hits, stream_hits=None):
     """The timed step against the oracle, once, after the timed regions: the oracle hashes
     the step's images (its f32 pipeline) and its scalar matcher lists every hit of the 8B
     hashes in the same planted rows. Equal when the GPU step's sorted hit list and the last
@@ -740,13 +796,17 @@ def parity_check(args, imgs, rows, gpu_hits, gpu_count, e2e_hits):
     def same(h):
         return (len(h) == len(want) and all(np.array_equal(h[f], want[f])
                                             for f in ("index", "query", "distance")))
-    return {"gpu_hits": int(gpu_count), "oracle_hits": int(len(want)),
-            "equal": bool(gpu_count == len(want) and same(gpu_hits)),
-            "e2e_equal": bool(same(e2e_hits)),
-            "oracle_s": round(time.perf_counter() - t0, 2),
-            "what": "sorted (index, query, distance) lists of the timed step and of the last "
-                    "ypdq_screen_host call vs the oracle's scalar matcher over all %d x %d pairs "
-                    "of the same planted rows" % (8 * len(imgs), rows.shape[0])}
+    out = {"gpu_hits": int(gpu_count), "oracle_hits": int(len(want)),
+           "equal": bool(gpu_count == len(want) and same(gpu_hits)),
+           "e2e_equal": bool(same(e2e_hits)),
+           "oracle_s": round(time.perf_counter() - t0, 2),
+           "what": "sorted (index, query, distance) lists of the timed step, of the last "
+                   "ypdq_screen_host call and of the last streamed request vs the oracle's "
+                   "scalar matcher over all %d x %d pairs of the same planted rows"
+                   % (8 * len(imgs), rows.shape[0])}
+    if stream_hits is not None:
+        out["e2e_stream_equal"] = bool(same(stream_hits))
+    return out
 
 
 def cpu_time(args, imgs, rows):
