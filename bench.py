@@ -612,8 +612,8 @@ def run_ours(args):
     hash_avg = statistics.mean(hash_ms)
     scan_avg = statistics.mean(scan_ms)
     algo = scan_algo_used(args.algo, nq, args.threshold)
-    scan_launches = 1 if algo == 3 else (nq + 2047) // 2048
-    if scan_avg >= hash_avg and algo == 3:
+    scan_launches = 1 if algo in (3, 4) else (nq + 2047) // 2048
+    if scan_avg >= hash_avg and algo in (3, 4):
         # tensor-core scan, one launch per step: FP8 flops the MMAs execute per (row, query)
         # pair, 2 * K: K = 128 at t <= 36 and 192 for passes of 256 queries at t <= 62 (the
         # prefix bound; mirrors launch_scan_tc), else 256. Peak: the dense FP8 burst measured
@@ -622,22 +622,34 @@ def run_ours(args):
                   192 if (nq > 128 and args.threshold <= 62) else 256)
         flops = 2.0 * k_bits * nq * n
         achieved = flops / (scan_avg / 1000.0) / 1e12
-        fp8 = fp8_dense_burst(local) if rank == 0 else None
-        peak = fp8 if fp8 else 2 * bf16_peak
-        # past 256 queries at t <= 36 the launch runs passes of 512 queries, two per
-        # accumulator column (mirrors launch_scan_tc)
+        # past 256 queries at t <= 36 the launch runs several queries per accumulator column:
+        # FP8 pairs (passes of 512) or FP4 triples (passes of 720), whichever needs fewer
+        # pass-costs (mirrors launch_scan_tc)
         pairs = args.threshold <= 36 and nq > 256
-        per_pass = 512 if pairs else 256
+        triples = pairs and (83 * -(-nq // 720) < 72 * -(-nq // 512)
+                             or args.algo == 4)
+        per_pass = 720 if triples else 512 if pairs else 256
         passes = (nq + per_pass - 1) // per_pass
+        if triples:
+            fp4 = fp4_dense_burst(local) if rank == 0 else None
+            peak = fp4 if fp4 else 2 * fp8_dense_burst(local)
+            peak_source = ("measured fp4 burst (torch._scaled_mm, e2m1 with e4m3 scales per 16, "
+                           "8192^3, best of 10, this GPU, this run)" if fp4 else
+                           "measured fp8 burst x 2 (fp4 dense)")
+            kernel = ("scan_pair_kernel<2> (tcgen05 kind::mxf4 block-scaled e2m1, three queries "
+                      "per f32 accumulator column)")
+        else:
+            fp8 = fp8_dense_burst(local) if rank == 0 else None
+            peak = fp8 if fp8 else 2 * bf16_peak
+            peak_source = ("measured fp8 burst (torch._scaled_mm e4m3 8192^3, best of 10, this "
+                           "GPU, this run)" if fp8 else "%s bf16 burst x 2 (fp8 dense)" % peak_kind)
+            kernel = ("scan_pair_kernel<0> (tcgen05 kind::f8f6f4, e5m2, two queries per f32 "
+                      "accumulator column)" if pairs else "scan_tc_kernel (tcgen05 kind::f8f6f4)")
         roofline = {"bound": "tensor",
-                    "kernel": ("scan_pair_kernel (tcgen05 kind::f8f6f4, e5m2, two queries per f32 "
-                               "accumulator column)" if pairs else
-                               "scan_tc_kernel (tcgen05 kind::f8f6f4)"),
+                    "kernel": kernel,
                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak,
-                    "peak_source": ("measured fp8 burst (torch._scaled_mm e4m3 8192^3, best of "
-                                    "10, this GPU, this run)" if fp8 else
-                                    "%s bf16 burst x 2 (fp8 dense)" % peak_kind),
+                    "peak_source": peak_source,
                     "traffic": (passes * NCU_DRAM_BYTES_PER_PASS_10M * (n / 1e7)
                                 + hits_per_step * 16.0 if pairs else None),
                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a "
@@ -647,6 +659,8 @@ def run_ours(args):
                     "traffic_note": "traffic_computed = 32 B x rows x %d query passes of %d + 16 B "
                                     "per hit (the database streams once per pass), computed, not "
                                     "a counter" % (passes, per_pass),
+                    "mma_flop_note": "2 x %d FLOP per (row, query) pair: the K the MMAs execute "
+                                     "per query" % k_bits,
                     "launch_ms": scan_avg, "launches_per_step": 1,
                     "mma_k_bits": k_bits,
                     "pairs_per_s": nq * n / (scan_avg / 1e3),
@@ -682,7 +696,9 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (images %d MiB, DB %d MiB > 129 MB L2)"
                          % (B * 4 * 512 * 512 >> 20, n * 32 >> 20),
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "scan_algo": {1: "simt", 2: "b1mma", 3: "tcgen05_fp8"}[algo]},
+                   "scan_algo": ({1: "simt", 2: "b1mma"}.get(algo) or
+                                 ("tcgen05 fp4 triples" if roofline.get("kernel", "").startswith(
+                                     "scan_pair_kernel<2>") else "tcgen05 fp8"))},
         "kernels_ms": {"hash": hash_avg, "scan": scan_avg},
         "latency_ms": ({"p50": serve["points"][0]["p50_ms"], "p99": serve["points"][0]["p99_ms"],
                         "at": "serving loop, %g req/s Poisson" % serve["points"][0]["offered_req_s"]}

@@ -133,8 +133,11 @@ typedef enum {
   YPDQ_SCAN_SIMT = 1,   /* XOR + popcount, one row per thread */
   YPDQ_SCAN_B1MMA = 2,  /* legacy binary MMA (mma.sync .b1 .xor.popc) */
   YPDQ_SCAN_TC = 3,     /* tcgen05 FP8 tensor cores on +-1 vectors: dot = 256 - 2 d */
-  YPDQ_SCAN_TC_FP4 = 4  /* tcgen05 block-scaled FP4 (e2m1) pairs, passes of 480 queries, at
-                           threshold <= 36; above that the same as YPDQ_SCAN_TC */
+  YPDQ_SCAN_TC_FP4 = 4  /* tcgen05 block-scaled FP4 (e2m1), three queries per accumulator
+                           column, passes of 720 queries, at threshold <= 36; above that the
+                           same as YPDQ_SCAN_TC (which, past 256 queries at threshold <= 36,
+                           itself takes this form or FP8 pairs, whichever needs fewer
+                           pass-costs) */
 } ypdq_scan_algo;
 
 /* ------------------------------------------------------------------ context */
@@ -430,7 +433,7 @@ typedef struct {
   uint32_t bucket_kernel[YPDQ_SERVER_MAX_BUCKETS];  /* tensor-core scan form: 0 one query per
                                                        accumulator column, 1 two per column,
                                                        2 queries as the MMA's A operand,
-                                                       3 two per column with FP4 operands */
+                                                       3 three per column, FP4 operands */
 } ypdq_server_stats;
 
 /* Fills cfg with the defaults above (threshold 31, f32 input, FP32 DCT, exact semantics). */

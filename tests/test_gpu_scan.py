@@ -346,22 +346,26 @@ def test_pair_kernel_matches_oracle(ctx, yp, oracle, n_q):
             assert np.array_equal(as_tuples(got), as_tuples(want)), (t, algo, len(got), len(want))
 
 
-@pytest.mark.parametrize("n_q", [1, 2, 239, 240, 241, 479, 480, 481, 961])
-def test_fp4_pair_kernel_matches_oracle(ctx, yp, oracle, n_q):
-    """YPDQ_SCAN_TC_FP4: the pair kernel with block-scaled e2m1 operands (K = 64 per MMA,
-    the second query of a pair scaled by 2^9 through its scale factors), passes of 480
-    queries. Pass boundaries, a pair with one query, rows equal or complementary to a
-    query on the 128-bit prefix (d = +-128 in either half of a column), every threshold
-    0..36 at one size; above 36 the call runs the FP8 scan."""
+@pytest.mark.parametrize("n_q", [1, 2, 3, 239, 241, 479, 719, 720, 721, 1441])
+def test_fp4_triple_kernel_matches_oracle(ctx, yp, oracle, n_q):
+    """YPDQ_SCAN_TC_FP4: block-scaled e2m1 operands (K = 64 per MMA), three queries per f32
+    accumulator column (B scale factors 2^-1, 2^7, 2^15), passes of 720 queries, the first
+    126 bits as the bound. Pass boundaries, triples with one or two queries, rows equal or
+    complementary to a query on the prefix (every field at its extreme), rows that differ from
+    a query only in the two prefix bits the bound leaves out (distance 2: found, with the
+    full distance), every threshold 0..36 at one size; above 36 the call runs the FP8 scan."""
     rows = yp.synth.rows_128(6000, seed=n_q + 900)
     q = yp.synth.rows_128(n_q, seed=n_q + 901)
     yp.synth.plant(rows, q, 300, 0, 40, seed=9)
     rows[10], rows[11] = q[0], ~q[n_q - 1]
     rows[14, :16], rows[14, 16:] = q[n_q // 2, :16], ~q[n_q // 2, 16:]
     rows[15, :16], rows[15, 16:] = ~q[n_q - 1, :16], q[n_q - 1, 16:]
+    for i in range(3):                                 # one row per field of a triple
+        rows[20 + i] = q[min(i, n_q - 1)]
+        rows[20 + i, 15] ^= np.uint8(0xC0)             # bits 126 and 127 of the prefix
     rows[5999] = q[0]                                  # the last, partial tile
     rows[200:264] = q[np.arange(64) % n_q]             # many hits in one tile
-    ts = range(37) if n_q == 481 else (0, 1, 16, 31, 35, 36, 40)
+    ts = range(37) if n_q == 721 else (0, 1, 2, 16, 31, 35, 36, 40)
     for t in ts:
         want = oracle.find_all(rows, q, t)
         got = yp.scan(ctx, rows, q, t, algo=yp._lib.SCAN_TC_FP4)

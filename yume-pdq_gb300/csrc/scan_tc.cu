@@ -250,13 +250,14 @@ __device__ __forceinline__ uint64_t candidate_mask(const uint32_t (&raw)[32], fl
 // lane without candidates passes cand = 0. The loops run once per candidate of the lane,
 // which keeps this rare path short: it runs while the tile's epilogue warp holds up the next
 // tile, and a planted near-duplicate row makes it run for several queries of a pass.
+// (stride: bit j of cand stands for query q_first + stride * j; 1 unless given.)
 __device__ __forceinline__ void emit_candidates(uint64_t cand, uint64_t row, uint64_t q_first,
                                                 uint32_t n_queries, const Params& prm,
-                                                int lane) {
-  if (q_first >= n_queries) {
-    cand = 0;
-  } else if (n_queries - q_first < 64) {
-    cand &= (1ull << (n_queries - q_first)) - 1;
+                                                int lane, uint32_t stride = 1) {
+  {
+    // bits whose query is past the end
+    const uint64_t lim = q_first >= n_queries ? 0 : (n_queries - q_first + stride - 1) / stride;
+    if (lim < 64) cand &= (1ull << lim) - 1;
   }
   uint4 r0 = make_uint4(0, 0, 0, 0), r1 = r0;
   if (cand) {
@@ -268,7 +269,7 @@ __device__ __forceinline__ void emit_candidates(uint64_t cand, uint64_t row, uin
   uint64_t hits = 0;
   for (uint64_t m = cand; m; m &= m - 1) {
     const int j = __ffsll(static_cast<long long>(m)) - 1;
-    const uint4* qp = reinterpret_cast<const uint4*>(qbase + j * 32);
+    const uint4* qp = reinterpret_cast<const uint4*>(qbase + static_cast<uint64_t>(stride) * j * 32);
     if (popc256(r0, r1, __ldg(qp), __ldg(qp + 1)) <= prm.threshold) hits |= 1ull << j;
   }
   const uint32_t mine = static_cast<uint32_t>(__popcll(hits));
@@ -287,10 +288,10 @@ __device__ __forceinline__ void emit_candidates(uint64_t cand, uint64_t row, uin
   for (uint64_t m = hits; m; m &= m - 1, ++pos) {
     if (pos >= prm.capacity) break;
     const int j = __ffsll(static_cast<long long>(m)) - 1;
-    const uint4* qp = reinterpret_cast<const uint4*>(qbase + j * 32);
+    const uint4* qp = reinterpret_cast<const uint4*>(qbase + static_cast<uint64_t>(stride) * j * 32);
     ypdq_hit h;
     h.index = row;
-    h.query = static_cast<uint32_t>(q_first + j) + prm.query_base;
+    h.query = static_cast<uint32_t>(q_first + static_cast<uint64_t>(stride) * j) + prm.query_base;
     h.distance = popc256(r0, r1, __ldg(qp), __ldg(qp + 1));
     prm.hits[pos] = h;
   }
@@ -300,8 +301,8 @@ __device__ __forceinline__ void emit_candidates(uint64_t cand, uint64_t row, uin
 // candidate, and inlined at each of its chunks it would crowd the registers of the common path.
 __device__ __noinline__ void emit_candidates_call(uint64_t cand, uint64_t row, uint64_t q_first,
                                                   uint32_t n_queries, const Params* prm,
-                                                  int lane) {
-  emit_candidates(cand, row, q_first, n_queries, *prm, lane);
+                                                  int lane, uint32_t stride) {
+  emit_candidates(cand, row, q_first, n_queries, *prm, lane, stride);
 }
 
 __device__ __forceinline__ void raise_abort(Smem& sm, int* dev_err) {
@@ -697,6 +698,31 @@ constexpr uint32_t kSfOneCol = 496, kSfBigCol = 504;  // 8 columns each
 constexpr uint32_t kE8m0One = 0x7F7F7F7Fu;  // 2^(127 - 127) in each byte
 constexpr uint32_t kE8m0Big = 0x88888888u;  // 2^(136 - 127) = 512 in each byte
 __host__ __device__ constexpr int pair_n_of(bool fp4) { return fp4 ? kPair4N : kPairN; }
+
+// The triple form (kForm 2): three queries per f32 column, FP4 operands as above. The bound
+// is the first 126 bits (the queries' bits 126 and 127 expand to 0.0): per query the dot
+// product d is even and in [-126, 126], so e = d / 2 fits 7 bits. With B scale factors 2^-1,
+// 2^7 and 2^15 for queries 3j, 3j + 1 and 3j + 2 (A's scale 1), column j holds
+// v = e_a + 256 e_b + 65536 e_c: every 32-element block adds an integer (its 32 products of
+// +-1 sum to an even number), so with the stage starting at the decoding constant every
+// value is an integer in [2^23, 2^24) and f32 accumulation is exact. Scale regions of 8
+// columns in the two gaps the stages leave (columns 240-255 and 496-511): 2^0 at 240 (A),
+// 2^-1 at 248, 2^7 at 496, 2^15 at 504. A block-scaled MMA with N = 240 reads more than 4
+// columns of B scale factors (4-column regions made the last read run past column 511, an
+// illegal access) and at most 8 (the pair form's 8-column regions at 496 and 504 give exact
+// results). Passes of 720 queries.
+__host__ __device__ constexpr uint32_t sf_tri_col(int i) {
+  return i == 0 ? 240u : i == 1 ? 248u : i == 2 ? 496u : 504u;
+}
+__host__ __device__ constexpr uint32_t sf_tri_val(int i) {
+  return i == 0 ? 0x7F7F7F7Fu : i == 1 ? 0x7E7E7E7Eu : i == 2 ? 0x86868686u : 0x8E8E8E8Eu;
+}
+// forms of scan_pair_kernel
+constexpr int kFormFp8Pairs = 0, kFormFp4Pairs = 1, kFormFp4Triples = 2;
+__host__ __device__ constexpr int form_columns(int form) { return form == 0 ? kPairN : kPair4N; }
+__host__ __device__ constexpr int form_queries(int form) {
+  return (form == 2 ? 3 : 2) * form_columns(form);
+}
 // Both forms read their accumulator stage with 8 epilogue warps, two per TMEM lane quarter,
 // each warp half the stage's columns (128 for FP8, 120 for FP4) in two rounds.
 __host__ __device__ constexpr int pair_epilogue_warps(bool) { return 8; }
@@ -788,6 +814,10 @@ __device__ __forceinline__ void tmem_take16(uint32_t (&r)[16]) {
 // m (m = 0..3) holds bits m, m + 4, ..., m + 28 of the word in nibbles 0..7, which `<< (3 - m)`
 // moves to each nibble's sign bit. Rows and queries share the bijection, so the dot product
 // of two expanded rows is 128 - 2 * (prefix distance).
+// kUnit0: the first of the four 16-byte units written (0, or 4 for bytes 64-127 of the row).
+// kDrop2: the prefix's last two bits (126, 127: nibble 7 of output words 2 and 3 of packed
+// word 3) become 0.0, so the dot product covers the first 126 bits only.
+template <int kUnit0 = 0, bool kDrop2 = false>
 __device__ __forceinline__ void expand_row_fp4(const uint4 w0, uint8_t* chunk, int row) {
   const uint32_t words[4] = {w0.x, w0.y, w0.z, w0.w};
   uint8_t* const base = chunk + row * 128;
@@ -800,7 +830,11 @@ __device__ __forceinline__ void expand_row_fp4(const uint4 w0, uint8_t* chunk, i
     out.y = ((w << 2) & 0x88888888u) | 0x22222222u;
     out.z = ((w << 1) & 0x88888888u) | 0x22222222u;
     out.w = (w & 0x88888888u) | 0x22222222u;
-    *reinterpret_cast<uint4*>(base + ((p ^ sw) << 4)) = out;
+    if (kDrop2 && p == 3) {
+      out.z &= 0x0FFFFFFFu;
+      out.w &= 0x0FFFFFFFu;
+    }
+    *reinterpret_cast<uint4*>(base + (((kUnit0 + p) ^ sw) << 4)) = out;
   }
 }
 
@@ -815,6 +849,24 @@ __device__ __forceinline__ void mma_pair_issue(uint32_t d, uint32_t a0, uint32_t
     mma_f8(d, sw128_desc(a0 + 32 * ks), sw128_desc(b1 + 32 * ks), idesc, 1u);
 }
 
+// FP4 triples: two MMAs of K = 64 per query; queries 3j and 3j + 1 share B chunk 0 (bytes
+// 0-63 and 64-127 of a row), query 3j + 2 is B chunk 1.
+__device__ __forceinline__ void mma_triple4_issue(uint32_t d, uint32_t a0, uint32_t b0,
+                                                  uint32_t b1, uint32_t idesc, uint32_t sf) {
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks)
+    mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 32 * ks), idesc, sf + sf_tri_col(0),
+             sf + sf_tri_col(1), 1u);
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks)
+    mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 64 + 32 * ks), idesc,
+             sf + sf_tri_col(0), sf + sf_tri_col(2), 1u);
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks)
+    mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b1 + 32 * ks), idesc, sf + sf_tri_col(0),
+             sf + sf_tri_col(3), 1u);
+}
+
 // FP4: two MMAs of K = 64 per query of the pair; query 2j + 1's B scale is 2^9.
 __device__ __forceinline__ void mma_pair4_issue(uint32_t d, uint32_t a0, uint32_t b0,
                                                 uint32_t b1, uint32_t idesc, uint32_t sf_one,
@@ -827,11 +879,13 @@ __device__ __forceinline__ void mma_pair4_issue(uint32_t d, uint32_t a0, uint32_
     mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b1 + 32 * ks), idesc, sf_one, sf_big, 1u);
 }
 
-template <bool kFp4>
-__global__ void __launch_bounds__(pair_threads(kFp4), 1)
+template <int kForm>
+__global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
     scan_pair_kernel(const __grid_constant__ Params prm) {
-  constexpr int kN = pair_n_of(kFp4);       // pairs per pass
-  constexpr int kQueries = 2 * kN;          // queries per pass
+  constexpr bool kFp4 = kForm != kFormFp8Pairs;
+  constexpr bool kTriples = kForm == kFormFp4Triples;
+  constexpr int kN = form_columns(kForm);     // accumulator columns (pairs or triples) a pass
+  constexpr int kQueries = form_queries(kForm);
   // roles: epilogue warps 0 .. kEpi - 1, then the producer, the MMA issuer, four expanders
   constexpr int kEpi = pair_epilogue_warps(kFp4);
   constexpr int kProducerWarp = kEpi, kMmaWarp = kEpi + 1, kExpandWarp0 = kEpi + 2;
@@ -885,11 +939,15 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1)
     return;
   }
   // The decoding constant (see the epilogue) goes into every accumulator column, of both
-  // stages, before any MMA is issued; each epilogue warp writes its own columns. The FP4 form
-  // also fills its scale-factor regions: group 0 the 2^0 region, group 1 the 2^9 one.
+  // stages, before any MMA is issued; each epilogue warp writes its own columns. The FP4 forms
+  // also fill their scale-factor regions (pairs: group 0 the 2^0 region, group 1 the 2^9 one;
+  // triples: group 0 the regions at 496 and 500, group 1 those at 504 and 508).
   const float dot_min = 128.0f - 2.0f * static_cast<float>(prm.threshold);
+  // triples: 2^23 + 63 (1 + 256 + 65536) + 257 (t + 2), an integer below 2^24
   const uint32_t magic_bits =
-      __float_as_uint(8388608.0f + 65664.0f + 513.0f * (384.0f - dot_min));
+      kTriples ? __float_as_uint(8388608.0f + 4144959.0f +
+                                 257.0f * (static_cast<float>(prm.threshold) + 2.0f))
+               : __float_as_uint(8388608.0f + 65664.0f + 513.0f * (384.0f - dot_min));
   constexpr uint32_t kGroupCols = kFp4 ? 120 : 128;
   // (16 columns per store: a store's source is a block of consecutive registers)
   auto fill_cols = [&](uint32_t taddr, auto cols) {
@@ -906,9 +964,13 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1)
     const uint32_t g = static_cast<uint32_t>(warp >> 2);
     for (uint32_t st = 0; st < kAccStages; ++st)
       fill_group(tmem_base + lanes + st * kPairStageCols + kGroupCols * g);
-    if (kFp4 && warp < 8)
+    if constexpr (kTriples) {
+      tmem_st8_fill(tmem_base + lanes + sf_tri_col(2 * g), sf_tri_val(2 * g));
+      tmem_st8_fill(tmem_base + lanes + sf_tri_col(2 * g + 1), sf_tri_val(2 * g + 1));
+    } else if constexpr (kFp4) {
       tmem_st8_fill(tmem_base + lanes + (warp < 4 ? kSfOneCol : kSfBigCol),
                     warp < 4 ? kE8m0One : kE8m0Big);
+    }
     tmem_st_wait();
   }
   tc_fence_before();
@@ -959,6 +1021,32 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1)
     uint32_t slot = 0, phase = 0, ga = 0;
     for (uint32_t p = 0; p < n_passes; ++p) {
       if (!mbar_wait(&sm.b_empty, (p & 1u) ^ 1u, abort_flag, prm.wait_ns)) goto fail;
+      if constexpr (kTriples) {
+        // triple j: queries 3j and 3j + 1 in bytes 0-63 and 64-127 of chunk 0's row j, query
+        // 3j + 2 in bytes 0-63 of chunk 1's row j (126-bit prefixes); a query past the end
+        // is zero
+        for (uint32_t j = e; j < static_cast<uint32_t>(kN); j += 128) {
+          const uint64_t q0 = static_cast<uint64_t>(p) * kQueries + 3 * j;
+          const uint4 zero = make_uint4(0, 0, 0, 0);
+          auto src = [&](uint64_t q) {
+            return q < n_queries ? *reinterpret_cast<const uint4*>(prm.queries + q * 32) : zero;
+          };
+          expand_row_fp4<0, true>(src(q0), bchunk0, static_cast<int>(j));
+          expand_row_fp4<4, true>(src(q0 + 1), bchunk0, static_cast<int>(j));
+          expand_row_fp4<0, true>(src(q0 + 2), bchunk1, static_cast<int>(j));
+          // zero words of a query past the end expand to +-1 values: clear those units
+          const int sw = static_cast<int>(j) & 7;
+#pragma unroll
+          for (int f = 0; f < 3; ++f) {
+            if (q0 + f < n_queries) continue;
+            uint8_t* const rowp = (f == 2 ? bchunk1 : bchunk0) + j * 128;
+            const int u0 = f == 1 ? 4 : 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              *reinterpret_cast<uint4*>(rowp + (((u0 + u) ^ sw) << 4)) = zero;
+          }
+        }
+      } else
       for (uint32_t j = e; j < static_cast<uint32_t>(kN); j += 128) {
         const uint64_t q0 = static_cast<uint64_t>(p) * kQueries + 2 * j;
         const uint4 zero = make_uint4(0, 0, 0, 0);
@@ -1046,7 +1134,9 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1)
           }
           tc_fence_after();
           const uint32_t a0 = smem_u32(a_smem + static_cast<size_t>(as) * kChunkBytes);
-          if constexpr (kFp4)
+          if constexpr (kTriples)
+            mma_triple4_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc, tmem_base);
+          else if constexpr (kFp4)
             mma_pair4_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc,
                             tmem_base + kSfOneCol, tmem_base + kSfBigCol);
           else
@@ -1119,6 +1209,89 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1)
     using C8 = std::integral_constant<int, 8>;
     using C16 = std::integral_constant<int, 16>;
     using C32 = std::integral_constant<int, 32>;
+    // Triples: bit 7 / bit 15 of a column's bits mark a candidate for its first / second
+    // query; its third query is a candidate when the bits (a float in [2^23, 2^24), so
+    // ordered as integers) reach 2^23 + 65536 (126 - t).
+    const uint32_t tc_bits =
+        __float_as_uint(8388608.0f + 65536.0f * (126.0f - static_cast<float>(prm.threshold)));
+    auto tri_any = [&](const uint32_t* raw, auto cols) -> bool {
+      constexpr int kCols = decltype(cols)::value;
+      uint32_t any = 0, mx = 0;
+#pragma unroll
+      for (int i = 0; i < kCols; ++i) {
+        any |= raw[i];
+        mx = max(mx, raw[i]);
+      }
+      return (any & 0x8080u) || mx >= tc_bits;
+    };
+    // the rare path: one lane's candidate masks of one chunk, bit i for triple i of the chunk
+    auto tri_masks = [&](const uint32_t* raw, auto cols, uint32_t (&m)[3]) {
+      constexpr int kCols = decltype(cols)::value;
+#pragma unroll
+      for (int i = 0; i < kCols; ++i) {
+        m[0] |= ((raw[i] >> 7) & 1u) << i;
+        m[1] |= ((raw[i] >> 15) & 1u) << i;
+        m[2] |= (raw[i] >= tc_bits ? 1u : 0u) << i;
+      }
+    };
+    // One tile of the triple form: the group's 120 columns in two rounds (32 + 32, then
+    // 32 + 16 + 8), decoded, the columns reset, the stage handed back, then any candidates
+    // re-checked (queries q_first + 3 i + f for triple i, field f).
+    auto triple_tile = [&](uint32_t cols, uint64_t row, bool row_ok, uint64_t q_first,
+                           uint32_t n_q, uint32_t (&raw0)[32], uint32_t (&raw1)[32],
+                           float (&unused)[32], uint32_t ac) {
+      // chunk c (triples kChunkTriple[c] ..) of the group: its candidates re-checked exactly
+      // (all lanes take part)
+      auto report = [&](const uint32_t (&m)[3], uint32_t first_triple) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+          if (__any_sync(0xffffffffu, m[f] != 0))
+            emit_candidates_call(m[f], row, q_first + 3 * first_triple + f, n_q, &prm, lane, 3);
+      };
+      tmem_ld32_nowait(cols, raw0);
+      tmem_ld32_nowait(cols + 32, raw1);
+      tmem_ld_wait();
+      tmem_take(raw0, unused);
+      tmem_take(raw1, unused);
+      const bool mine1 = row_ok && (tri_any(raw0, C32{}) || tri_any(raw1, C32{}));
+      if (__any_sync(0xffffffffu, mine1)) {
+        // rare: report round 1's candidates now, while its columns are in registers (the
+        // stage is handed back a little later)
+        uint32_t m0[3] = {}, m1[3] = {};
+        if (mine1) {
+          tri_masks(raw0, C32{}, m0);
+          tri_masks(raw1, C32{}, m1);
+        }
+        report(m0, 0);
+        report(m1, 32);
+      }
+      uint32_t raw2[16], raw3[8];
+      tmem_ld32_nowait(cols + 64, raw0);
+      tmem_ld16_nowait(cols + 96, raw2);
+      tmem_ld8_nowait(cols + 112, raw3);
+      tmem_ld_wait();
+      tmem_take(raw0, unused);
+      tmem_take16(raw2);
+      tmem_take8(raw3);
+      const bool mine2 =
+          row_ok && (tri_any(raw0, C32{}) || tri_any(raw2, C16{}) || tri_any(raw3, C8{}));
+      uint32_t m2[3] = {}, m3[3] = {}, m4[3] = {};
+      if (mine2) {
+        tri_masks(raw0, C32{}, m2);
+        tri_masks(raw2, C16{}, m3);
+        tri_masks(raw3, C8{}, m4);
+      }
+      fill_group(cols);
+      tmem_st_wait();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+      if (__any_sync(0xffffffffu, mine2)) {
+        report(m2, 64);
+        report(m3, 96);
+        report(m4, 112);
+      }
+    };
     uint32_t ga = 0;
     bool ok = true;
     for (uint32_t p = 0; p < n_passes && ok; ++p) {
@@ -1134,9 +1307,14 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1)
         const uint64_t row = tile * kTileRows + quarter * 32 + lane;
         const bool row_ok = row < prm.n_rows;
         const uint32_t cols = tmem_base + lane_addr + ac * kPairStageCols + kGroupCols * group;
-        const uint64_t q_first = pass_q + 2 * static_cast<uint64_t>(kGroupCols * group);
+        const uint64_t q_first =
+            pass_q + (kTriples ? 3 : 2) * static_cast<uint64_t>(kGroupCols * group);
         uint32_t raw0[32], raw1[32];
         float unused[32];
+        if constexpr (kTriples) {
+          triple_tile(cols, row, row_ok, q_first, n_queries, raw0, raw1, unused, ac);
+          continue;
+        }
         // round 1: pairs 0..63 of the group
         tmem_ld32_nowait(cols, raw0);
         tmem_ld32_nowait(cols + 32, raw1);
@@ -1191,7 +1369,7 @@ __global__ void __launch_bounds__(pair_threads(kFp4), 1)
         // at pair `pair` of the group
         auto report = [&](uint64_t m, uint32_t pair) {
           if (__any_sync(0xffffffffu, m != 0))
-            emit_candidates_call(m, row, q_first + 2 * pair, n_queries, &prm, lane);
+            emit_candidates_call(m, row, q_first + 2 * pair, n_queries, &prm, lane, 1);
         };
         if (need1) {
           report(m0, 0);
@@ -1545,8 +1723,9 @@ cudaError_t scan_tc_init() {
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 4>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 6>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 8>),
-                        reinterpret_cast<const void*>(tc::scan_pair_kernel<false>),
-                        reinterpret_cast<const void*>(tc::scan_pair_kernel<true>),
+                        reinterpret_cast<const void*>(tc::scan_pair_kernel<tc::kFormFp8Pairs>),
+                        reinterpret_cast<const void*>(tc::scan_pair_kernel<tc::kFormFp4Pairs>),
+                        reinterpret_cast<const void*>(tc::scan_pair_kernel<tc::kFormFp4Triples>),
                         reinterpret_cast<const void*>(tc::scan_rows_kernel<4>),
                         reinterpret_cast<const void*>(tc::scan_rows_kernel<6>),
                         reinterpret_cast<const void*>(tc::scan_rows_kernel<8>)}) {
@@ -1611,12 +1790,22 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   if (p.pair_n && (!half_k || (p.pair_n != static_cast<uint32_t>(tc::kPairN) &&
                                 p.pair_n != kPairFp4N)))
     return cudaErrorInvalidValue;  // pairs need the 128-bit bound (t <= 36)
-  // at t <= 36, passes of 512 queries, two per accumulator column (scan_pair_kernel), when
-  // asked for or by default past one pass of 256; pair_n = kPairFp4N: the FP4 form (passes of
-  // 480 queries)
+  // at t <= 36 and past one pass of 256 (or when asked for): several queries per accumulator
+  // column (scan_pair_kernel), FP8 pairs in passes of 512 or, with pair_n = kPairFp4N, FP4
+  // pairs (480) or triples (per_column = 3, 720)
   if (half_k && !p.n_tile && (p.pair_n || p.n_queries > static_cast<uint32_t>(tc::kMaxN))) {
-    const bool fp4 = p.pair_n == kPairFp4N;
-    prm.n_tile = 2u * static_cast<uint32_t>(tc::pair_n_of(fp4));
+    // Without a form asked for: a pass of 720 queries in FP4 triples costs ~1.15 x a pass of
+    // 512 in FP8 pairs (0.415 vs 0.36 ms on 10M rows), so take the form with fewer pass-costs
+    uint64_t p3 = (p.n_queries + tc::form_queries(tc::kFormFp4Triples) - 1) /
+                  tc::form_queries(tc::kFormFp4Triples);
+    uint64_t p2 = (p.n_queries + tc::form_queries(tc::kFormFp8Pairs) - 1) /
+                  tc::form_queries(tc::kFormFp8Pairs);
+    const bool auto_triples = !p.pair_n && 83 * p3 < 72 * p2;
+    const bool fp4 = p.pair_n == kPairFp4N || auto_triples;
+    const int form = !fp4 ? tc::kFormFp8Pairs
+                     : (auto_triples || p.per_column == 3) ? tc::kFormFp4Triples
+                                                           : tc::kFormFp4Pairs;
+    prm.n_tile = static_cast<uint32_t>(tc::form_queries(form));
     prm.a_stages = tc::kPairAStages;
     // layout: [fixed Smem][A: 4 x 16 KB][B: 2 x 256 pairs x 128 B][packed ring], 1024-aligned
     prm.b_offset = static_cast<uint32_t>(tc::kFixedBytes +
@@ -1627,10 +1816,13 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
     prm.pack_stages = static_cast<uint32_t>(stages);
     prm.pack_offset = static_cast<uint32_t>(b_end);
     const size_t smem = b_end + stages * tc::kPackBytes + 1024;
-    if (fp4)
-      tc::scan_pair_kernel<true><<<static_cast<unsigned>(grid), tc::pair_threads(true), smem, s>>>(prm);
+    const unsigned g = static_cast<unsigned>(grid);
+    if (form == tc::kFormFp4Triples)
+      tc::scan_pair_kernel<tc::kFormFp4Triples><<<g, tc::pair_threads(true), smem, s>>>(prm);
+    else if (form == tc::kFormFp4Pairs)
+      tc::scan_pair_kernel<tc::kFormFp4Pairs><<<g, tc::pair_threads(true), smem, s>>>(prm);
     else
-      tc::scan_pair_kernel<false><<<static_cast<unsigned>(grid), tc::pair_threads(false), smem, s>>>(prm);
+      tc::scan_pair_kernel<tc::kFormFp8Pairs><<<g, tc::pair_threads(false), smem, s>>>(prm);
     return cudaGetLastError();
   }
   // passes of <= 128 queries: two MMA issuers and A in tensor memory (the pass is bound by

@@ -203,6 +203,8 @@ struct ScanLaunch {
                            // two per accumulator column (FP8 operands); kPairFp4N = passes of
                            // that many pairs with block-scaled FP4 operands; with n_tile and pair_n
                            // both 0 the launcher takes pairs past 256 queries
+  uint32_t per_column;     // with pair_n = kPairFp4N: 3 = three queries per accumulator
+                           // column (passes of 3 kPairFp4N queries), else two
 };
 
 // hash.cu
