@@ -110,9 +110,10 @@ def test_server_config_default_and_argument_checks(yp):
 
 def test_screen_chunk_plan(yp):
     """ypdq_screen_plan (host-only): the chunks of ypdq_screen_host cover [0, n) in order,
-    are whole multiples of 32 images (64 at t <= 36) except the last and number at most 32. They grow
-    geometrically when hashing and scanning an image takes longer than copying it, and
-    slowly (by the hash kernel's fixed cost per chunk) when it does not."""
+    are whole multiples of 32 images (90 at t <= 36: one pass of 720 queries in triples)
+    except the last and number at most 32. They grow geometrically when hashing and scanning
+    an image takes longer than copying it, and slowly (by the hash kernel's fixed cost per
+    chunk) when it does not; then a remainder smaller than a pass is the last chunk."""
     lib = yp._lib.load()
     bounds = (ctypes.c_int64 * 33)()
     k = ctypes.c_int()
@@ -128,20 +129,22 @@ def test_screen_chunk_plan(yp):
             b = plan(n, kind, rows, t)
             sizes = np.diff(b)
             assert b[0] == 0 and b[-1] == n and (sizes > 0).all() and len(sizes) <= 32
-            assert (sizes[:-1] % 32 == 0).all()
-    # 1,024 f32 images against 10M rows at t = 31: ~6 us of hash and scan per image against
-    # ~5 us of copy, so the chunks grow from 64 images (one pass of 512 queries in pairs) to
-    # a few hundred, in whole passes
+            assert (sizes[:-1] % (90 if t <= 36 else 32) == 0).all()
+    # 1,024 f32 images against 10M rows at t = 31: ~5 us of hash and scan per image against
+    # ~5 us of copy, so whole 90-image passes, growing slowly, and the remainder last
     sizes = np.diff(plan(1024, 0, 10_000_000, 31))
-    assert sizes[0] == 64 and (sizes % 64 == 0).all() and sizes.max() >= 192
-    assert 5 <= len(sizes) <= 12
+    assert sizes[0] == 90 and (sizes[:-1] % 90 == 0).all() and sizes[-1] <= 180
+    assert 6 <= len(sizes) <= 16
+    # at 100M rows the scan is ten times longer than the copy: chunks grow geometrically
+    big = np.diff(plan(1024, 0, 100_000_000, 31))
+    assert big[0] == 90 and (big[:-1] % 90 == 0).all() and big.max() >= 180 and len(big) < 10
     # above t = 36 passes hold 256 queries: chunks of whole 32-image passes
     sizes48 = np.diff(plan(1024, 0, 10_000_000, 48))
     assert sizes48[0] == 32 and (sizes48 % 32 == 0).all()
     # a small database: copying dominates and a chunk's compute is mostly the hash kernel's
     # one round over its images, so chunks grow only by that fixed cost
     small = np.diff(plan(1024, 0, 60_000, 31))
-    assert (np.diff(small[:-1]) >= 0).all() and len(small) > len(sizes) and small.max() <= 304
+    assert (np.diff(small[:-1]) >= 0).all() and len(small) >= len(sizes) and small.max() <= 304
     # the Jarosz filter (dct_precision 0x200) adds ~1 us of compute per image: where the scan
     # dominates, its chunks grow at least as fast
     assert len(plan(1024, 0, 10_000_000, 31, dct=0x200)) <= len(plan(1024, 0, 10_000_000, 31))

@@ -114,10 +114,12 @@ int64_t jarosz_chunk(int64_t n) { return n < 2048 ? (n > 0 ? n : 1) : 2048; }
 // S_{c+1} u <= S_1 u + S_c v + c h, i.e. S_{c+1} <= S_1 + (v / u) S_c + c (h / u): chunks
 // grow geometrically by the compute/copy ratio, and only the first chunk's copy is exposed.
 // `ratio` is v / u and `chunk_images` h / u. Chunks are whole multiples of `granule` images
-// (whole scan passes: 32 images = 256 queries, or 64 = one pass of 512 queries taken in
-// pairs); the first is one granule unless more than `max_chunks` chunks would be needed.
+// (whole scan passes: 32 images = 256 queries, or 90 = one pass of 720 queries taken in
+// triples); the first is one granule unless more than `max_chunks` chunks would be needed.
 // When copying is the longer stage (v / u <= 1) chunks still grow by h / u each, since a
-// chunk's fixed cost is then all its compute.
+// chunk's fixed cost is then all its compute, and a remainder smaller than a granule stays
+// the last chunk: its compute after the last copy is exposed, so it should be small. When
+// computing is the longer stage the remainder joins the last chunk instead.
 int plan_screen_chunks(int64_t n, double ratio, double chunk_images, int max_chunks,
                        int64_t granule, int64_t* bounds) {
   const double r = std::min(2.0, std::max(1.0, ratio));
@@ -132,7 +134,7 @@ int plan_screen_chunks(int64_t n, double ratio, double chunk_images, int max_chu
       const double limit = static_cast<double>(first) + r * static_cast<double>(end) + nch * h;
       int64_t next =
           std::max<int64_t>(end + granule, static_cast<int64_t>(limit) / granule * granule);
-      if (next + granule > n) next = n;  // no remainder smaller than a granule
+      if (next >= n || (next + granule > n && ratio > 1.0)) next = n;
       end = next;
       bounds[++nch] = end;
     }
@@ -146,10 +148,10 @@ struct ChunkCost {
   double fixed_us, per_image_us;
 };
 ChunkCost screen_chunk_cost(int input_kind, bool jarosz, uint64_t n_rows, uint32_t threshold) {
-  // the tensor-core scan: 14.0 T (row, query) pairs/s in passes of 512 queries taken in
-  // pairs (the 128-bit prefix bound), 9.5 T with the 192-bit bound, 8.3 T with all 256
-  // bits; 8 queries per image
-  const double pairs_per_us = threshold <= 36 ? 14.0e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
+  // the tensor-core scan: 16.5 T (row, query) pairs/s in passes of 720 queries taken in
+  // triples (FP4, the 126-bit prefix bound), 9.5 T with the 192-bit bound, 8.3 T with all
+  // 256 bits; 8 queries per image
+  const double pairs_per_us = threshold <= 36 ? 16.5e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
   const double scan_us = 8.0 * static_cast<double>(n_rows) / pairs_per_us;
   // the Jarosz filter: four passes, each at least one line's sequential replay (512
   // dependent steps, ~5 us) however few images the chunk holds, plus the DCT
@@ -168,8 +170,8 @@ int screen_chunks(int64_t n, int input_kind, int dct_precision, uint64_t n_rows,
   const double copy_us = static_cast<double>(image_bytes_of(input_kind)) / 2.11e5;
   const ChunkCost cost =
       screen_chunk_cost(input_kind, dct_precision == YPDQ_COMPRESS_JAROSZ, n_rows, threshold);
-  // at t <= 36 chunks of 64 images fill whole passes of the pair scan (512 queries)
-  const int64_t granule = threshold <= 36 ? 64 : 32;
+  // at t <= 36 chunks of 90 images fill whole passes of the triple scan (720 queries)
+  const int64_t granule = threshold <= 36 ? 90 : 32;
   return plan_screen_chunks(n, 0.95 * cost.per_image_us / copy_us, 0.95 * cost.fixed_us / copy_us,
                             ypdq_ctx::kMaxChunks, granule, bounds);
 }
