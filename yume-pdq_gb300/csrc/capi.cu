@@ -73,6 +73,20 @@ ypdq_status scratch(ypdq_ctx* ctx, int slot, size_t bytes, void** out) {
   return YPDQ_OK;
 }
 
+// The context's page-locked staging buffer, at least `bytes` long (under ctx->mu).
+ypdq_status host_stage(ypdq_ctx* ctx, size_t bytes, uint8_t** out) {
+  if (ctx->h_stage_bytes < bytes) {
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    ctx->h_stage = nullptr;
+    ctx->h_stage_bytes = 0;
+    const size_t want = bytes < 65536 ? 65536 : bytes;
+    CK(cudaMallocHost(&ctx->h_stage, want), "cudaMallocHost(staging)");
+    ctx->h_stage_bytes = want;
+  }
+  *out = static_cast<uint8_t*>(ctx->h_stage);
+  return YPDQ_OK;
+}
+
 ypdq_status check_ctx(ypdq_ctx* ctx) {
   if (!ctx) return fail(YPDQ_ERR_INVALID, "ctx is NULL");
   CK(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -247,6 +261,7 @@ ypdq_status ypdq_ctx_destroy(ypdq_ctx* ctx) {
   for (int i = 0; i < 8; ++i)
     if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
   if (ctx->jarosz_scratch) cudaFree(ctx->jarosz_scratch);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->jarosz_done) cudaEventDestroy(ctx->jarosz_done);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -592,16 +607,24 @@ ypdq_status ypdq_screen_host(ypdq_ctx* ctx, ypdq_db* db, const void* h_images, i
     CK(launch_scan(sp, YPDQ_SCAN_AUTO, ctx->num_sms, s), "scan launch");
   }
   if (jarosz && n > 0) CK(cudaEventRecord(ctx->jarosz_done, s), "record jarosz scratch");
-  uint64_t total = 0;
-  CK(cudaMemcpyAsync(&total, d_cnt, sizeof(uint64_t), cudaMemcpyDeviceToHost, s), "D2H count");
+  // results come back through the page-locked staging buffer: [count][error word][hits]
+  uint8_t* stage = nullptr;
+  if ((st = host_stage(ctx, 64 + sizeof(ypdq_hit) * capacity, &stage))) return st;
+  CK(cudaMemcpyAsync(stage, d_cnt, sizeof(uint64_t), cudaMemcpyDeviceToHost, s), "D2H count");
+  CK(cudaMemcpyAsync(stage + 8, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H error word");
   CK(cudaStreamSynchronize(s), "screen sync");
+  uint64_t total = 0;
+  memcpy(&total, stage, sizeof(total));
   const uint64_t m = total < capacity ? total : capacity;
   CK(launch_sort_hits(static_cast<ypdq_hit*>(d_hits), m, s), "sort launch");
-  if (m > 0) CK(cudaMemcpyAsync(h_hits, d_hits, m * sizeof(ypdq_hit), cudaMemcpyDeviceToHost, s), "D2H hits");
+  if (m > 0) CK(cudaMemcpyAsync(stage + 64, d_hits, m * sizeof(ypdq_hit), cudaMemcpyDeviceToHost, s), "D2H hits");
   if (h_hashes && n > 0) CK(cudaMemcpyAsync(h_hashes, d_hash, 256 * n, cudaMemcpyDeviceToHost, s), "D2H hashes");
   if (h_quality && n > 0) CK(cudaMemcpyAsync(h_quality, d_q, 32 * n, cudaMemcpyDeviceToHost, s), "D2H quality");
   CK(cudaStreamSynchronize(s), "screen sync");
-  if ((st = read_device_errors(ctx))) return st;
+  if (m > 0) memcpy(h_hits, stage + 64, m * sizeof(ypdq_hit));
+  int dev_err = 0;
+  memcpy(&dev_err, stage + 8, sizeof(dev_err));
+  if (dev_err && (st = read_device_errors(ctx))) return st;
   *n_hits = total;
   if (total > capacity) return fail(YPDQ_ERR_OVERFLOW, "%llu hits > capacity %llu",
                                     (unsigned long long)total, (unsigned long long)capacity);

@@ -23,6 +23,10 @@ struct ypdq_ctx {
   std::mutex mu;                  // guards the scratch buffers below
   void* scratch[8] = {};
   size_t scratch_bytes[8] = {};
+  // page-locked host staging of ypdq_screen_host's results (count, error word, hits), so
+  // its device-to-host copies never take the driver's path for pageable memory
+  void* h_stage = nullptr;
+  size_t h_stage_bytes = 0;
   void* jarosz_scratch = nullptr;  // YPDQ_COMPRESS_JAROSZ filter planes
   size_t jarosz_bytes = 0;
   cudaEvent_t jarosz_done = nullptr;  // recorded after the last work that used it

@@ -279,10 +279,7 @@ cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t
   if (algo == YPDQ_SCAN_TC) return launch_scan_tc(p, num_sms, s);
   if (algo == YPDQ_SCAN_TC_FP4) {
     ScanLaunch q = p;
-    if (p.threshold <= 36) {
-      q.pair_n = kPairFp4N;  // FP4 operands, three queries per accumulator column
-      q.per_column = 3;
-    }
+    if (p.threshold <= 36) q.pair_n = kPairFp4N;  // FP4, three queries per column
     return launch_scan_tc(q, num_sms, s);
   }
   // a device-side query count needs the whole query set in one launch

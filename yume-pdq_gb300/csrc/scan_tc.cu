@@ -688,29 +688,24 @@ __global__ void __launch_bounds__(threads_of(kDual), 1) scan_tc_kernel(const Par
 constexpr int kPairN = 256;                 // pairs per pass (MMA N), 512 queries
 constexpr int kPairAStages = 4;             // A tiles in shared memory (16 KiB each)
 
-// The FP4 form (kFp4): block-scaled e2m1 operands, K = 64 per MMA. Scale factors live in
-// tensor memory beside the accumulators, so a stage holds 240 pairs (480 queries per pass):
-// stage s at columns 256 s .. 256 s + 239, scale factor 2^0 in columns 496-503 and 2^9 in
-// 504-511 (every byte of each region the same E8M0 value).
+// The FP4 forms use block-scaled e2m1 operands, K = 64 per MMA, whose scale factors live in
+// tensor memory beside the accumulators: a stage holds 240 columns (stage s at columns
+// 256 s .. 256 s + 239).
 constexpr int kPair4N = static_cast<int>(kPairFp4N);
 constexpr uint32_t kPairStageCols = 256;
-constexpr uint32_t kSfOneCol = 496, kSfBigCol = 504;  // 8 columns each
-constexpr uint32_t kE8m0One = 0x7F7F7F7Fu;  // 2^(127 - 127) in each byte
-constexpr uint32_t kE8m0Big = 0x88888888u;  // 2^(136 - 127) = 512 in each byte
-__host__ __device__ constexpr int pair_n_of(bool fp4) { return fp4 ? kPair4N : kPairN; }
 
-// The triple form (kForm 2): three queries per f32 column, FP4 operands as above. The bound
-// is the first 126 bits (the queries' bits 126 and 127 expand to 0.0): per query the dot
-// product d is even and in [-126, 126], so e = d / 2 fits 7 bits. With B scale factors 2^-1,
-// 2^7 and 2^15 for queries 3j, 3j + 1 and 3j + 2 (A's scale 1), column j holds
+// The triple form (kForm 2): three queries per f32 column, FP4 operands. The bound is the
+// first 126 bits (the queries' bits 126 and 127 expand to 0.0): per query the dot product d
+// is even and in [-126, 126], so e = d / 2 fits 7 bits. With B scale factors 2^-1, 2^7 and
+// 2^15 for queries 3j, 3j + 1 and 3j + 2 (A's scale 1), column j holds
 // v = e_a + 256 e_b + 65536 e_c: every 32-element block adds an integer (its 32 products of
 // +-1 sum to an even number), so with the stage starting at the decoding constant every
 // value is an integer in [2^23, 2^24) and f32 accumulation is exact. Scale regions of 8
 // columns in the two gaps the stages leave (columns 240-255 and 496-511): 2^0 at 240 (A),
 // 2^-1 at 248, 2^7 at 496, 2^15 at 504. A block-scaled MMA with N = 240 reads more than 4
 // columns of B scale factors (4-column regions made the last read run past column 511, an
-// illegal access) and at most 8 (the pair form's 8-column regions at 496 and 504 give exact
-// results). Passes of 720 queries.
+// illegal access) and at most 8 (8-column regions at 496 and 504 of an earlier pair form
+// gave exact results). Passes of 720 queries.
 __host__ __device__ constexpr uint32_t sf_tri_col(int i) {
   return i == 0 ? 240u : i == 1 ? 248u : i == 2 ? 496u : 504u;
 }
@@ -718,13 +713,14 @@ __host__ __device__ constexpr uint32_t sf_tri_val(int i) {
   return i == 0 ? 0x7F7F7F7Fu : i == 1 ? 0x7E7E7E7Eu : i == 2 ? 0x86868686u : 0x8E8E8E8Eu;
 }
 // forms of scan_pair_kernel
-constexpr int kFormFp8Pairs = 0, kFormFp4Pairs = 1, kFormFp4Triples = 2;
+constexpr int kFormFp8Pairs = 0, kFormFp4Triples = 2;
 __host__ __device__ constexpr int form_columns(int form) { return form == 0 ? kPairN : kPair4N; }
 __host__ __device__ constexpr int form_queries(int form) {
   return (form == 2 ? 3 : 2) * form_columns(form);
 }
+
 // Both forms read their accumulator stage with 8 epilogue warps, two per TMEM lane quarter,
-// each warp half the stage's columns (128 for FP8, 120 for FP4) in two rounds.
+// each warp half the stage's columns (128 for FP8 pairs, 120 for FP4 triples) in two rounds.
 __host__ __device__ constexpr int pair_epilogue_warps(bool) { return 8; }
 __host__ __device__ constexpr int pair_threads(bool fp4) {
   return (pair_epilogue_warps(fp4) + 6) * 32;
@@ -867,18 +863,6 @@ __device__ __forceinline__ void mma_triple4_issue(uint32_t d, uint32_t a0, uint3
              sf + sf_tri_col(3), 1u);
 }
 
-// FP4: two MMAs of K = 64 per query of the pair; query 2j + 1's B scale is 2^9.
-__device__ __forceinline__ void mma_pair4_issue(uint32_t d, uint32_t a0, uint32_t b0,
-                                                uint32_t b1, uint32_t idesc, uint32_t sf_one,
-                                                uint32_t sf_big) {
-#pragma unroll
-  for (int ks = 0; ks < 2; ++ks)
-    mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 32 * ks), idesc, sf_one, sf_one, 1u);
-#pragma unroll
-  for (int ks = 0; ks < 2; ++ks)
-    mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b1 + 32 * ks), idesc, sf_one, sf_big, 1u);
-}
-
 template <int kForm>
 __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
     scan_pair_kernel(const __grid_constant__ Params prm) {
@@ -967,9 +951,6 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
     if constexpr (kTriples) {
       tmem_st8_fill(tmem_base + lanes + sf_tri_col(2 * g), sf_tri_val(2 * g));
       tmem_st8_fill(tmem_base + lanes + sf_tri_col(2 * g + 1), sf_tri_val(2 * g + 1));
-    } else if constexpr (kFp4) {
-      tmem_st8_fill(tmem_base + lanes + (warp < 4 ? kSfOneCol : kSfBigCol),
-                    warp < 4 ? kE8m0One : kE8m0Big);
     }
     tmem_st_wait();
   }
@@ -1053,10 +1034,7 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
         // a query past the end gives a zero B row: its products are all 0
         if (q0 < n_queries) {
           const uint4* src = reinterpret_cast<const uint4*>(prm.queries + q0 * 32);
-          if constexpr (kFp4)
-            expand_row_fp4(src[0], bchunk0, static_cast<int>(j));
-          else
-            expand_row<4, 0x3C3C3C3Cu>(src[0], src[1], bchunk0, nullptr, static_cast<int>(j));
+          expand_row<4, 0x3C3C3C3Cu>(src[0], src[1], bchunk0, nullptr, static_cast<int>(j));
         } else {
 #pragma unroll
           for (int u = 0; u < 8; ++u)
@@ -1064,10 +1042,7 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
         }
         if (q0 + 1 < n_queries) {
           const uint4* src = reinterpret_cast<const uint4*>(prm.queries + (q0 + 1) * 32);
-          if constexpr (kFp4)
-            expand_row_fp4(src[0], bchunk1, static_cast<int>(j));
-          else
-            expand_row<4, 0x60606060u>(src[0], src[1], bchunk1, nullptr, static_cast<int>(j));
+          expand_row<4, 0x60606060u>(src[0], src[1], bchunk1, nullptr, static_cast<int>(j));
         } else {
 #pragma unroll
           for (int u = 0; u < 8; ++u)
@@ -1136,9 +1111,6 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
           const uint32_t a0 = smem_u32(a_smem + static_cast<size_t>(as) * kChunkBytes);
           if constexpr (kTriples)
             mma_triple4_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc, tmem_base);
-          else if constexpr (kFp4)
-            mma_pair4_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc,
-                            tmem_base + kSfOneCol, tmem_base + kSfBigCol);
           else
             mma_pair_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc);
           mma_commit(&sm.a_empty[as]);
@@ -1323,40 +1295,22 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
         tmem_take(raw1, unused);
         const bool mine1 = row_ok && ((chunk_any(raw0, C32{}) | chunk_any(raw1, C32{})) & 0x40200u);
         const bool need1 = __any_sync(0xffffffffu, mine1);
-        uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0;
+        uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
         if (need1 && mine1) {
           m0 = chunk_mask(raw0, C32{});
           m1 = chunk_mask(raw1, C32{});
         }
         // round 2: pairs 64.. of the group
         bool mine2;
-        if constexpr (kFp4) {
-          uint32_t raw2[16], raw3[8];
-          tmem_ld32_nowait(cols + 64, raw0);
-          tmem_ld16_nowait(cols + 96, raw2);
-          tmem_ld8_nowait(cols + 112, raw3);
-          tmem_ld_wait();
-          tmem_take(raw0, unused);
-          tmem_take16(raw2);
-          tmem_take8(raw3);
-          mine2 = row_ok && ((chunk_any(raw0, C32{}) | chunk_any(raw2, C16{}) |
-                              chunk_any(raw3, C8{})) & 0x40200u);
-          if (mine2) {
-            m2 = chunk_mask(raw0, C32{});
-            m3 = chunk_mask(raw2, C16{});
-            m4 = chunk_mask(raw3, C8{});
-          }
-        } else {
-          tmem_ld32_nowait(cols + 64, raw0);
-          tmem_ld32_nowait(cols + 96, raw1);
-          tmem_ld_wait();
-          tmem_take(raw0, unused);
-          tmem_take(raw1, unused);
-          mine2 = row_ok && ((chunk_any(raw0, C32{}) | chunk_any(raw1, C32{})) & 0x40200u);
-          if (mine2) {
-            m2 = chunk_mask(raw0, C32{});
-            m3 = chunk_mask(raw1, C32{});
-          }
+        tmem_ld32_nowait(cols + 64, raw0);
+        tmem_ld32_nowait(cols + 96, raw1);
+        tmem_ld_wait();
+        tmem_take(raw0, unused);
+        tmem_take(raw1, unused);
+        mine2 = row_ok && ((chunk_any(raw0, C32{}) | chunk_any(raw1, C32{})) & 0x40200u);
+        if (mine2) {
+          m2 = chunk_mask(raw0, C32{});
+          m3 = chunk_mask(raw1, C32{});
         }
         // decoded: reset the warp's columns (one wait for all stores: a store's source
         // registers stay reserved until then) and hand the stage back before any hit reporting
@@ -1378,7 +1332,7 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
         if (__any_sync(0xffffffffu, mine2)) {
           report(m2, 64);
           report(m3, 96);
-          if constexpr (kFp4) report(m4, 112);
+
         }
       }
     }
@@ -1724,7 +1678,6 @@ cudaError_t scan_tc_init() {
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 6>),
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 8>),
                         reinterpret_cast<const void*>(tc::scan_pair_kernel<tc::kFormFp8Pairs>),
-                        reinterpret_cast<const void*>(tc::scan_pair_kernel<tc::kFormFp4Pairs>),
                         reinterpret_cast<const void*>(tc::scan_pair_kernel<tc::kFormFp4Triples>),
                         reinterpret_cast<const void*>(tc::scan_rows_kernel<4>),
                         reinterpret_cast<const void*>(tc::scan_rows_kernel<6>),
@@ -1792,7 +1745,7 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
     return cudaErrorInvalidValue;  // pairs need the 128-bit bound (t <= 36)
   // at t <= 36 and past one pass of 256 (or when asked for): several queries per accumulator
   // column (scan_pair_kernel), FP8 pairs in passes of 512 or, with pair_n = kPairFp4N, FP4
-  // pairs (480) or triples (per_column = 3, 720)
+  // triples in passes of 720
   if (half_k && !p.n_tile && (p.pair_n || p.n_queries > static_cast<uint32_t>(tc::kMaxN))) {
     // Without a form asked for: a pass of 720 queries in FP4 triples costs ~1.15 x a pass of
     // 512 in FP8 pairs (0.415 vs 0.36 ms on 10M rows), so take the form with fewer pass-costs
@@ -1801,10 +1754,8 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
     uint64_t p2 = (p.n_queries + tc::form_queries(tc::kFormFp8Pairs) - 1) /
                   tc::form_queries(tc::kFormFp8Pairs);
     const bool auto_triples = !p.pair_n && 83 * p3 < 72 * p2;
-    const bool fp4 = p.pair_n == kPairFp4N || auto_triples;
-    const int form = !fp4 ? tc::kFormFp8Pairs
-                     : (auto_triples || p.per_column == 3) ? tc::kFormFp4Triples
-                                                           : tc::kFormFp4Pairs;
+    const int form = p.pair_n == kPairFp4N || auto_triples ? tc::kFormFp4Triples
+                                                           : tc::kFormFp8Pairs;
     prm.n_tile = static_cast<uint32_t>(tc::form_queries(form));
     prm.a_stages = tc::kPairAStages;
     // layout: [fixed Smem][A: 4 x 16 KB][B: 2 x 256 pairs x 128 B][packed ring], 1024-aligned
@@ -1819,8 +1770,6 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
     const unsigned g = static_cast<unsigned>(grid);
     if (form == tc::kFormFp4Triples)
       tc::scan_pair_kernel<tc::kFormFp4Triples><<<g, tc::pair_threads(true), smem, s>>>(prm);
-    else if (form == tc::kFormFp4Pairs)
-      tc::scan_pair_kernel<tc::kFormFp4Pairs><<<g, tc::pair_threads(true), smem, s>>>(prm);
     else
       tc::scan_pair_kernel<tc::kFormFp8Pairs><<<g, tc::pair_threads(false), smem, s>>>(prm);
     return cudaGetLastError();

@@ -67,7 +67,6 @@ struct Bucket {
   uint32_t pair_n = 0;   // or query pairs per pass, two per column (t <= 36)
   float ms = 0.0f;
   uint64_t steps = 0;
-  uint32_t per_column = 0;  // 3: with pair_n = kPairFp4N, three queries per column
 };
 
 struct Slot {
@@ -155,7 +154,6 @@ ypdq_status capture_bucket(ypdq_server* S, Slot& sl, const Bucket& b, cudaGraphE
   sp.nq_dev = &sl.d_hdr->n_queries;
   sp.n_tile = b.algo == YPDQ_SCAN_TC ? b.n_tile : 0;
   sp.pair_n = b.algo == YPDQ_SCAN_TC ? b.pair_n : 0;
-  sp.per_column = b.algo == YPDQ_SCAN_TC ? b.per_column : 0;
   sp.threshold = S->cfg.threshold;
   sp.hits = sl.d_hits;
   sp.capacity = S->cfg.step_hit_capacity;
@@ -473,7 +471,7 @@ ypdq_status autotune(ypdq_server* S) {
     // (FP8 operands) and of 3 kPairFp4N in triples (block-scaled FP4 operands)
     if (S->cfg.threshold <= 36 && nq > 128) {
       cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, 256, 0.0f, 0});
-      cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, kPairFp4N, 0.0f, 0, 3});
+      cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, kPairFp4N, 0.0f, 0});
     }
     float best = 0.0f;
     for (Bucket& c : cand) {
@@ -484,7 +482,6 @@ ypdq_status autotune(ypdq_server* S) {
         b.algo = c.algo;
         b.n_tile = c.n_tile;
         b.pair_n = c.pair_n;
-        b.per_column = c.per_column;
         b.ms = c.ms;
       }
     }
@@ -690,7 +687,7 @@ ypdq_status ypdq_server_get_stats(ypdq_server* S, ypdq_server_stats* o, int rese
     // tensor-core kernel: 0 one query per column (n_tile), 1 pairs, 2 queries as A, 3 FP4
     // triples
     o->bucket_kernel[i] = !tc ? 0 : b.pair_n == kPairFp4N ? 3 : b.pair_n ? 1 : b.n_tile ? 0 : 2;
-    o->bucket_n_tile[i] = !tc ? 0 : b.pair_n ? (b.per_column == 3 ? 3 : 2) * b.pair_n
+    o->bucket_n_tile[i] = !tc ? 0 : b.pair_n ? (b.pair_n == kPairFp4N ? 3 : 2) * b.pair_n
                                              : b.n_tile ? b.n_tile : 128;
     o->bucket_ms[i] = S->buckets[i].ms;
     o->bucket_steps[i] = S->buckets[i].steps;

@@ -11,7 +11,7 @@ namespace ypdq {
 // Device-side error bits, OR-ed into the context's error word by a kernel that gives up.
 constexpr int kDevErrTimeout = 1;
 
-// Pairs per pass of the FP4 pair scan (pair_n of its launches): 2 queries per pair.
+// Accumulator columns per pass of the FP4 scan (pair_n of its launches): three queries each.
 constexpr uint32_t kPairFp4N = 240;
 
 // Longest time a device-side wait spins before the kernel reports a timeout and returns.
@@ -201,10 +201,9 @@ struct ScanLaunch {
                            // 0 picks min(256, n_queries rounded up to 64)
   uint32_t pair_n;         // tensor-core scan at t <= 36: 256 = passes of 256 query pairs,
                            // two per accumulator column (FP8 operands); kPairFp4N = passes of
-                           // that many pairs with block-scaled FP4 operands; with n_tile and pair_n
-                           // both 0 the launcher takes pairs past 256 queries
-  uint32_t per_column;     // with pair_n = kPairFp4N: 3 = three queries per accumulator
-                           // column (passes of 3 kPairFp4N queries), else two
+                           // that many triples of queries, three per column, with block-scaled
+                           // FP4 operands; with n_tile and pair_n both 0 the launcher picks
+                           // past 256 queries
 };
 
 // hash.cu
