@@ -304,9 +304,9 @@ def serve_run(yp, srv, pool, rate, seconds, rng, hit_cap=4096):
         if now - t0 >= seconds:
             break
         if rate is not None and now < t_next:
-            # wait in the server (a condition variable, GIL released) until the next arrival,
-            # instead of spinning on the server's lock from this thread
-            srv.poll(timeout_us=max(1, int((t_next - now) * 1e6)))
+            # spin: a thread that sleeps until the next arrival can wake late and then submit
+            # the requests it owes at once (a burst the arrival process does not have)
+            srv.poll(timeout_us=0)
             continue
         n = int(min(64, max(1, np.exp(rng.uniform(0.0, np.log(65.0))))))
         s0 = int(rng.integers(0, n_pool - n + 1))
