@@ -258,7 +258,7 @@ def fp4_dense_burst(device=0, n=8192, reps=10):
 def scan_algo_used(algo, nq, threshold):
     """The algorithm ypdq_scan runs for YPDQ_SCAN_AUTO (mirrors auto_scan_algo in scan.cu)."""
     if algo == 0:
-        simt_max = (24 if threshold <= 34 else 16 if threshold <= 36 else
+        simt_max = (13 if threshold <= 34 else 9 if threshold <= 36 else
                     24 if threshold <= 62 else 12)
         return 1 if nq <= simt_max else 3
     return algo
@@ -409,7 +409,8 @@ def large_db(yp, ctx, args, members=1000, trials=40, n_queries=1024):
 def scan_sweep(yp, ctx, d_rows, n, d_hash, args, qs=(1, 8, 64, 256, 1024), reps=6):
     """Scan only against the bench database: query batches of 1, 8, 64, 256 and 1,024 hashes
     (the step's own dihedral hashes, whose near-duplicates are planted in the database) at
-    the bench threshold, through the SIMT scan, the tensor-core scan and YPDQ_SCAN_AUTO:
+    the bench threshold, through the SIMT scan, the tensor-core scans (FP8 and FP4) and
+    YPDQ_SCAN_AUTO:
     launch time (median of reps - 1 after one warm launch), database stream rate and its
     fraction of the measured HBM copy rate. Every launch reads the whole database (larger
     than L2)."""
@@ -422,7 +423,7 @@ def scan_sweep(yp, ctx, d_rows, n, d_hash, args, qs=(1, 8, 64, 256, 1024), reps=
            "peak_source": peak_kind, "points": []}
     for q in qs:
         pt = {"queries": q, "auto_algo": {1: "simt", 3: "tc"}[scan_algo_used(0, q, args.threshold)]}
-        for name, algo in (("simt", 1), ("tc", 3), ("auto", 0)):
+        for name, algo in (("simt", 1), ("tc", 3), ("tc_fp4", 4), ("auto", 0)):
             ms = []
             for rep in range(reps):
                 ctx.record(e0, stream)

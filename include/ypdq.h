@@ -433,7 +433,9 @@ typedef struct {
   uint32_t bucket_kernel[YPDQ_SERVER_MAX_BUCKETS];  /* tensor-core scan form: 0 one query per
                                                        accumulator column, 1 two per column,
                                                        2 queries as the MMA's A operand,
-                                                       3 three per column, FP4 operands */
+                                                       3 three per column, FP4 operands,
+                                                       4 queries as A with three database
+                                                       rows per column, FP4 operands */
 } ypdq_server_stats;
 
 /* Fills cfg with the defaults above (threshold 31, f32 input, FP32 DCT, exact semantics). */

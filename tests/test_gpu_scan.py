@@ -372,42 +372,44 @@ def test_fp4_triple_kernel_matches_oracle(ctx, yp, oracle, n_q):
         assert np.array_equal(as_tuples(got), as_tuples(want)), (t, len(got), len(want))
 
 
-@pytest.mark.parametrize("n_q,algo", [(64, 3), (256, 3), (300, 3), (300, 4)])
-def test_device_wait_timeout_is_reported_and_recovered(ctx, yp, oracle, n_q, algo):
-    """The timeout path of the tensor-core scans (64 queries: queries as A; 256: one pass;
-    300: the pair kernel, FP8 and FP4). Under a 1 ms wait limit a launch whose
-    producer issues nothing (ypdq_debug_stall_scans) stops with its waits run out: the
-    stream sync reports YPDQ_ERR_TIMEOUT, and the next scan on the same context returns the
-    oracle's hits. No trap, no fault, no unbounded wait."""
+@pytest.mark.parametrize("n_q,algo,t", [(64, 3, 40), (64, 3, 31), (256, 3, 31), (300, 3, 31),
+                                         (300, 4, 31)])
+def test_device_wait_timeout_is_reported_and_recovered(ctx, yp, oracle, n_q, algo, t):
+    """The timeout path of the tensor-core scans (64 queries: queries as A, FP8 at t = 40 and
+    three rows per column, FP4, at t = 31; 256: one pass; 300: the pair kernel, FP8 and FP4).
+    Under a 1 ms wait limit a launch whose producer issues nothing (ypdq_debug_stall_scans)
+    stops with its waits run out: the stream sync reports YPDQ_ERR_TIMEOUT, and the next scan
+    on the same context returns the oracle's hits. No trap, no fault, no unbounded wait."""
     lib = ctx.lib
     rows = yp.synth.rows_128(50_000, seed=n_q + 70)
     q = yp.synth.rows_128(n_q, seed=n_q + 71)
-    yp.synth.plant(rows, q, 200, 0, 31, seed=72)
+    yp.synth.plant(rows, q, 200, 0, t, seed=72)
     d_rows, d_q = ctx.to_device(rows), ctx.to_device(q)
     cap = 1 << 14
     d_hits, d_cnt = ctx.alloc(cap * 16), ctx.alloc(8)
     assert lib.ypdq_set_scan_wait_limit(1_000_000) == 0
     try:
         assert lib.ypdq_debug_stall_scans(1) == 0
-        yp.core.scan_device(ctx, d_rows, rows.shape[0], d_q, n_q, 31, d_hits, cap, d_cnt, algo)
+        yp.core.scan_device(ctx, d_rows, rows.shape[0], d_q, n_q, t, d_hits, cap, d_cnt, algo)
         with pytest.raises(yp.YpdqError) as err:
             ctx.sync()
         assert err.value.status == yp._lib.ERR_TIMEOUT
     finally:
         lib.ypdq_debug_stall_scans(0)
         lib.ypdq_set_scan_wait_limit(0)
-    got = yp.scan(ctx, rows, q, 31, algo=algo)
-    assert np.array_equal(as_tuples(got), as_tuples(oracle.find_all(rows, q, 31)))
+    got = yp.scan(ctx, rows, q, t, algo=algo)
+    assert np.array_equal(as_tuples(got), as_tuples(oracle.find_all(rows, q, t)))
     assert lib.ypdq_set_scan_wait_limit(61 * 10 ** 9) == yp._lib.ERR_INVALID
     assert lib.ypdq_debug_stall_scans(-1) == yp._lib.ERR_INVALID
 
 
 @pytest.mark.parametrize("n_q", [1, 2, 31, 33, 64, 100, 127, 128])
 def test_rows_kernel_matches_oracle(ctx, yp, oracle, n_q):
-    """Up to 128 queries the tensor-core scan takes the queries as the MMA's A operand and
-    256 database rows per MMA. Row counts that end mid-tile, rows equal or complementary to
-    a query, several planted rows per 64-row chunk, and thresholds on both sides of each
-    prefix-bound switch (36 / 37, 62 / 63) and at the range's ends."""
+    """Up to 128 queries the tensor-core scan takes the queries as the MMA's A operand: at
+    t <= 36 with three database rows per column (FP4, 720 rows per MMA), above with 256 rows
+    per MMA (FP8). Row counts that end mid-tile, rows equal or complementary to a query,
+    several planted rows per 64-row chunk, and thresholds on both sides of each prefix-bound
+    switch (36 / 37, 62 / 63) and at the range's ends."""
     rows = yp.synth.rows_128(6001, seed=n_q + 500)
     q = yp.synth.rows_128(n_q, seed=n_q + 501)
     yp.synth.plant(rows, q, min(600, 6001), 0, 70, seed=n_q)
@@ -417,3 +419,36 @@ def test_rows_kernel_matches_oracle(ctx, yp, oracle, n_q):
         want = oracle.find_all(rows, q, t)
         got = yp.scan(ctx, rows, q, t, algo=3, capacity=1 << 20)
         assert np.array_equal(as_tuples(got), as_tuples(want)), (t, len(got), len(want))
+
+
+@pytest.mark.parametrize("n_q", [1, 2, 3, 31, 32, 33, 64, 65, 100, 127, 128])
+def test_fp4_rows_kernel_matches_oracle(ctx, yp, oracle, n_q):
+    """YPDQ_SCAN_TC_FP4 (and YPDQ_SCAN_TC) with at most 128 queries at t <= 36: the queries
+    are the MMA's A operand and three database rows share each f32 accumulator column (rows
+    3j, 3j + 1, 3j + 2 of a 720-row tile with B scales 2^-1, 2^7, 2^15), the first 126 bits
+    as the bound. Row counts that end mid-tile and mid-column (6000 + 0, 1, 2 rows; 5761: one
+    row in the last tile), the three rows of one column equal or complementary to queries
+    (every field at its extreme), rows that differ from a query only in the two prefix bits
+    the bound leaves out, a run of hits across the columns of one tile, lane quarters with
+    and without queries, every threshold 0..36 at one size; above 36 the call runs the FP8
+    scan."""
+    n_rows = 5761 if n_q == 64 else 6000 + n_q % 3  # 5761: one row in the last tile
+    rows = yp.synth.rows_128(n_rows, seed=n_q + 1300)
+    q = yp.synth.rows_128(n_q, seed=n_q + 1301)
+    yp.synth.plant(rows, q, 400, 0, 40, seed=n_q + 1302)
+    rows[30], rows[31], rows[32] = q[0], q[n_q - 1], ~q[n_q // 2]   # one column, three fields
+    rows[33], rows[34], rows[35] = ~q[0], ~q[n_q - 1], q[n_q // 2]
+    rows[40, :16], rows[40, 16:] = q[n_q // 2, :16], ~q[n_q // 2, 16:]
+    rows[41, :16], rows[41, 16:] = ~q[n_q - 1, :16], q[n_q - 1, 16:]
+    for i in range(3):                                 # one row per field of a column
+        rows[60 + i] = q[min(i, n_q - 1)]
+        rows[60 + i, 15] ^= np.uint8(0xC0)             # bits 126 and 127 of the prefix
+    rows[1440:1536] = q[np.arange(96) % n_q]           # many hits in one tile
+    rows[n_rows - 1] = q[0]                            # the last, partial tile
+    rows[n_rows - 3] = q[n_q - 1]
+    ts = range(37) if n_q == 33 else (0, 1, 2, 16, 31, 35, 36, 40)
+    for t in ts:
+        want = oracle.find_all(rows, q, t)
+        for algo in (yp._lib.SCAN_TC_FP4, 3):
+            got = yp.scan(ctx, rows, q, t, algo=algo, capacity=1 << 20)
+            assert np.array_equal(as_tuples(got), as_tuples(want)), (t, algo, len(got), len(want))

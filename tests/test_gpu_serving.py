@@ -158,13 +158,14 @@ def test_autotune_table_and_target(ctx, yp, workload):
         st = srv.stats()
         assert [b["images"] for b in st["buckets"]] == [1, 2, 4, 8, 16, 32, 64]
         assert all(b["ms"] > 0 and b["algo"] in ("simt", "tc", "tc pairs", "tc rows",
-                                                 "tc fp4 triples")
+                                                 "tc fp4 triples", "tc fp4 rows")
                    for b in st["buckets"])
         # passes of 512 queries in pairs and of 720 in triples are timed from 17 images
         assert all(b["algo"] not in ("tc pairs", "tc fp4 triples") or b["images"] > 16
                    for b in st["buckets"])
         # queries as the MMA's A operand are timed up to 16 images (128 queries)
-        assert all(b["algo"] != "tc rows" or b["images"] <= 16 for b in st["buckets"])
+        assert all(b["algo"] not in ("tc rows", "tc fp4 rows") or b["images"] <= 16
+                   for b in st["buckets"])
         srv.submit(imgs[:50], tag=0)
         (r,) = srv.drain()
         assert np.array_equal(r.hits, yp.screen_host(ctx, db, imgs[:50], threshold=31))

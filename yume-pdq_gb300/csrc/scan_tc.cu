@@ -699,8 +699,12 @@ constexpr uint32_t kPairStageCols = 256;
 // is even and in [-126, 126], so e = d / 2 fits 7 bits. With B scale factors 2^-1, 2^7 and
 // 2^15 for queries 3j, 3j + 1 and 3j + 2 (A's scale 1), column j holds
 // v = e_a + 256 e_b + 65536 e_c: every 32-element block adds an integer (its 32 products of
-// +-1 sum to an even number), so with the stage starting at the decoding constant every
-// value is an integer in [2^23, 2^24) and f32 accumulation is exact. Scale regions of 8
+// +-1 sum to an even number), so every partial sum is an integer below 2^23 in magnitude and
+// f32 accumulation is exact. The tile's first MMA overwrites the stage; the epilogue adds the
+// decoding constant in registers (v + MAGIC, an integer in [2^23, 2^24), exact), so a stage
+// goes back to the MMA issuer as soon as its loads have landed, with no reset stores to wait
+// for (presetting the stages to MAGIC and writing it back after each read cost ~5 % more at
+// 8,192 queries). Scale regions of 8
 // columns in the two gaps the stages leave (columns 240-255 and 496-511): 2^0 at 240 (A),
 // 2^-1 at 248, 2^7 at 496, 2^15 at 504. A block-scaled MMA with N = 240 reads more than 4
 // columns of B scale factors (4-column regions made the last read run past column 511, an
@@ -846,13 +850,15 @@ __device__ __forceinline__ void mma_pair_issue(uint32_t d, uint32_t a0, uint32_t
 }
 
 // FP4 triples: two MMAs of K = 64 per query; queries 3j and 3j + 1 share B chunk 0 (bytes
-// 0-63 and 64-127 of a row), query 3j + 2 is B chunk 1.
+// 0-63 and 64-127 of a row), query 3j + 2 is B chunk 1. acc_first: the first MMA adds to the
+// stage (1: it holds the decoding constant) or overwrites it (0).
 __device__ __forceinline__ void mma_triple4_issue(uint32_t d, uint32_t a0, uint32_t b0,
-                                                  uint32_t b1, uint32_t idesc, uint32_t sf) {
+                                                  uint32_t b1, uint32_t idesc, uint32_t sf,
+                                                  uint32_t acc_first = 1u) {
 #pragma unroll
   for (int ks = 0; ks < 2; ++ks)
     mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 32 * ks), idesc, sf + sf_tri_col(0),
-             sf + sf_tri_col(1), 1u);
+             sf + sf_tri_col(1), ks == 0 ? acc_first : 1u);
 #pragma unroll
   for (int ks = 0; ks < 2; ++ks)
     mma_mxf4(d, sw128_desc(a0 + 32 * ks), sw128_desc(b0 + 64 + 32 * ks), idesc,
@@ -922,10 +928,10 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
     if (warp == kMmaWarp) tmem_dealloc(tmem_base, kTmemCols);
     return;
   }
-  // The decoding constant (see the epilogue) goes into every accumulator column, of both
-  // stages, before any MMA is issued; each epilogue warp writes its own columns. The FP4 forms
-  // also fill their scale-factor regions (pairs: group 0 the 2^0 region, group 1 the 2^9 one;
-  // triples: group 0 the regions at 496 and 500, group 1 those at 504 and 508).
+  // FP8 pairs: the decoding constant (see the epilogue) goes into every accumulator column,
+  // of both stages, before any MMA is issued; each epilogue warp writes its own columns.
+  // Triples: the scale-factor regions (group 0 those at 240 and 248, group 1 those at 496
+  // and 504); their stages are not preset.
   const float dot_min = 128.0f - 2.0f * static_cast<float>(prm.threshold);
   // triples: 2^23 + 63 (1 + 256 + 65536) + 257 (t + 2), an integer below 2^24
   const uint32_t magic_bits =
@@ -946,8 +952,9 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
   if (warp < kEpi) {
     const uint32_t lanes = (static_cast<uint32_t>(warp & 3) * 32) << 16;
     const uint32_t g = static_cast<uint32_t>(warp >> 2);
-    for (uint32_t st = 0; st < kAccStages; ++st)
-      fill_group(tmem_base + lanes + st * kPairStageCols + kGroupCols * g);
+    if constexpr (!kTriples)
+      for (uint32_t st = 0; st < kAccStages; ++st)
+        fill_group(tmem_base + lanes + st * kPairStageCols + kGroupCols * g);
     if constexpr (kTriples) {
       tmem_st8_fill(tmem_base + lanes + sf_tri_col(2 * g), sf_tri_val(2 * g));
       tmem_st8_fill(tmem_base + lanes + sf_tri_col(2 * g + 1), sf_tri_val(2 * g + 1));
@@ -1110,7 +1117,7 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
           tc_fence_after();
           const uint32_t a0 = smem_u32(a_smem + static_cast<size_t>(as) * kChunkBytes);
           if constexpr (kTriples)
-            mma_triple4_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc, tmem_base);
+            mma_triple4_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc, tmem_base, 0u);
           else
             mma_pair_issue(tmem_base + ac * kPairStageCols, a0, b0, b1, idesc);
           mma_commit(&sm.a_empty[as]);
@@ -1151,10 +1158,12 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
 
   // ---- epilogue warps 0..7: rows (warp % 4) * 32 + lane; group g = warp / 4 reads pairs
   // kGroupCols g .. + kGroupCols - 1 of the stage in two rounds: 64 columns (two loads of 32),
-  // then the rest (FP8: two loads of 32; FP4: loads of 32, 16 and 8). Each column holds
-  // v + MAGIC (the stage was filled with MAGIC before its MMAs), so the common case (no
+  // then the rest (FP8: two loads of 32; FP4: loads of 32, 16 and 8). FP8 pairs: each column
+  // holds v + MAGIC (the stage was filled with MAGIC before its MMAs), so the common case (no
   // candidate in the round's columns) costs one three-input OR per two columns and one vote;
   // the warp writes MAGIC back into its columns before it hands the stage to the MMA issuer.
+  // Triples: the warp adds MAGIC to each column in registers and hands the stage back once
+  // its second round of loads has landed.
   {
     const uint32_t quarter = static_cast<uint32_t>(warp & 3);
     const uint32_t group = static_cast<uint32_t>(warp >> 2);
@@ -1196,6 +1205,14 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
       }
       return (any & 0x8080u) || mx >= tc_bits;
     };
+    // triples: v (an integer, |v| < 2^23) to v + MAGIC, an integer in [2^23, 2^24): exact
+    const float magic_f = __uint_as_float(magic_bits);
+    auto add_magic = [&](uint32_t* raw, auto cols) {
+      constexpr int kCols = decltype(cols)::value;
+#pragma unroll
+      for (int i = 0; i < kCols; ++i)
+        raw[i] = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic_f));
+    };
     // the rare path: one lane's candidate masks of one chunk, bit i for triple i of the chunk
     auto tri_masks = [&](const uint32_t* raw, auto cols, uint32_t (&m)[3]) {
       constexpr int kCols = decltype(cols)::value;
@@ -1225,6 +1242,8 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
       tmem_ld_wait();
       tmem_take(raw0, unused);
       tmem_take(raw1, unused);
+      add_magic(raw0, C32{});
+      add_magic(raw1, C32{});
       const bool mine1 = row_ok && (tri_any(raw0, C32{}) || tri_any(raw1, C32{}));
       if (__any_sync(0xffffffffu, mine1)) {
         // rare: report round 1's candidates now, while its columns are in registers (the
@@ -1245,6 +1264,13 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
       tmem_take(raw0, unused);
       tmem_take16(raw2);
       tmem_take8(raw3);
+      // all of the warp's columns are in registers: hand the stage back
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+      add_magic(raw0, C32{});
+      add_magic(raw2, C16{});
+      add_magic(raw3, C8{});
       const bool mine2 =
           row_ok && (tri_any(raw0, C32{}) || tri_any(raw2, C16{}) || tri_any(raw3, C8{}));
       uint32_t m2[3] = {}, m3[3] = {}, m4[3] = {};
@@ -1253,11 +1279,6 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
         tri_masks(raw2, C16{}, m3);
         tri_masks(raw3, C8{}, m4);
       }
-      fill_group(cols);
-      tmem_st_wait();
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
       if (__any_sync(0xffffffffu, mine2)) {
         report(m2, 64);
         report(m3, 96);
@@ -1344,7 +1365,8 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
 }
 
 // ---------------------------------------------------------------------------------------
-// scan_rows_kernel: narrow passes (<= 128 queries) with the operands swapped.
+// scan_rows_kernel: narrow passes (<= 128 queries) with the operands swapped, at t > 36
+// (at t <= 36 scan_rows3_kernel runs them).
 //
 // The queries are the MMA's A operand (M = 128 rows; a query past the end is a zero row,
 // whose dot products are 0 and never reach dot_min) and the database tiles its B operand,
@@ -1369,12 +1391,13 @@ constexpr int kRowsMaxQueries = kTileRows;   // queries per launch (MMA M)
 // query q): the exact distance of each from popcounts, hits within the threshold written at
 // positions taken with one atomic per warp. Called by all 32 lanes; a lane without
 // candidates passes cand = 0.
+// (stride: bit j of cand stands for row row0 + stride * j; 1 unless given.)
 __device__ __forceinline__ void emit_rows(uint64_t cand, uint64_t row0, uint32_t q,
-                                          const Params& prm, int lane) {
-  if (row0 >= prm.n_rows) {
-    cand = 0;
-  } else if (prm.n_rows - row0 < 64) {
-    cand &= (1ull << (prm.n_rows - row0)) - 1;
+                                          const Params& prm, int lane, uint32_t stride = 1) {
+  {
+    // bits whose row is past the end
+    const uint64_t lim = row0 >= prm.n_rows ? 0 : (prm.n_rows - row0 + stride - 1) / stride;
+    if (lim < 64) cand &= (1ull << lim) - 1;
   }
   uint4 q0 = make_uint4(0, 0, 0, 0), q1 = q0;
   if (cand) {
@@ -1385,7 +1408,7 @@ __device__ __forceinline__ void emit_rows(uint64_t cand, uint64_t row0, uint32_t
   uint64_t hits = 0;
   for (uint64_t m = cand; m; m &= m - 1) {
     const int j = __ffsll(static_cast<long long>(m)) - 1;
-    const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + (row0 + j) * 32);
+    const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + (row0 + stride * j) * 32);
     if (popc256(__ldg(rp), __ldg(rp + 1), q0, q1) <= prm.threshold) hits |= 1ull << j;
   }
   const uint32_t mine = static_cast<uint32_t>(__popcll(hits));
@@ -1404,9 +1427,9 @@ __device__ __forceinline__ void emit_rows(uint64_t cand, uint64_t row0, uint32_t
   for (uint64_t m = hits; m; m &= m - 1, ++pos) {
     if (pos >= prm.capacity) break;
     const int j = __ffsll(static_cast<long long>(m)) - 1;
-    const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + (row0 + j) * 32);
+    const uint4* rp = reinterpret_cast<const uint4*>(prm.rows + (row0 + stride * j) * 32);
     ypdq_hit h;
-    h.index = row0 + j;
+    h.index = row0 + stride * j;
     h.query = q + prm.query_base;
     h.distance = popc256(__ldg(rp), __ldg(rp + 1), q0, q1);
     prm.hits[pos] = h;
@@ -1669,6 +1692,409 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_rows_kernel(const P
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// scan_rows3_kernel: narrow passes (<= 128 queries) at t <= 36 with three database rows per
+// f32 accumulator column and block-scaled FP4 operands.
+//
+// The triple form of scan_pair_kernel with the operands swapped: the queries (126-bit
+// prefixes) are A, M = 128 lanes, expanded once per launch; a tile of 720 database rows is B,
+// rows 3j, 3j + 1 and 3j + 2 in column j (bytes 0-63 and 64-127 of row j of B chunk 0, bytes
+// 0-63 of row j of chunk 1, with B scales 2^-1, 2^7 and 2^15). Column j of lane q then holds
+// e_a + 256 e_b + 65536 e_c over the decoding constant, e = 63 - (distance over the prefix),
+// decoded by the same bit tests. Per database row the tensor core runs 6 MMAs of N = 240 for
+// 720 rows (~1.4 clk) where scan_rows_kernel runs 4 FP8 MMAs of N = 256 for 256 rows (~2 clk),
+// and the epilogue reads 240 columns per 720 rows instead of 256 per 256. TMEM, scale regions
+// and the decoding (MAGIC added in registers) are those of the triple form. Epilogue warp w
+// reads queries 32 (w % 4) + lane and the 120 columns 120 (w / 4) ..; a lane quarter without
+// queries (A rows zero) only hands each stage back. Rows past the end of the last tile are
+// zero B units (their fields stay 0, below every candidate test).
+// Roles: warps 0-7 epilogue, 8 producer (bulk copies of 22.5 KiB packed tiles), 9 MMA and
+// TMEM allocation, 10-13 expanders (thread e: the rows of columns e and e + 128).
+constexpr int kRows3Cols = kPair4N;                 // accumulator columns per tile (MMA N)
+constexpr int kRows3Rows = 3 * kRows3Cols;          // database rows per tile
+constexpr int kRows3PackBytes = kRows3Rows * 32;    // one packed tile
+constexpr int kRows3ChunkBytes = kRows3Cols * 128;  // one B chunk (240 rows x 128 B)
+constexpr int kRows3BStages = 2;                    // expanded tiles (2 chunks each)
+static_assert(kRows3ChunkBytes % 1024 == 0, "B chunks stay 1024-byte aligned");
+
+// expand_row_fp4 with the first unit chosen at run time; keep = 0 writes zero units
+__device__ __forceinline__ void expand_prefix_fp4(const uint4 w0, uint8_t* chunk, int row,
+                                                  int unit0, uint32_t keep) {
+  const uint32_t words[4] = {w0.x, w0.y, w0.z, w0.w};
+  uint8_t* const base = chunk + row * 128;
+  const int sw = row & 7;
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const uint32_t w = words[p];
+    uint4 out;
+    out.x = (((w << 3) & 0x88888888u) | 0x22222222u) & keep;
+    out.y = (((w << 2) & 0x88888888u) | 0x22222222u) & keep;
+    out.z = (((w << 1) & 0x88888888u) | 0x22222222u) & keep;
+    out.w = ((w & 0x88888888u) | 0x22222222u) & keep;
+    *reinterpret_cast<uint4*>(base + (((unit0 + p) ^ sw) << 4)) = out;
+  }
+}
+
+// emit_rows out of line (the rare path; keeps the epilogue's registers for its loads)
+__device__ __noinline__ void emit_rows_call(uint64_t cand, uint64_t row0, uint32_t q,
+                                            const Params* prm, int lane, uint32_t stride) {
+  emit_rows(cand, row0, q, *prm, lane, stride);
+}
+
+__global__ void __launch_bounds__(threads_of(false), 1)
+    scan_rows3_kernel(const __grid_constant__ Params prm) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* const smem_base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  Smem& sm = *reinterpret_cast<Smem*>(smem_base);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t n_pack = prm.pack_stages;
+  const uint32_t n_queries = prm.nq_dev ? min(*prm.nq_dev, prm.n_queries) : prm.n_queries;
+  uint8_t* const q_smem = smem_base + kFixedBytes;  // 128 query rows x 128 B
+  uint8_t* const b_smem = q_smem + kChunkBytes;     // [kRows3BStages][2][240 x 128 B]
+  uint8_t* const packed = smem_base + prm.pack_offset;
+  const uint64_t n_tiles = (prm.n_rows + kRows3Rows - 1) / kRows3Rows;
+  const uint64_t my_tiles =
+      blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  volatile int* abort_flag = &sm.abort_flag;
+
+  if (tid == 0) {
+    for (uint32_t s = 0; s < n_pack; ++s) {
+      mbar_init(&sm.pk_full[s], 1);
+      mbar_init(&sm.pk_empty[s], 4);
+    }
+    for (int s = 0; s < kRows3BStages; ++s) {
+      mbar_init(&sm.a_full[s], 4);   // expanded tile stage s is ready
+      mbar_init(&sm.a_empty[s], 1);  // the MMAs reading it have completed
+    }
+    for (int s = 0; s < kAccStages; ++s) {
+      mbar_init(&sm.acc_full[s], 1);
+      mbar_init(&sm.acc_empty[s], kEpilogueWarps);
+    }
+    mbar_init(&sm.b_full, 4);  // the queries are expanded
+    mbar_init(&sm.epi_exit, kEpilogueWarps);
+    mbar_init(&sm.exp_exit, 4);
+    mbar_init(&sm.mma_done, 1);
+    sm.abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == kMmaWarp) {
+    tmem_alloc(&sm.tmem_base, kTmemCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = sm.tmem_base;
+  if (my_tiles == 0 || n_queries == 0) {
+    if (warp == kMmaWarp) tmem_dealloc(tmem_base, kTmemCols);
+    return;
+  }
+  // The scale regions, as in the triple form. The stages are not preset: a tile's first MMA
+  // overwrites its stage, and the epilogue adds the decoding constant in registers (exact:
+  // v and the sum are integers below 2^24), so it hands a stage back as soon as its loads
+  // have landed, with no tensor-memory stores to wait for.
+  const float magic = 8388608.0f + 4144959.0f + 257.0f * (static_cast<float>(prm.threshold) + 2.0f);
+  constexpr int kGroupCols = kRows3Cols / 2;  // 120 columns per epilogue warp
+  if (warp < kEpilogueWarps) {
+    const uint32_t lanes = (static_cast<uint32_t>(warp & 3) * 32) << 16;
+    const uint32_t g = static_cast<uint32_t>(warp >> 2);
+    tmem_st8_fill(tmem_base + lanes + sf_tri_col(2 * g), sf_tri_val(2 * g));
+    tmem_st8_fill(tmem_base + lanes + sf_tri_col(2 * g + 1), sf_tri_val(2 * g + 1));
+    tmem_st_wait();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+
+  if (warp == kProducerWarp) {
+    if (lane == 0 && !prm.stall) {
+      uint32_t slot = 0, phase = 0, issued = 0;
+      bool ok = true;
+      for (uint64_t k = 0; k < my_tiles; ++k) {
+        const uint64_t tile = blockIdx.x + k * gridDim.x;
+        if (!mbar_wait(&sm.pk_empty[slot], phase ^ 1u, abort_flag, prm.wait_ns)) {
+          ok = false;
+          break;
+        }
+        const uint64_t r0 = tile * kRows3Rows;
+        const uint64_t nr = (prm.n_rows - r0) < kRows3Rows ? (prm.n_rows - r0) : kRows3Rows;
+        const uint32_t bytes = static_cast<uint32_t>(nr * 32);
+        mbar_arrive_expect_tx(&sm.pk_full[slot], bytes);
+        bulk_g2s(packed + slot * kRows3PackBytes, prm.rows + r0 * 32, bytes, &sm.pk_full[slot],
+                 policy_evict_first());
+        ++issued;
+        if (++slot == n_pack) {
+          slot = 0;
+          phase ^= 1u;
+        }
+      }
+      if (!ok) {
+        raise_abort(sm, prm.dev_err);
+        // let the copies already issued land (bounded), as in scan_tc_kernel
+        for (uint32_t k = 1; k <= n_pack && k <= issued; ++k) {
+          const uint32_t sl = (slot + n_pack - k) % n_pack;
+          const uint32_t ph = (k <= slot) ? phase : (phase ^ 1u);
+          const uint64_t t0 = globaltimer_ns();
+          while (!mbar_try_wait(&sm.pk_full[sl], ph))
+            if (globaltimer_ns() - t0 > prm.wait_ns / 4) break;
+        }
+      }
+    }
+    return;
+  }
+
+  if (warp >= kExpandWarp0 && warp < kExpandWarp0 + 4) {
+    const int e = tid - kExpandWarp0 * 32;  // 0..127: query e; tile rows e + 128 i
+    // Thread e expands columns j = e and e + 128 (< 240), the three rows of each: in one
+    // store instruction the lanes write one field of consecutive columns, so eight lanes
+    // (one wavefront of 16-byte stores) cover eight distinct swizzled units. (Consecutive
+    // rows per lane put fields a and c of a column, same unit of chunks 0 and 1, in one
+    // wavefront: twice the store wavefronts.)
+    constexpr int kHalves = (kRows3Cols + 127) / 128;
+    {
+      const uint4 w = static_cast<uint32_t>(e) < n_queries
+                          ? __ldg(reinterpret_cast<const uint4*>(prm.queries +
+                                                                  static_cast<uint64_t>(e) * 32))
+                          : make_uint4(0, 0, 0, 0);
+      if (static_cast<uint32_t>(e) < n_queries)
+        expand_row_fp4<0, true>(w, q_smem, e);
+      else
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          *reinterpret_cast<uint4*>(q_smem + e * 128 + u * 16) = make_uint4(0, 0, 0, 0);
+    }
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.b_full);
+    uint32_t slot = 0, phase = 0;
+    for (uint64_t k = 0; k < my_tiles; ++k) {
+      const uint64_t tile = blockIdx.x + k * gridDim.x;
+      const uint32_t bs = static_cast<uint32_t>(k % kRows3BStages);
+      const uint32_t bph = static_cast<uint32_t>(k / kRows3BStages) & 1u;
+      const uint64_t r0 = tile * kRows3Rows;
+      const uint32_t nr = static_cast<uint32_t>(
+          (prm.n_rows - r0) < kRows3Rows ? (prm.n_rows - r0) : kRows3Rows);
+      if (!mbar_wait(&sm.pk_full[slot], phase, abort_flag, prm.wait_ns)) goto fail;
+      uint4 w[kHalves][3];
+#pragma unroll
+      for (int h = 0; h < kHalves; ++h) {
+        const int j = e + 128 * h;
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+          w[h][f] = j < kRows3Cols ? *reinterpret_cast<const uint4*>(
+                                         packed + slot * kRows3PackBytes + (3 * j + f) * 32)
+                                   : make_uint4(0, 0, 0, 0);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.pk_empty[slot]);
+      if (++slot == n_pack) {
+        slot = 0;
+        phase ^= 1u;
+      }
+      if (!mbar_wait(&sm.a_empty[bs], bph ^ 1u, abort_flag, prm.wait_ns)) goto fail;
+      {
+        uint8_t* const b0 = b_smem + static_cast<size_t>(bs) * 2 * kRows3ChunkBytes;
+        uint8_t* const b1 = b0 + kRows3ChunkBytes;
+#pragma unroll
+        for (int h = 0; h < kHalves; ++h) {
+          const int j = e + 128 * h;
+          if (j >= kRows3Cols) continue;
+#pragma unroll
+          for (int f = 0; f < 3; ++f)
+            expand_prefix_fp4(w[h][f], f == 2 ? b1 : b0, j, f == 1 ? 4 : 0,
+                              static_cast<uint32_t>(3 * j + f) < nr ? 0xFFFFFFFFu : 0u);
+        }
+      }
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.a_full[bs]);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.exp_exit);
+    return;
+  fail:
+    if (lane == 0) {
+      raise_abort(sm, prm.dev_err);
+      mbar_arrive(&sm.exp_exit);
+    }
+    return;
+  }
+
+  if (warp == kMmaWarp) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_mxf4(kRows3Cols);
+      bool ok = mbar_wait(&sm.b_full, 0, abort_flag, prm.wait_ns);
+      tc_fence_after();
+      const uint32_t qa = smem_u32(q_smem);
+      for (uint64_t k = 0; k < my_tiles && ok; ++k) {
+        const uint32_t bs = static_cast<uint32_t>(k % kRows3BStages);
+        const uint32_t ac = static_cast<uint32_t>(k % kAccStages);
+        if (!mbar_wait(&sm.a_full[bs], static_cast<uint32_t>(k / kRows3BStages) & 1u, abort_flag,
+                       prm.wait_ns) ||
+            !mbar_wait(&sm.acc_empty[ac], (static_cast<uint32_t>(k / kAccStages) & 1u) ^ 1u,
+                       abort_flag, prm.wait_ns)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t b0 = smem_u32(b_smem + static_cast<size_t>(bs) * 2 * kRows3ChunkBytes);
+        mma_triple4_issue(tmem_base + ac * kPairStageCols, qa, b0, b0 + kRows3ChunkBytes, idesc,
+                          tmem_base, 0u);
+        mma_commit(&sm.a_empty[bs]);
+        mma_commit(&sm.acc_full[ac]);
+      }
+      if (!ok) raise_abort(sm, prm.dev_err);
+      mma_commit(&sm.mma_done);
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.mma_done, 0))
+        if (globaltimer_ns() - t0 > prm.wait_ns) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
+    }
+    __syncwarp();
+    {
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.epi_exit, 0))
+        if (globaltimer_ns() - t0 > prm.wait_ns) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
+      const uint64_t t1 = globaltimer_ns();
+      while (!mbar_try_wait(&sm.exp_exit, 0))
+        if (globaltimer_ns() - t1 > prm.wait_ns) {
+          raise_abort(sm, prm.dev_err);
+          break;
+        }
+    }
+    tc_fence_after();
+    tmem_dealloc(tmem_base, kTmemCols);
+    return;
+  }
+
+  // ---- epilogue warps 0..7: query q = 32 (warp % 4) + lane; group warp / 4 reads the
+  // stage's columns 120 g .. 120 g + 119 (database rows 360 g .. + 359 of the tile) in two
+  // rounds, 32 + 32 then 32 + 16 + 8, adds the decoding constant to each column and tests
+  // the bits as scan_pair_kernel's triple form does; the stage goes back to the MMA issuer
+  // once the second round's loads have landed
+  {
+    const uint32_t quarter = static_cast<uint32_t>(warp & 3);
+    const uint32_t group = static_cast<uint32_t>(warp >> 2);
+    const uint32_t lane_addr = (quarter * 32) << 16;
+    const uint32_t q = quarter * 32 + lane;
+    const bool q_ok = q < n_queries;
+    const bool active = quarter * 32 < n_queries;
+    // field c's test: the column's bits (a float in [2^23, 2^24)) reach 2^23 + 65536 (126 - t)
+    const uint32_t tc_bits =
+        __float_as_uint(8388608.0f + 65536.0f * (126.0f - static_cast<float>(prm.threshold)));
+    auto tri_any = [&](const uint32_t* raw, auto cols) -> bool {
+      constexpr int kCols = decltype(cols)::value;
+      uint32_t any = 0, mx = 0;
+#pragma unroll
+      for (int i = 0; i < kCols; ++i) {
+        any |= raw[i];
+        mx = max(mx, raw[i]);
+      }
+      return (any & 0x8080u) || mx >= tc_bits;
+    };
+    auto tri_masks = [&](const uint32_t* raw, auto cols, uint32_t (&m)[3]) {
+      constexpr int kCols = decltype(cols)::value;
+#pragma unroll
+      for (int i = 0; i < kCols; ++i) {
+        m[0] |= ((raw[i] >> 7) & 1u) << i;
+        m[1] |= ((raw[i] >> 15) & 1u) << i;
+        m[2] |= (raw[i] >= tc_bits ? 1u : 0u) << i;
+      }
+    };
+    // v (an integer, |v| < 2^23) to v + MAGIC, an integer in [2^23, 2^24): exact
+    auto add_magic = [&](uint32_t* raw, auto cols) {
+      constexpr int kCols = decltype(cols)::value;
+#pragma unroll
+      for (int i = 0; i < kCols; ++i) raw[i] = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic));
+    };
+    using C8 = std::integral_constant<int, 8>;
+    using C16 = std::integral_constant<int, 16>;
+    using C32 = std::integral_constant<int, 32>;
+    bool ok = true;
+    for (uint64_t k = 0; k < my_tiles && ok; ++k) {
+      const uint64_t tile = blockIdx.x + k * gridDim.x;
+      const uint32_t ac = static_cast<uint32_t>(k % kAccStages);
+      if (!mbar_wait(&sm.acc_full[ac], static_cast<uint32_t>(k / kAccStages) & 1u, abort_flag,
+                     prm.wait_ns)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      if (!active) {
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+        continue;
+      }
+      const uint32_t cols = tmem_base + lane_addr + ac * kPairStageCols + kGroupCols * group;
+      // database row of field f of the group's column i: row_g + 3 i + f
+      const uint64_t row_g = tile * kRows3Rows + 3ull * kGroupCols * group;
+      auto report = [&](const uint32_t (&m)[3], uint32_t first) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+          if (__any_sync(0xffffffffu, m[f] != 0))
+            emit_rows_call(m[f], row_g + 3 * first + f, q, &prm, lane, 3);
+      };
+      uint32_t raw0[32], raw1[32];
+      float unused[32];
+      tmem_ld32_nowait(cols, raw0);
+      tmem_ld32_nowait(cols + 32, raw1);
+      tmem_ld_wait();
+      tmem_take(raw0, unused);
+      tmem_take(raw1, unused);
+      add_magic(raw0, C32{});
+      add_magic(raw1, C32{});
+      const bool mine1 = q_ok && (tri_any(raw0, C32{}) || tri_any(raw1, C32{}));
+      if (__any_sync(0xffffffffu, mine1)) {
+        uint32_t m0[3] = {}, m1[3] = {};
+        if (mine1) {
+          tri_masks(raw0, C32{}, m0);
+          tri_masks(raw1, C32{}, m1);
+        }
+        report(m0, 0);
+        report(m1, 32);
+      }
+      uint32_t raw2[16], raw3[8];
+      tmem_ld32_nowait(cols + 64, raw0);
+      tmem_ld16_nowait(cols + 96, raw2);
+      tmem_ld8_nowait(cols + 112, raw3);
+      tmem_ld_wait();
+      tmem_take(raw0, unused);
+      tmem_take16(raw2);
+      tmem_take8(raw3);
+      // all of the warp's columns are in registers: hand the stage back
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
+      add_magic(raw0, C32{});
+      add_magic(raw2, C16{});
+      add_magic(raw3, C8{});
+      const bool mine2 =
+          q_ok && (tri_any(raw0, C32{}) || tri_any(raw2, C16{}) || tri_any(raw3, C8{}));
+      uint32_t m2[3] = {}, m3[3] = {}, m4[3] = {};
+      if (mine2) {
+        tri_masks(raw0, C32{}, m2);
+        tri_masks(raw2, C16{}, m3);
+        tri_masks(raw3, C8{}, m4);
+      }
+      if (__any_sync(0xffffffffu, mine2)) {
+        report(m2, 64);
+        report(m3, 96);
+        report(m4, 112);
+      }
+    }
+    if (!ok && lane == 0) raise_abort(sm, prm.dev_err);
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.epi_exit);
+  }
+}
+
 }  // namespace tc
 
 cudaError_t scan_tc_init() {
@@ -1679,9 +2105,9 @@ cudaError_t scan_tc_init() {
                         reinterpret_cast<const void*>(tc::scan_tc_kernel<false, 8>),
                         reinterpret_cast<const void*>(tc::scan_pair_kernel<tc::kFormFp8Pairs>),
                         reinterpret_cast<const void*>(tc::scan_pair_kernel<tc::kFormFp4Triples>),
-                        reinterpret_cast<const void*>(tc::scan_rows_kernel<4>),
                         reinterpret_cast<const void*>(tc::scan_rows_kernel<6>),
-                        reinterpret_cast<const void*>(tc::scan_rows_kernel<8>)}) {
+                        reinterpret_cast<const void*>(tc::scan_rows_kernel<8>),
+                        reinterpret_cast<const void*>(tc::scan_rows3_kernel)}) {
     const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                static_cast<int>(tc::kSmemLimit));
     if (e != cudaSuccess) return e;
@@ -1716,10 +2142,30 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   const bool half_k = p.threshold <= 36;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
-  // at most 128 queries and no pass width asked for: queries as A, 256 database rows per
-  // MMA (scan_rows_kernel)
-  if (!p.n_tile && !p.pair_n && p.n_queries <= static_cast<uint32_t>(tc::kRowsMaxQueries)) {
-    const int ks = half_k ? 4 : (p.threshold <= 62 ? 6 : 8);
+  // at most 128 queries at t <= 36, no pass width or FP8 pairs asked for: queries as A,
+  // three database rows per accumulator column (scan_rows3_kernel; 0.097 ms on 10M rows for
+  // 1 to 128 queries, against 0.124-0.133 ms for scan_rows_kernel's FP8 form)
+  if (half_k && !p.n_tile && p.pair_n != static_cast<uint32_t>(tc::kPairN) &&
+      p.n_queries <= static_cast<uint32_t>(tc::kRowsMaxQueries)) {
+    const size_t b_end = tc::kFixedBytes + tc::kChunkBytes +
+                         static_cast<size_t>(tc::kRows3BStages) * 2 * tc::kRows3ChunkBytes;
+    size_t stages = (tc::kSmemLimit - 1024 - b_end) / tc::kRows3PackBytes;
+    if (stages > static_cast<size_t>(tc::kMaxPackStages)) stages = tc::kMaxPackStages;
+    if (stages < 2) return cudaErrorInvalidConfiguration;
+    prm.n_tile = tc::kRowsMaxQueries;
+    prm.pack_stages = static_cast<uint32_t>(stages);
+    prm.pack_offset = static_cast<uint32_t>(b_end);
+    const size_t smem = b_end + stages * tc::kRows3PackBytes + 1024;
+    const uint64_t rtiles = (p.n_rows + tc::kRows3Rows - 1) / tc::kRows3Rows;
+    const unsigned g = static_cast<unsigned>(rtiles < static_cast<uint64_t>(num_sms) ? rtiles : num_sms);
+    tc::scan_rows3_kernel<<<g, tc::threads_of(false), smem, s>>>(prm);
+    return cudaGetLastError();
+  }
+  // at most 128 queries at t > 36 and no pass width asked for: queries as A, 256 database
+  // rows per MMA (scan_rows_kernel)
+  if (!half_k && !p.n_tile && !p.pair_n &&
+      p.n_queries <= static_cast<uint32_t>(tc::kRowsMaxQueries)) {
+    const int ks = p.threshold <= 62 ? 6 : 8;
     const int chunks = ks > 4 ? 2 : 1;
     const size_t b_end = tc::kFixedBytes + static_cast<size_t>(chunks) * tc::kChunkBytes +
                          static_cast<size_t>(tc::rows_b_stages(ks)) * chunks * tc::kRowsChunkBytes;
@@ -1732,9 +2178,7 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
     const size_t smem = b_end + stages * tc::kRowsPackBytes + 1024;
     const uint64_t rtiles = (p.n_rows + tc::kRowsN - 1) / tc::kRowsN;
     const unsigned g = static_cast<unsigned>(rtiles < static_cast<uint64_t>(num_sms) ? rtiles : num_sms);
-    if (ks == 4)
-      tc::scan_rows_kernel<4><<<g, tc::threads_of(false), smem, s>>>(prm);
-    else if (ks == 6)
+    if (ks == 6)
       tc::scan_rows_kernel<6><<<g, tc::threads_of(false), smem, s>>>(prm);
     else
       tc::scan_rows_kernel<8><<<g, tc::threads_of(false), smem, s>>>(prm);

@@ -462,7 +462,8 @@ ypdq_status autotune(ypdq_server* S) {
     std::vector<Bucket> cand;
     const uint32_t nq = 8 * b.images;
     if (nq <= 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_SIMT, 0, 0, 0.0f, 0});
-    // up to 128 queries: the launcher's choice, queries as A and 256 rows per MMA
+    // up to 128 queries: the launcher's choice, queries as A (at t <= 36 720 rows per MMA,
+    // three per column, FP4 operands; above, 256 rows per MMA, FP8)
     if (nq <= 128) cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, 0, 0.0f, 0});
     const uint32_t nq64 = (nq + 63u) & ~63u;
     for (uint32_t nt = 64; nt <= 256; nt *= 2)
@@ -684,11 +685,20 @@ ypdq_status ypdq_server_get_stats(ypdq_server* S, ypdq_server_stats* o, int rese
     o->bucket_algo[i] = S->buckets[i].algo;
     const Bucket& b = S->buckets[i];
     const bool tc = b.algo == YPDQ_SCAN_TC;
-    // tensor-core kernel: 0 one query per column (n_tile), 1 pairs, 2 queries as A, 3 FP4
-    // triples
-    o->bucket_kernel[i] = !tc ? 0 : b.pair_n == kPairFp4N ? 3 : b.pair_n ? 1 : b.n_tile ? 0 : 2;
-    o->bucket_n_tile[i] = !tc ? 0 : b.pair_n ? (b.pair_n == kPairFp4N ? 3 : 2) * b.pair_n
-                                             : b.n_tile ? b.n_tile : 128;
+    // tensor-core kernel: 0 one query per column (n_tile), 1 pairs, 2 queries as A (FP8),
+    // 3 FP4 triples, 4 queries as A with three rows per column (FP4; up to 128 queries at
+    // t <= 36, with or without the FP4 form asked for)
+    const bool rows_a = 8 * b.images <= 128 && !b.n_tile && b.pair_n != 256;
+    const bool rows3 = rows_a && S->cfg.threshold <= 36;
+    o->bucket_kernel[i] = !tc                      ? 0
+                          : rows3                  ? 4
+                          : b.pair_n == kPairFp4N ? 3
+                          : b.pair_n              ? 1
+                          : b.n_tile              ? 0
+                                                  : 2;
+    o->bucket_n_tile[i] = !tc || rows_a ? (tc ? 128 : 0)
+                          : b.pair_n    ? (b.pair_n == kPairFp4N ? 3 : 2) * b.pair_n
+                                        : b.n_tile;
     o->bucket_ms[i] = S->buckets[i].ms;
     o->bucket_steps[i] = S->buckets[i].steps;
   }

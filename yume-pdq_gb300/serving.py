@@ -158,7 +158,8 @@ class Server:
         d = {k: getattr(s, k) for k, _ in _lib.ServerStats._fields_ if not k.startswith("bucket")}
         nb = s.n_buckets
         d["buckets"] = [{"images": s.bucket_images[i],
-                         "algo": ({1: "simt", 3: ("tc", "tc pairs", "tc rows", "tc fp4 triples")[s.bucket_kernel[i]]}
+                         "algo": ({1: "simt", 3: ("tc", "tc pairs", "tc rows", "tc fp4 triples",
+                                                  "tc fp4 rows")[s.bucket_kernel[i]]}
                                   .get(s.bucket_algo[i], s.bucket_algo[i])),
                          "n_tile": s.bucket_n_tile[i], "ms": round(float(s.bucket_ms[i]), 4),
                          "steps": s.bucket_steps[i]} for i in range(nb)]
