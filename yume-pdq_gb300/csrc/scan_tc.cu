@@ -869,6 +869,16 @@ __device__ __forceinline__ void mma_triple4_issue(uint32_t d, uint32_t a0, uint3
              sf + sf_tri_col(3), 1u);
 }
 
+// OR of N consecutive registers as a balanced tree (depth log2 N), not one dependent chain:
+// the triple decode runs it on the stage hand-off path.
+template <int N>
+__device__ __forceinline__ uint32_t or_tree(const uint32_t* r) {
+  if constexpr (N == 1)
+    return r[0];
+  else
+    return or_tree<N / 2>(r) | or_tree<N - N / 2>(r + N / 2);
+}
+
 template <int kForm>
 __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
     scan_pair_kernel(const __grid_constant__ Params prm) {
@@ -1195,37 +1205,33 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
     // ordered as integers) reach 2^23 + 65536 (126 - t).
     const uint32_t tc_bits =
         __float_as_uint(8388608.0f + 65536.0f * (126.0f - static_cast<float>(prm.threshold)));
+    // The common-case test, one FADD and half a three-input OR per column: with MAGIC2 =
+    // MAGIC + 65536 (t + 2), v + MAGIC2 has bits 7 and 15 of v + MAGIC (fields a and b) and
+    // reaches 2^24 exactly when field c is a candidate, which sets bit 23 of its bits (the
+    // exponent's low bit). A sum at or past 2^24 may round its low bits, but its column is
+    // flagged either way and the masks come from v + MAGIC (exact).
+    const float magic_f = __uint_as_float(magic_bits);
+    const float magic2_f = magic_f + 65536.0f * (static_cast<float>(prm.threshold) + 2.0f);
     auto tri_any = [&](const uint32_t* raw, auto cols) -> bool {
       constexpr int kCols = decltype(cols)::value;
-      uint32_t any = 0, mx = 0;
-#pragma unroll
-      for (int i = 0; i < kCols; ++i) {
-        any |= raw[i];
-        mx = max(mx, raw[i]);
-      }
-      return (any & 0x8080u) || mx >= tc_bits;
-    };
-    // triples: v (an integer, |v| < 2^23) to v + MAGIC, an integer in [2^23, 2^24): exact
-    const float magic_f = __uint_as_float(magic_bits);
-    auto add_magic = [&](uint32_t* raw, auto cols) {
-      constexpr int kCols = decltype(cols)::value;
+      uint32_t x[kCols];
 #pragma unroll
       for (int i = 0; i < kCols; ++i)
-        raw[i] = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic_f));
+        x[i] = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic2_f));
+      return (or_tree<kCols>(x) & 0x808080u) != 0;
     };
     // the rare path: one lane's candidate masks of one chunk, bit i for triple i of the chunk
+    // (from v + MAGIC: bits 7 and 15, and field c's test on the whole value)
     auto tri_masks = [&](const uint32_t* raw, auto cols, uint32_t (&m)[3]) {
       constexpr int kCols = decltype(cols)::value;
 #pragma unroll
       for (int i = 0; i < kCols; ++i) {
-        m[0] |= ((raw[i] >> 7) & 1u) << i;
-        m[1] |= ((raw[i] >> 15) & 1u) << i;
-        m[2] |= (raw[i] >= tc_bits ? 1u : 0u) << i;
+        const uint32_t r = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic_f));
+        m[0] |= ((r >> 7) & 1u) << i;
+        m[1] |= ((r >> 15) & 1u) << i;
+        m[2] |= (r >= tc_bits ? 1u : 0u) << i;
       }
     };
-    // One tile of the triple form: the group's 120 columns in two rounds (32 + 32, then
-    // 32 + 16 + 8), decoded, the columns reset, the stage handed back, then any candidates
-    // re-checked (queries q_first + 3 i + f for triple i, field f).
     auto triple_tile = [&](uint32_t cols, uint64_t row, bool row_ok, uint64_t q_first,
                            uint32_t n_q, uint32_t (&raw0)[32], uint32_t (&raw1)[32],
                            float (&unused)[32], uint32_t ac) {
@@ -1242,9 +1248,7 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
       tmem_ld_wait();
       tmem_take(raw0, unused);
       tmem_take(raw1, unused);
-      add_magic(raw0, C32{});
-      add_magic(raw1, C32{});
-      const bool mine1 = row_ok && (tri_any(raw0, C32{}) || tri_any(raw1, C32{}));
+      const bool mine1 = row_ok & (tri_any(raw0, C32{}) | tri_any(raw1, C32{}));
       if (__any_sync(0xffffffffu, mine1)) {
         // rare: report round 1's candidates now, while its columns are in registers (the
         // stage is handed back a little later)
@@ -1268,11 +1272,8 @@ __global__ void __launch_bounds__(pair_threads(kForm != 0), 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
-      add_magic(raw0, C32{});
-      add_magic(raw2, C16{});
-      add_magic(raw3, C8{});
       const bool mine2 =
-          row_ok && (tri_any(raw0, C32{}) || tri_any(raw2, C16{}) || tri_any(raw3, C8{}));
+          row_ok & (tri_any(raw0, C32{}) | tri_any(raw2, C16{}) | tri_any(raw3, C8{}));
       uint32_t m2[3] = {}, m3[3] = {}, m4[3] = {};
       if (mine2) {
         tri_masks(raw0, C32{}, m2);
@@ -1714,7 +1715,15 @@ constexpr int kRows3Cols = kPair4N;                 // accumulator columns per t
 constexpr int kRows3Rows = 3 * kRows3Cols;          // database rows per tile
 constexpr int kRows3PackBytes = kRows3Rows * 32;    // one packed tile
 constexpr int kRows3ChunkBytes = kRows3Cols * 128;  // one B chunk (240 rows x 128 B)
-constexpr int kRows3BStages = 2;                    // expanded tiles (2 chunks each)
+// Three expanded tiles in five chunks of 240 rows x 128 B, every byte used: stage s's fields
+// a and b are chunk s (bytes 0-63 and 64-127 of row j); the fields c of stages 0 and 1 are
+// chunk 3 (bytes 0-63 and 64-127), that of stage 2 bytes 0-63 of chunk 4, whose bytes
+// 64-127 of rows 0-127 hold the queries (A). Three stages let the expanders fill a tile while
+// the MMAs of the two before it run (with two, the slowest expander warp, which shares its
+// scheduler with epilogue warps, sat on the MMA chain: ~2,000 clk a tile against ~1,000 of
+// MMAs); the five chunks leave room for three packed tiles in flight.
+constexpr int kRows3BStages = 3;
+constexpr int kRows3BChunks = 5;
 static_assert(kRows3ChunkBytes % 1024 == 0, "B chunks stay 1024-byte aligned");
 
 // expand_row_fp4 with the first unit chosen at run time; keep = 0 writes zero units
@@ -1749,8 +1758,8 @@ __global__ void __launch_bounds__(threads_of(false), 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t n_pack = prm.pack_stages;
   const uint32_t n_queries = prm.nq_dev ? min(*prm.nq_dev, prm.n_queries) : prm.n_queries;
-  uint8_t* const q_smem = smem_base + kFixedBytes;  // 128 query rows x 128 B
-  uint8_t* const b_smem = q_smem + kChunkBytes;     // [kRows3BStages][2][240 x 128 B]
+  uint8_t* const b_smem = smem_base + kFixedBytes;  // [kRows3BChunks][240 x 128 B]
+  uint8_t* const q_smem = b_smem + 4 * kRows3ChunkBytes;  // queries: bytes 64-127 of rows
   uint8_t* const packed = smem_base + prm.pack_offset;
   const uint64_t n_tiles = (prm.n_rows + kRows3Rows - 1) / kRows3Rows;
   const uint64_t my_tiles =
@@ -1844,7 +1853,7 @@ __global__ void __launch_bounds__(threads_of(false), 1)
   }
 
   if (warp >= kExpandWarp0 && warp < kExpandWarp0 + 4) {
-    const int e = tid - kExpandWarp0 * 32;  // 0..127: query e; tile rows e + 128 i
+    const int e = tid - kExpandWarp0 * 32;  // 0..127: query e; the rows of columns e, e + 128
     // Thread e expands columns j = e and e + 128 (< 240), the three rows of each: in one
     // store instruction the lanes write one field of consecutive columns, so eight lanes
     // (one wavefront of 16-byte stores) cover eight distinct swizzled units. (Consecutive
@@ -1857,11 +1866,12 @@ __global__ void __launch_bounds__(threads_of(false), 1)
                                                                   static_cast<uint64_t>(e) * 32))
                           : make_uint4(0, 0, 0, 0);
       if (static_cast<uint32_t>(e) < n_queries)
-        expand_row_fp4<0, true>(w, q_smem, e);
+        expand_row_fp4<4, true>(w, q_smem, e);
       else
 #pragma unroll
         for (int u = 0; u < 8; ++u)
-          *reinterpret_cast<uint4*>(q_smem + e * 128 + u * 16) = make_uint4(0, 0, 0, 0);
+          if ((u ^ (e & 7)) >= 4)  // units 4-7 (swizzled); 0-3 are stage 2's fields c
+            *reinterpret_cast<uint4*>(q_smem + e * 128 + u * 16) = make_uint4(0, 0, 0, 0);
     }
     fence_proxy_async_smem();
     __syncwarp();
@@ -1893,15 +1903,16 @@ __global__ void __launch_bounds__(threads_of(false), 1)
       }
       if (!mbar_wait(&sm.a_empty[bs], bph ^ 1u, abort_flag, prm.wait_ns)) goto fail;
       {
-        uint8_t* const b0 = b_smem + static_cast<size_t>(bs) * 2 * kRows3ChunkBytes;
-        uint8_t* const b1 = b0 + kRows3ChunkBytes;
+        uint8_t* const b0 = b_smem + static_cast<size_t>(bs) * kRows3ChunkBytes;
+        uint8_t* const b1 = b_smem + (bs < 2 ? 3 : 4) * kRows3ChunkBytes;
 #pragma unroll
         for (int h = 0; h < kHalves; ++h) {
           const int j = e + 128 * h;
           if (j >= kRows3Cols) continue;
 #pragma unroll
           for (int f = 0; f < 3; ++f)
-            expand_prefix_fp4(w[h][f], f == 2 ? b1 : b0, j, f == 1 ? 4 : 0,
+            expand_prefix_fp4(w[h][f], f == 2 ? b1 : b0, j,
+                              f == 1 || (f == 2 && bs == 1) ? 4 : 0,
                               static_cast<uint32_t>(3 * j + f) < nr ? 0xFFFFFFFFu : 0u);
         }
       }
@@ -1925,7 +1936,7 @@ __global__ void __launch_bounds__(threads_of(false), 1)
       const uint32_t idesc = idesc_mxf4(kRows3Cols);
       bool ok = mbar_wait(&sm.b_full, 0, abort_flag, prm.wait_ns);
       tc_fence_after();
-      const uint32_t qa = smem_u32(q_smem);
+      const uint32_t qa = smem_u32(q_smem) + 64;  // bytes 64-127 of the rows
       for (uint64_t k = 0; k < my_tiles && ok; ++k) {
         const uint32_t bs = static_cast<uint32_t>(k % kRows3BStages);
         const uint32_t ac = static_cast<uint32_t>(k % kAccStages);
@@ -1937,9 +1948,9 @@ __global__ void __launch_bounds__(threads_of(false), 1)
           break;
         }
         tc_fence_after();
-        const uint32_t b0 = smem_u32(b_smem + static_cast<size_t>(bs) * 2 * kRows3ChunkBytes);
-        mma_triple4_issue(tmem_base + ac * kPairStageCols, qa, b0, b0 + kRows3ChunkBytes, idesc,
-                          tmem_base, 0u);
+        const uint32_t b0 = smem_u32(b_smem + static_cast<size_t>(bs) * kRows3ChunkBytes);
+        const uint32_t b1 = smem_u32(b_smem + (bs < 2 ? 3 : 4) * kRows3ChunkBytes) + (bs == 1 ? 64 : 0);
+        mma_triple4_issue(tmem_base + ac * kPairStageCols, qa, b0, b1, idesc, tmem_base, 0u);
         mma_commit(&sm.a_empty[bs]);
         mma_commit(&sm.acc_full[ac]);
       }
@@ -1987,30 +1998,25 @@ __global__ void __launch_bounds__(threads_of(false), 1)
     // field c's test: the column's bits (a float in [2^23, 2^24)) reach 2^23 + 65536 (126 - t)
     const uint32_t tc_bits =
         __float_as_uint(8388608.0f + 65536.0f * (126.0f - static_cast<float>(prm.threshold)));
+    // the common-case test and the rare path's masks of scan_pair_kernel's triple form
+    const float magic2 = magic + 65536.0f * (static_cast<float>(prm.threshold) + 2.0f);
     auto tri_any = [&](const uint32_t* raw, auto cols) -> bool {
       constexpr int kCols = decltype(cols)::value;
-      uint32_t any = 0, mx = 0;
+      uint32_t x[kCols];
 #pragma unroll
-      for (int i = 0; i < kCols; ++i) {
-        any |= raw[i];
-        mx = max(mx, raw[i]);
-      }
-      return (any & 0x8080u) || mx >= tc_bits;
+      for (int i = 0; i < kCols; ++i)
+        x[i] = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic2));
+      return (or_tree<kCols>(x) & 0x808080u) != 0;
     };
     auto tri_masks = [&](const uint32_t* raw, auto cols, uint32_t (&m)[3]) {
       constexpr int kCols = decltype(cols)::value;
 #pragma unroll
       for (int i = 0; i < kCols; ++i) {
-        m[0] |= ((raw[i] >> 7) & 1u) << i;
-        m[1] |= ((raw[i] >> 15) & 1u) << i;
-        m[2] |= (raw[i] >= tc_bits ? 1u : 0u) << i;
+        const uint32_t r = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic));
+        m[0] |= ((r >> 7) & 1u) << i;
+        m[1] |= ((r >> 15) & 1u) << i;
+        m[2] |= (r >= tc_bits ? 1u : 0u) << i;
       }
-    };
-    // v (an integer, |v| < 2^23) to v + MAGIC, an integer in [2^23, 2^24): exact
-    auto add_magic = [&](uint32_t* raw, auto cols) {
-      constexpr int kCols = decltype(cols)::value;
-#pragma unroll
-      for (int i = 0; i < kCols; ++i) raw[i] = __float_as_uint(__fadd_rn(__uint_as_float(raw[i]), magic));
     };
     using C8 = std::integral_constant<int, 8>;
     using C16 = std::integral_constant<int, 16>;
@@ -2047,9 +2053,7 @@ __global__ void __launch_bounds__(threads_of(false), 1)
       tmem_ld_wait();
       tmem_take(raw0, unused);
       tmem_take(raw1, unused);
-      add_magic(raw0, C32{});
-      add_magic(raw1, C32{});
-      const bool mine1 = q_ok && (tri_any(raw0, C32{}) || tri_any(raw1, C32{}));
+      const bool mine1 = q_ok & (tri_any(raw0, C32{}) | tri_any(raw1, C32{}));
       if (__any_sync(0xffffffffu, mine1)) {
         uint32_t m0[3] = {}, m1[3] = {};
         if (mine1) {
@@ -2071,11 +2075,8 @@ __global__ void __launch_bounds__(threads_of(false), 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.acc_empty[ac]);
-      add_magic(raw0, C32{});
-      add_magic(raw2, C16{});
-      add_magic(raw3, C8{});
       const bool mine2 =
-          q_ok && (tri_any(raw0, C32{}) || tri_any(raw2, C16{}) || tri_any(raw3, C8{}));
+          q_ok & (tri_any(raw0, C32{}) | tri_any(raw2, C16{}) | tri_any(raw3, C8{}));
       uint32_t m2[3] = {}, m3[3] = {}, m4[3] = {};
       if (mine2) {
         tri_masks(raw0, C32{}, m2);
@@ -2147,8 +2148,8 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   // 1 to 128 queries, against 0.124-0.133 ms for scan_rows_kernel's FP8 form)
   if (half_k && !p.n_tile && p.pair_n != static_cast<uint32_t>(tc::kPairN) &&
       p.n_queries <= static_cast<uint32_t>(tc::kRowsMaxQueries)) {
-    const size_t b_end = tc::kFixedBytes + tc::kChunkBytes +
-                         static_cast<size_t>(tc::kRows3BStages) * 2 * tc::kRows3ChunkBytes;
+    const size_t b_end = tc::kFixedBytes +
+                         static_cast<size_t>(tc::kRows3BChunks) * tc::kRows3ChunkBytes;
     size_t stages = (tc::kSmemLimit - 1024 - b_end) / tc::kRows3PackBytes;
     if (stages > static_cast<size_t>(tc::kMaxPackStages)) stages = tc::kMaxPackStages;
     if (stages < 2) return cudaErrorInvalidConfiguration;

@@ -60,15 +60,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// mbar_try_wait that may suspend the thread until the phase completes or about hint_ns pass
+// (the suspend-time hint of mbarrier.try_wait), instead of the hardware's short default.
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_t parity,
+                                                   uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // Wait for the phase with the given parity. Gives up (returns false) when *abort_flag is
-// set by another warp or when limit_ns passes; the caller then raises the error.
+// set by another warp or when limit_ns passes; the caller then raises the error. Between
+// checks the thread sleeps in try_wait (up to 20 us a time) rather than spinning: a spinning
+// waiter takes issue slots from the warps that share its scheduler, which in the tensor-core
+// scans are the expanders and the epilogue on the critical path.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
                                           const volatile int* abort_flag,
                                           uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   for (;;) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_hint(bar, parity, 20000u)) return true;
     if (*abort_flag) return false;
     if (globaltimer_ns() - t0 > limit_ns) return false;
   }
