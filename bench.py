@@ -258,7 +258,7 @@ def fp4_dense_burst(device=0, n=8192, reps=10):
 def scan_algo_used(algo, nq, threshold):
     """The algorithm ypdq_scan runs for YPDQ_SCAN_AUTO (mirrors auto_scan_algo in scan.cu)."""
     if algo == 0:
-        simt_max = (13 if threshold <= 34 else 9 if threshold <= 36 else
+        simt_max = (9 if threshold <= 34 else 6 if threshold <= 36 else
                     24 if threshold <= 62 else 12)
         return 1 if nq <= simt_max else 3
     return algo

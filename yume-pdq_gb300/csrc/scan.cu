@@ -264,11 +264,11 @@ cudaError_t scan_init() {
 // SIMT is HBM-bound up to a few queries; past that it is bound by its popcount and logic
 // pipes, at 2, 3 or 4 popcounts per pair depending on the threshold (the prefix bound in
 // scan_simt_kernel). A narrow tensor-core pass (at most 128 queries) costs about the time of
-// 13 SIMT queries at t <= 34 (10M rows: 0.100 ms against 0.089 ms for 12 SIMT queries and
-// 0.100 ms for 14), 9 at t = 35..36 (the SIMT side at three popcounts: 0.088 ms for 8,
-// 0.106 ms for 10), 24 at t <= 62 and 12 above (the FP8 passes, neither side pruned as far).
+// 9 SIMT queries at t <= 34 (10M rows: 0.072-0.078 ms against 0.066 ms for 8 SIMT queries
+// and 0.080 ms for 10), 6 at t = 35..36 (the SIMT side at three popcounts: 0.071 ms for 6,
+// 0.088 ms for 8), 24 at t <= 62 and 12 above (the FP8 passes, neither side pruned as far).
 int auto_scan_algo(uint32_t n_queries, uint32_t threshold) {
-  const uint32_t simt_max = threshold <= 34 ? 13 : threshold <= 36 ? 9 : threshold <= 62 ? 24 : 12;
+  const uint32_t simt_max = threshold <= 34 ? 9 : threshold <= 36 ? 6 : threshold <= 62 ? 24 : 12;
   return n_queries <= simt_max ? YPDQ_SCAN_SIMT : YPDQ_SCAN_TC;
 }
 
