@@ -427,7 +427,8 @@ typedef struct {
   uint32_t n_buckets;
   uint32_t bucket_images[YPDQ_SERVER_MAX_BUCKETS];
   int32_t bucket_algo[YPDQ_SERVER_MAX_BUCKETS];     /* ypdq_scan_algo the bucket's graph uses */
-  uint32_t bucket_n_tile[YPDQ_SERVER_MAX_BUCKETS];  /* tensor-core queries per pass (0: SIMT) */
+  uint32_t bucket_n_tile[YPDQ_SERVER_MAX_BUCKETS];  /* tensor-core queries per pass or launch
+                                                       (0: SIMT) */
   float bucket_ms[YPDQ_SERVER_MAX_BUCKETS];         /* step time measured by the autotuner */
   uint64_t bucket_steps[YPDQ_SERVER_MAX_BUCKETS];   /* steps launched per bucket */
   uint32_t bucket_kernel[YPDQ_SERVER_MAX_BUCKETS];  /* tensor-core scan form: 0 one query per

@@ -421,17 +421,18 @@ def test_rows_kernel_matches_oracle(ctx, yp, oracle, n_q):
         assert np.array_equal(as_tuples(got), as_tuples(want)), (t, len(got), len(want))
 
 
-@pytest.mark.parametrize("n_q", [1, 2, 3, 31, 32, 33, 64, 65, 100, 127, 128])
+@pytest.mark.parametrize("n_q", [1, 2, 3, 31, 32, 33, 64, 65, 100, 127, 128, 129, 200, 256,
+                                 300, 385, 512])
 def test_fp4_rows_kernel_matches_oracle(ctx, yp, oracle, n_q):
-    """YPDQ_SCAN_TC_FP4 (and YPDQ_SCAN_TC) with at most 128 queries at t <= 36: the queries
-    are the MMA's A operand and three database rows share each f32 accumulator column (rows
-    3j, 3j + 1, 3j + 2 of a 720-row tile with B scales 2^-1, 2^7, 2^15), the first 126 bits
-    as the bound. Row counts that end mid-tile and mid-column (6000 + 0, 1, 2 rows; 5761: one
-    row in the last tile), the three rows of one column equal or complementary to queries
-    (every field at its extreme), rows that differ from a query only in the two prefix bits
-    the bound leaves out, a run of hits across the columns of one tile, lane quarters with
-    and without queries, every threshold 0..36 at one size; above 36 the call runs the FP8
-    scan."""
+    """YPDQ_SCAN_TC_FP4 (and YPDQ_SCAN_TC) with at most 512 queries at t <= 36, one launch per
+    128 queries: the queries are the MMA's A operand and three database rows share each f32
+    accumulator column (rows 3j, 3j + 1, 3j + 2 of a 720-row tile with B scales 2^-1, 2^7,
+    2^15), the first 126 bits as the bound. Row counts that end mid-tile and mid-column
+    (6000 + 0, 1, 2 rows; 5761: one row in the last tile), the three rows of one column equal
+    or complementary to queries (every field at its extreme), rows that differ from a query
+    only in the two prefix bits the bound leaves out, a run of hits across the columns of one
+    tile, lane quarters with and without queries, launches with a partial last 128, every
+    threshold 0..36 at one size; above 36 the call runs the FP8 scan."""
     n_rows = 5761 if n_q == 64 else 6000 + n_q % 3  # 5761: one row in the last tile
     rows = yp.synth.rows_128(n_rows, seed=n_q + 1300)
     q = yp.synth.rows_128(n_q, seed=n_q + 1301)

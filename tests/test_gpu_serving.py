@@ -160,12 +160,13 @@ def test_autotune_table_and_target(ctx, yp, workload):
         assert all(b["ms"] > 0 and b["algo"] in ("simt", "tc", "tc pairs", "tc rows",
                                                  "tc fp4 triples", "tc fp4 rows")
                    for b in st["buckets"])
-        # passes of 512 queries in pairs and of 720 in triples are timed from 17 images
-        assert all(b["algo"] not in ("tc pairs", "tc fp4 triples") or b["images"] > 16
-                   for b in st["buckets"])
-        # queries as the MMA's A operand are timed up to 16 images (128 queries)
-        assert all(b["algo"] not in ("tc rows", "tc fp4 rows") or b["images"] <= 16
-                   for b in st["buckets"])
+        # FP8 pair passes are timed from 17 images; FP4 triple passes run past 64 images only
+        assert all(b["algo"] != "tc pairs" or b["images"] > 16 for b in st["buckets"])
+        assert all(b["algo"] != "tc fp4 triples" for b in st["buckets"])
+        # queries as the MMA's A operand: FP8 up to 16 images (128 queries, t > 36 only),
+        # FP4 with three rows per column up to 64 images (512 queries, 128 per launch)
+        assert all(b["algo"] != "tc rows" for b in st["buckets"])
+        assert all(b["algo"] != "tc fp4 rows" or b["n_tile"] == 128 for b in st["buckets"])
         srv.submit(imgs[:50], tag=0)
         (r,) = srv.drain()
         assert np.array_equal(r.hits, yp.screen_host(ctx, db, imgs[:50], threshold=31))

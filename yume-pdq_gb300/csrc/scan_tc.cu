@@ -215,6 +215,7 @@ struct Params {
   int* dev_err;
   uint32_t query_base;    // added to reported query numbers
   const uint32_t* nq_dev; // device-side query count (graph replay), bounded by n_queries
+  uint32_t nq_off;        // scan_rows3_kernel: this launch's first query of the *nq_dev ones
   uint32_t pack_stages;   // packed tiles in flight (<= kMaxPackStages)
   uint32_t pack_offset;   // byte offset of the packed ring in shared memory
   uint32_t a_stages;      // expanded tiles in flight
@@ -1758,7 +1759,12 @@ __global__ void __launch_bounds__(threads_of(false), 1)
   Smem& sm = *reinterpret_cast<Smem*>(smem_base);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t n_pack = prm.pack_stages;
-  const uint32_t n_queries = prm.nq_dev ? min(*prm.nq_dev, prm.n_queries) : prm.n_queries;
+  // a launch covers queries nq_off .. nq_off + n_queries - 1 of a device-side count
+  uint32_t n_queries = prm.n_queries;
+  if (prm.nq_dev) {
+    const uint32_t nq = *prm.nq_dev;
+    n_queries = nq > prm.nq_off ? min(nq - prm.nq_off, prm.n_queries) : 0u;
+  }
   uint8_t* const b_smem = smem_base + kFixedBytes;  // [kRows3BChunks][240 x 128 B]
   uint8_t* const q_smem = b_smem + 4 * kRows3ChunkBytes;  // queries: bytes 64-127 of rows
   uint8_t* const packed = smem_base + prm.pack_offset;
@@ -2144,11 +2150,13 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   const bool half_k = p.threshold <= 36;
   const uint64_t tiles = (p.n_rows + tc::kTileRows - 1) / tc::kTileRows;
   const uint64_t grid = tiles < static_cast<uint64_t>(num_sms) ? tiles : num_sms;
-  // at most 128 queries at t <= 36, no pass width or FP8 pairs asked for: queries as A,
-  // three database rows per accumulator column (scan_rows3_kernel; 0.072-0.079 ms on 10M
-  // rows for 1 to 128 queries, against 0.124-0.133 ms for scan_rows_kernel's FP8 form)
+  // At t <= 36 with no pass width or FP8 pairs asked for, up to 512 queries: queries as A,
+  // three database rows per accumulator column (scan_rows3_kernel), one launch per 128
+  // queries. On 10M rows a launch takes 0.072-0.079 ms for 1 to 128 queries, so 2 to 4 of
+  // them beat one 256-query pass of scan_tc_kernel (0.23 ms) and one 720-query triple pass
+  // (0.327 ms); past 512 queries the triple passes cost less.
   if (half_k && !p.n_tile && p.pair_n != static_cast<uint32_t>(tc::kPairN) &&
-      p.n_queries <= static_cast<uint32_t>(tc::kRowsMaxQueries)) {
+      p.n_queries <= 4u * static_cast<uint32_t>(tc::kRowsMaxQueries)) {
     const size_t b_end = tc::kFixedBytes +
                          static_cast<size_t>(tc::kRows3BChunks) * tc::kRows3ChunkBytes;
     size_t stages = (tc::kSmemLimit - 1024 - b_end) / tc::kRows3PackBytes;
@@ -2160,8 +2168,20 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
     const size_t smem = b_end + stages * tc::kRows3PackBytes + 1024;
     const uint64_t rtiles = (p.n_rows + tc::kRows3Rows - 1) / tc::kRows3Rows;
     const unsigned g = static_cast<unsigned>(rtiles < static_cast<uint64_t>(num_sms) ? rtiles : num_sms);
-    tc::scan_rows3_kernel<<<g, tc::threads_of(false), smem, s>>>(prm);
-    return cudaGetLastError();
+    for (uint32_t q0 = 0; q0 < p.n_queries; q0 += tc::kRowsMaxQueries) {
+      tc::Params c = prm;
+      c.queries = p.queries + static_cast<size_t>(q0) * 32;
+      c.n_queries = p.n_queries - q0 < static_cast<uint32_t>(tc::kRowsMaxQueries)
+                        ? p.n_queries - q0
+                        : static_cast<uint32_t>(tc::kRowsMaxQueries);
+      c.query_base = p.query_base + q0;
+      c.nq_off = q0;
+      c.stall = q0 == 0 ? prm.stall : 0;
+      tc::scan_rows3_kernel<<<g, tc::threads_of(false), smem, s>>>(c);
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
   }
   // at most 128 queries at t > 36 and no pass width asked for: queries as A, 256 database
   // rows per MMA (scan_rows_kernel)
@@ -2189,19 +2209,13 @@ cudaError_t launch_scan_tc(const ScanLaunch& p, int num_sms, cudaStream_t s) {
   if (p.pair_n && (!half_k || (p.pair_n != static_cast<uint32_t>(tc::kPairN) &&
                                 p.pair_n != kPairFp4N)))
     return cudaErrorInvalidValue;  // pairs need the 128-bit bound (t <= 36)
-  // at t <= 36 and past one pass of 256 (or when asked for): several queries per accumulator
-  // column (scan_pair_kernel), FP8 pairs in passes of 512 or, with pair_n = kPairFp4N, FP4
-  // triples in passes of 720
+  // at t <= 36 past 512 queries (or when asked for): several queries per accumulator column
+  // (scan_pair_kernel), FP4 triples in passes of 720 or, with pair_n = 256, FP8 pairs in
+  // passes of 512. A triple pass costs less than a pair pass (0.327 against 0.36 ms on 10M
+  // rows) and covers more queries, so without a form asked for the triples run.
   if (half_k && !p.n_tile && (p.pair_n || p.n_queries > static_cast<uint32_t>(tc::kMaxN))) {
-    // Without a form asked for: a pass of 720 queries in FP4 triples costs ~1.15 x a pass of
-    // 512 in FP8 pairs (0.415 vs 0.36 ms on 10M rows), so take the form with fewer pass-costs
-    uint64_t p3 = (p.n_queries + tc::form_queries(tc::kFormFp4Triples) - 1) /
-                  tc::form_queries(tc::kFormFp4Triples);
-    uint64_t p2 = (p.n_queries + tc::form_queries(tc::kFormFp8Pairs) - 1) /
-                  tc::form_queries(tc::kFormFp8Pairs);
-    const bool auto_triples = !p.pair_n && 83 * p3 < 72 * p2;
-    const int form = p.pair_n == kPairFp4N || auto_triples ? tc::kFormFp4Triples
-                                                           : tc::kFormFp8Pairs;
+    const int form = p.pair_n == static_cast<uint32_t>(tc::kPairN) ? tc::kFormFp8Pairs
+                                                                   : tc::kFormFp4Triples;
     prm.n_tile = static_cast<uint32_t>(tc::form_queries(form));
     prm.a_stages = tc::kPairAStages;
     // layout: [fixed Smem][A: 4 x 16 KB][B: 2 x 256 pairs x 128 B][packed ring], 1024-aligned

@@ -462,18 +462,16 @@ ypdq_status autotune(ypdq_server* S) {
     std::vector<Bucket> cand;
     const uint32_t nq = 8 * b.images;
     if (nq <= 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_SIMT, 0, 0, 0.0f, 0});
-    // up to 128 queries: the launcher's choice, queries as A (at t <= 36 720 rows per MMA,
-    // three per column, FP4 operands; above, 256 rows per MMA, FP8)
-    if (nq <= 128) cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, 0, 0.0f, 0});
+    // the launcher's choice: at t <= 36 queries as A with three database rows per column (FP4,
+    // one launch per 128 queries) up to 512 queries and FP4 triple passes of 720 past that;
+    // above t = 36 queries as A (FP8) up to 128 queries, then one query per column
+    cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, 0, 0.0f, 0});
     const uint32_t nq64 = (nq + 63u) & ~63u;
     for (uint32_t nt = 64; nt <= 256; nt *= 2)
       if (nt <= nq64 || nt == 64) cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, nt, 0, 0.0f, 0});
-    // several queries per accumulator column (t <= 36): passes of 512 queries in pairs
-    // (FP8 operands) and of 3 kPairFp4N in triples (block-scaled FP4 operands)
-    if (S->cfg.threshold <= 36 && nq > 128) {
+    // FP8 pairs, passes of 512 queries (t <= 36)
+    if (S->cfg.threshold <= 36 && nq > 128)
       cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, 256, 0.0f, 0});
-      cand.push_back(Bucket{b.images, YPDQ_SCAN_TC, 0, kPairFp4N, 0.0f, 0});
-    }
     float best = 0.0f;
     for (Bucket& c : cand) {
       ypdq_status st = time_bucket(S, c, &c.ms);
@@ -685,20 +683,27 @@ ypdq_status ypdq_server_get_stats(ypdq_server* S, ypdq_server_stats* o, int rese
     o->bucket_algo[i] = S->buckets[i].algo;
     const Bucket& b = S->buckets[i];
     const bool tc = b.algo == YPDQ_SCAN_TC;
-    // tensor-core kernel: 0 one query per column (n_tile), 1 pairs, 2 queries as A (FP8),
-    // 3 FP4 triples, 4 queries as A with three rows per column (FP4; up to 128 queries at
-    // t <= 36, with or without the FP4 form asked for)
-    const bool rows_a = 8 * b.images <= 128 && !b.n_tile && b.pair_n != 256;
-    const bool rows3 = rows_a && S->cfg.threshold <= 36;
-    o->bucket_kernel[i] = !tc                      ? 0
-                          : rows3                  ? 4
-                          : b.pair_n == kPairFp4N ? 3
-                          : b.pair_n              ? 1
-                          : b.n_tile              ? 0
-                                                  : 2;
-    o->bucket_n_tile[i] = !tc || rows_a ? (tc ? 128 : 0)
-                          : b.pair_n    ? (b.pair_n == kPairFp4N ? 3 : 2) * b.pair_n
-                                        : b.n_tile;
+    // tensor-core kernel: 0 one query per column, 1 FP8 pairs, 2 queries as A (FP8), 3 FP4
+    // triples, 4 queries as A with three database rows per column (FP4); bucket_n_tile the
+    // queries per pass or launch
+    const uint32_t nq = 8 * b.images;
+    const bool low_t = S->cfg.threshold <= 36;
+    uint32_t kern = 0, width = 0;
+    if (tc) {
+      if (b.n_tile) {
+        kern = 0, width = b.n_tile;
+      } else if (b.pair_n == 256) {
+        kern = 1, width = 512;
+      } else if (low_t) {
+        kern = nq <= 512 ? 4 : 3, width = nq <= 512 ? 128 : 3 * kPairFp4N;
+      } else if (nq <= 128) {
+        kern = 2, width = 128;
+      } else {
+        kern = 0, width = std::min(256u, (nq + 63u) & ~63u);
+      }
+    }
+    o->bucket_kernel[i] = kern;
+    o->bucket_n_tile[i] = width;
     o->bucket_ms[i] = S->buckets[i].ms;
     o->bucket_steps[i] = S->buckets[i].steps;
   }
