@@ -146,8 +146,9 @@ def test_screen_chunk_plan(yp):
     small = np.diff(plan(1024, 0, 60_000, 31))
     assert (np.diff(small[:-1]) >= 0).all() and len(small) >= len(sizes) and small.max() <= 304
     # the Jarosz filter (dct_precision 0x200) adds ~1 us of compute per image: where the scan
-    # dominates, its chunks grow at least as fast
-    assert len(plan(1024, 0, 10_000_000, 31, dct=0x200)) <= len(plan(1024, 0, 10_000_000, 31))
+    # dominates (30M rows: ~11 us of scan per image against ~5 us of copy), its chunks grow
+    # at least as fast
+    assert len(plan(1024, 0, 30_000_000, 31, dct=0x200)) <= len(plan(1024, 0, 30_000_000, 31))
     assert lib.ypdq_screen_plan(10, 9, 0, 1, 31, bounds, ctypes.byref(k)) == yp._lib.ERR_INVALID
     assert lib.ypdq_screen_plan(-1, 0, 0, 1, 31, bounds, ctypes.byref(k)) == yp._lib.ERR_INVALID
     assert lib.ypdq_screen_plan(10, 0, 0, 1, 31, None, ctypes.byref(k)) == yp._lib.ERR_INVALID

@@ -162,10 +162,10 @@ struct ChunkCost {
   double fixed_us, per_image_us;
 };
 ChunkCost screen_chunk_cost(int input_kind, bool jarosz, uint64_t n_rows, uint32_t threshold) {
-  // the tensor-core scan: 16.5 T (row, query) pairs/s in passes of 720 queries taken in
+  // the tensor-core scan: 21.5 T (row, query) pairs/s in passes of 720 queries taken in
   // triples (FP4, the 126-bit prefix bound), 9.5 T with the 192-bit bound, 8.3 T with all
   // 256 bits; 8 queries per image
-  const double pairs_per_us = threshold <= 36 ? 16.5e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
+  const double pairs_per_us = threshold <= 36 ? 21.5e6 : threshold <= 62 ? 9.5e6 : 8.3e6;
   const double scan_us = 8.0 * static_cast<double>(n_rows) / pairs_per_us;
   // the Jarosz filter: four passes, each at least one line's sequential replay (512
   // dependent steps, ~5 us) however few images the chunk holds, plus the DCT
