@@ -604,6 +604,7 @@ def run_ours(args):
     e2e_hits = h_hits[:min(nh.value, len(h_hits))].copy()
     ctx.lib.ypdq_free_host(ctx.handle, h_img)
     stream_e2e = e2e_stream(yp, ctx, db, batch, args, pg, world, hits_per_step)
+    link = host_link(batch.nbytes, B) if rank == 0 else None
     # the serving sweep, the heavy-hit database and the precision variants describe one GPU:
     # rank 0 runs them (the other replicas wait at the final barrier)
     serve = serving(yp, ctx, db, batch, args) if rank == 0 else None
@@ -721,7 +722,10 @@ def run_ours(args):
                         "pinned host f32 images each, hits back to host memory; the copies of "
                         "one step overlap the hash and scan of another" % (args.steps, B),
                 "ms_per_step": stream_e2e["ms_per_step"],
-                "request_latency_ms": stream_e2e["latency_ms"]},
+                "request_latency_ms": stream_e2e["latency_ms"],
+                "frac_of_host_link": (stream_e2e["value"] / link["images_per_s_ceiling"]
+                                      if link else None)},
+        "host_link": link,
         "e2e_blocking": {"value": e2e_value, "unit": UNIT,
                          "path": "one blocking ypdq_screen_host call per batch of %d pinned "
                                  "host images (copies and compute overlap inside the call "
@@ -756,6 +760,32 @@ def cpu_workload(args, sample):
     hashes, _, _, _ = oracle.hash_batch(imgs)
     yp.synth.plant_near_duplicates(rows, hashes, args.planted, args.seed + 99)
     return imgs[:sample], rows
+
+
+def host_link(nbytes, images, reps=5):
+    """The host link's H2D rate: copies of nbytes from pinned host memory to the device by the
+    copy engine (torch, CUDA events on the copy's stream, median of reps after one warm copy),
+    and the images/s a stream of nbytes-sized batches could not exceed."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    ms = []
+    with torch.cuda.stream(s):
+        for rep in range(reps + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            d.copy_(h, non_blocking=True)
+            e1.record(s)
+            e1.synchronize()
+            if rep:
+                ms.append(e0.elapsed_time(e1))
+    t = statistics.median(ms)
+    del h, d
+    return {"bytes": nbytes, "ms": t, "h2d_GB_s": nbytes / (t / 1e3) / 1e9,
+            "images_per_s_ceiling": images / (t / 1e3),
+            "how": "torch copy of pinned host memory to the device, CUDA events, median of %d"
+                   % reps}
 
 
 def e2e_stream(yp, ctx, db, batch, args, pg, world, hits_per_step):
