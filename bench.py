@@ -816,8 +816,15 @@ def e2e_stream(yp, ctx, db, batch, args, pg, world, hits_per_step):
     run(max(1, args.warmup))
     if pg:
         pg.barrier()
+    # the submitting loop runs with Python's collector paused, as the serving sweep's does
+    import gc
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
-    res = run(args.steps)
+    try:
+        res = run(args.steps)
+    finally:
+        gc.enable()
     wall_ms = (time.perf_counter() - t0) * 1e3
     _, value = aggregate_over_ranks(pg, wall_ms, world, B * args.steps)
     assert all(r.ok for r in res) and len(res) == args.steps
