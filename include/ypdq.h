@@ -132,12 +132,13 @@ typedef enum {
   YPDQ_SCAN_AUTO = 0,   /* pick by query count */
   YPDQ_SCAN_SIMT = 1,   /* XOR + popcount, one row per thread */
   YPDQ_SCAN_B1MMA = 2,  /* legacy binary MMA (mma.sync .b1 .xor.popc) */
-  YPDQ_SCAN_TC = 3,     /* tcgen05 FP8 tensor cores on +-1 vectors: dot = 256 - 2 d */
-  YPDQ_SCAN_TC_FP4 = 4  /* tcgen05 block-scaled FP4 (e2m1), three queries per accumulator
-                           column, passes of 720 queries, at threshold <= 36; above that the
-                           same as YPDQ_SCAN_TC (which, past 256 queries at threshold <= 36,
-                           itself takes this form or FP8 pairs, whichever needs fewer
-                           pass-costs) */
+  YPDQ_SCAN_TC = 3,     /* tcgen05 tensor cores on +-1 vectors: at threshold <= 36 block-scaled
+                           FP4 (e2m1) on the first 126 bits, up to 512 queries with three
+                           database rows per accumulator column (launches of 128 queries),
+                           past that three queries per column (passes of 720); above 36 FP8
+                           (dot = 256 - 2 d) */
+  YPDQ_SCAN_TC_FP4 = 4  /* the FP4 forms of YPDQ_SCAN_TC at threshold <= 36 (the same choice
+                           between them); above that the same as YPDQ_SCAN_TC */
 } ypdq_scan_algo;
 
 /* ------------------------------------------------------------------ context */
