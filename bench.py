@@ -622,8 +622,21 @@ def run_ours(args):
     hash_avg = statistics.mean(hash_ms)
     scan_avg = statistics.mean(scan_ms)
     algo = scan_algo_used(args.algo, nq, args.threshold)
-    scan_launches = 1 if algo in (3, 4) else (nq + 2047) // 2048
-    if scan_avg >= hash_avg and algo in (3, 4):
+    # the tensor-core form launch_scan_tc takes (mirrors it): at t <= 36 FP4 row triples up
+    # to 512 queries (launches of 128), FP4 query triples past that (passes of 720), or with
+    # YPDQ_SCAN_TC_FP8 FP8 query pairs past 256 (passes of 512) and single queries below;
+    # above t = 36 single queries (passes of 256)
+    low_t = args.threshold <= 36
+    if low_t and args.algo != 5:
+        form = "rows3" if nq <= 512 else "triples"
+    elif low_t:
+        form = "pairs" if nq > 256 else "single"
+    else:
+        form = "single"
+    rows3_launches = (nq + 127) // 128
+    scan_launches = ((rows3_launches if form == "rows3" else 1) if algo in (3, 4, 5)
+                     else (nq + 2047) // 2048)
+    if scan_avg >= hash_avg and algo in (3, 4, 5):
         # tensor-core scan, one launch per step: FP8 flops the MMAs execute per (row, query)
         # pair, 2 * K: K = 128 at t <= 36 and 192 for passes of 256 queries at t <= 62 (the
         # prefix bound; mirrors launch_scan_tc), else 256. Peak: the dense FP8 burst measured
@@ -632,13 +645,9 @@ def run_ours(args):
                   192 if (nq > 128 and args.threshold <= 62) else 256)
         flops = 2.0 * k_bits * nq * n
         achieved = flops / (scan_avg / 1000.0) / 1e12
-        # past 256 queries at t <= 36 the launch runs several queries per accumulator column:
-        # FP8 pairs (passes of 512) or FP4 triples (passes of 720), whichever needs fewer
-        # pass-costs (mirrors launch_scan_tc)
-        pairs = args.threshold <= 36 and nq > 256
-        triples = pairs and (83 * -(-nq // 720) < 72 * -(-nq // 512)
-                             or args.algo == 4)
-        per_pass = 720 if triples else 512 if pairs else 256
+        triples = form in ("triples", "rows3")  # the FP4 forms
+        pairs = form != "single"  # several queries (or rows) per accumulator column
+        per_pass = {"triples": 720, "rows3": 128, "pairs": 512}.get(form, 256)
         passes = (nq + per_pass - 1) // per_pass
         if triples:
             fp4 = fp4_dense_burst(local) if rank == 0 else None
@@ -647,7 +656,9 @@ def run_ours(args):
                            "8192^3, best of 10, this GPU, this run)" if fp4 else
                            "measured fp8 burst x 2 (fp4 dense)")
             kernel = ("scan_pair_kernel<2> (tcgen05 kind::mxf4 block-scaled e2m1, three queries "
-                      "per f32 accumulator column)")
+                      "per f32 accumulator column)" if form == "triples" else
+                      "scan_rows3_kernel (tcgen05 kind::mxf4 block-scaled e2m1, queries as A, "
+                      "three database rows per f32 accumulator column)")
         else:
             fp8 = fp8_dense_burst(local) if rank == 0 else None
             peak = fp8 if fp8 else 2 * bf16_peak
@@ -671,7 +682,7 @@ def run_ours(args):
                                     "a counter" % (passes, per_pass),
                     "mma_flop_note": "2 x %d FLOP per (row, query) pair: the K the MMAs execute "
                                      "per query" % k_bits,
-                    "launch_ms": scan_avg, "launches_per_step": 1,
+                    "launch_ms": scan_avg / scan_launches, "launches_per_step": scan_launches,
                     "mma_k_bits": k_bits,
                     "pairs_per_s": nq * n / (scan_avg / 1e3),
                     "db_stream_gbs": (n * 32 * passes) / (scan_avg / 1e3) / 1e9,
@@ -707,8 +718,8 @@ def run_ours(args):
                          % (B * 4 * 512 * 512 >> 20, n * 32 >> 20),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "scan_algo": ({1: "simt", 2: "b1mma"}.get(algo) or
-                                 ("tcgen05 fp4 triples" if roofline.get("kernel", "").startswith(
-                                     "scan_pair_kernel<2>") else "tcgen05 fp8"))},
+                                 {"triples": "tcgen05 fp4 triples",
+                                  "rows3": "tcgen05 fp4 row triples"}.get(form, "tcgen05 fp8"))},
         "kernels_ms": {"hash": hash_avg, "scan": scan_avg},
         "latency_ms": ({"p50": serve["points"][0]["p50_ms"], "p99": serve["points"][0]["p99_ms"],
                         "at": "serving loop, %g req/s Poisson" % serve["points"][0]["offered_req_s"]}

@@ -137,8 +137,12 @@ typedef enum {
                            database rows per accumulator column (launches of 128 queries),
                            past that three queries per column (passes of 720); above 36 FP8
                            (dot = 256 - 2 d) */
-  YPDQ_SCAN_TC_FP4 = 4  /* the FP4 forms of YPDQ_SCAN_TC at threshold <= 36 (the same choice
+  YPDQ_SCAN_TC_FP4 = 4, /* the FP4 forms of YPDQ_SCAN_TC at threshold <= 36 (the same choice
                            between them); above that the same as YPDQ_SCAN_TC */
+  YPDQ_SCAN_TC_FP8 = 5  /* tcgen05 with FP8 operands at every threshold: at threshold <= 36
+                           two queries per accumulator column (passes of 512) past 256
+                           queries and one per column (passes of up to 256) otherwise; above
+                           36 the same as YPDQ_SCAN_TC */
 } ypdq_scan_algo;
 
 /* ------------------------------------------------------------------ context */

@@ -10,7 +10,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-ALGOS = [1, 2, 3, 4]  # YPDQ_SCAN_SIMT, YPDQ_SCAN_B1MMA, YPDQ_SCAN_TC, YPDQ_SCAN_TC_FP4
+# YPDQ_SCAN_SIMT, YPDQ_SCAN_B1MMA, YPDQ_SCAN_TC, YPDQ_SCAN_TC_FP4, YPDQ_SCAN_TC_FP8
+ALGOS = [1, 2, 3, 4, 5]
 
 
 def as_tuples(h):
@@ -326,8 +327,9 @@ def test_db_file_round_trip_and_scan(ctx, yp, oracle, tmp_path):
 
 @pytest.mark.parametrize("n_q", [257, 300, 511, 512, 513, 1025])
 def test_pair_kernel_matches_oracle(ctx, yp, oracle, n_q):
-    """More than 256 queries at t <= 36 run passes of 512 queries, two per f32 accumulator
-    column (the second scaled by 512). Odd counts leave a pair with one query; rows equal or
+    """YPDQ_SCAN_TC_FP8 past 256 queries at t <= 36 runs passes of 512 queries, two per f32
+    accumulator column (the second scaled by 512); YPDQ_SCAN_TC and AUTO run the FP4 forms on
+    the same cases. Odd counts leave a pair with one query; rows equal or
     complementary to a query on the 128-bit prefix put d = +-128 in either half of a column;
     thresholds cover 0..36 at one size and the range's edges at the others."""
     rows = yp.synth.rows_128(6000, seed=n_q)
@@ -341,19 +343,21 @@ def test_pair_kernel_matches_oracle(ctx, yp, oracle, n_q):
     ts = range(37) if n_q == 513 else (0, 1, 16, 31, 35, 36)
     for t in ts:
         want = oracle.find_all(rows, q, t)
-        for algo in (3, 0):  # YPDQ_SCAN_TC, YPDQ_SCAN_AUTO
+        for algo in (5, 3, 0):  # YPDQ_SCAN_TC_FP8, YPDQ_SCAN_TC, YPDQ_SCAN_AUTO
             got = yp.scan(ctx, rows, q, t, algo=algo)
             assert np.array_equal(as_tuples(got), as_tuples(want)), (t, algo, len(got), len(want))
 
 
-@pytest.mark.parametrize("n_q", [1, 2, 3, 239, 241, 479, 719, 720, 721, 1441])
+@pytest.mark.parametrize("n_q", [513, 514, 515, 719, 720, 721, 722, 1441])
 def test_fp4_triple_kernel_matches_oracle(ctx, yp, oracle, n_q):
-    """YPDQ_SCAN_TC_FP4: block-scaled e2m1 operands (K = 64 per MMA), three queries per f32
-    accumulator column (B scale factors 2^-1, 2^7, 2^15), passes of 720 queries, the first
-    126 bits as the bound. Pass boundaries, triples with one or two queries, rows equal or
-    complementary to a query on the prefix (every field at its extreme), rows that differ from
-    a query only in the two prefix bits the bound leaves out (distance 2: found, with the
-    full distance), every threshold 0..36 at one size; above 36 the call runs the FP8 scan."""
+    """YPDQ_SCAN_TC_FP4 past 512 queries: block-scaled e2m1 operands (K = 64 per MMA), three
+    queries per f32 accumulator column (B scale factors 2^-1, 2^7, 2^15), passes of 720
+    queries, the first 126 bits as the bound (up to 512 queries the row-triple scan runs,
+    test_fp4_rows_kernel_matches_oracle). Pass boundaries, triples with one or two queries,
+    rows equal or complementary to a query on the prefix (every field at its extreme), rows
+    that differ from a query only in the two prefix bits the bound leaves out (distance 2:
+    found, with the full distance), every threshold 0..36 at one size; above 36 the call runs
+    the FP8 scan."""
     rows = yp.synth.rows_128(6000, seed=n_q + 900)
     q = yp.synth.rows_128(n_q, seed=n_q + 901)
     yp.synth.plant(rows, q, 300, 0, 40, seed=9)
@@ -372,11 +376,12 @@ def test_fp4_triple_kernel_matches_oracle(ctx, yp, oracle, n_q):
         assert np.array_equal(as_tuples(got), as_tuples(want)), (t, len(got), len(want))
 
 
-@pytest.mark.parametrize("n_q,algo,t", [(64, 3, 40), (64, 3, 31), (256, 3, 31), (300, 3, 31),
-                                         (300, 4, 31)])
+@pytest.mark.parametrize("n_q,algo,t", [(64, 3, 40), (64, 3, 31), (256, 5, 31), (300, 5, 31),
+                                         (300, 3, 31), (800, 4, 31)])
 def test_device_wait_timeout_is_reported_and_recovered(ctx, yp, oracle, n_q, algo, t):
     """The timeout path of the tensor-core scans (64 queries: queries as A, FP8 at t = 40 and
-    three rows per column, FP4, at t = 31; 256: one pass; 300: the pair kernel, FP8 and FP4).
+    three rows per column, FP4, at t = 31; 256 with YPDQ_SCAN_TC_FP8: one pass of single
+    queries; 300: FP8 pairs and three launches of row triples; 800: FP4 query triples).
     Under a 1 ms wait limit a launch whose producer issues nothing (ypdq_debug_stall_scans)
     stops with its waits run out: the stream sync reports YPDQ_ERR_TIMEOUT, and the next scan
     on the same context returns the oracle's hits. No trap, no fault, no unbounded wait."""

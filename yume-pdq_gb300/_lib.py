@@ -25,7 +25,7 @@ INPUT_F32, INPUT_U8, INPUT_RGB8, INPUT_RGBA8 = 0, 1, 2, 3
 DCT_FP32, DCT_TF32, DCT_BF16X3 = 0, 1, 2
 DIHEDRAL_EXACT, DIHEDRAL_AVX2, DIHEDRAL_SCALAR = 0, 1, 2
 SEMANTICS = {"exact": DIHEDRAL_EXACT, "avx2": DIHEDRAL_AVX2, "scalar": DIHEDRAL_SCALAR}
-SCAN_AUTO, SCAN_SIMT, SCAN_B1MMA, SCAN_TC, SCAN_TC_FP4 = 0, 1, 2, 3, 4
+SCAN_AUTO, SCAN_SIMT, SCAN_B1MMA, SCAN_TC, SCAN_TC_FP4, SCAN_TC_FP8 = 0, 1, 2, 3, 4, 5
 PDQF_T, PDQF_NEGATE_ALT_COLS, PDQF_NEGATE_ALT_ROWS, PDQF_NEGATE_OFF_DIAGONALS = 0, 1, 2, 3
 H2D, D2H, D2D = 0, 1, 2
 

@@ -459,7 +459,7 @@ ypdq_status ypdq_scan(ypdq_ctx* ctx, const uint8_t* d_rows, uint64_t n_rows,
   if (n_queries > 0 && !d_queries) return fail(YPDQ_ERR_INVALID, "d_queries is NULL");
   if (capacity > 0 && !d_hits) return fail(YPDQ_ERR_INVALID, "d_hits is NULL");
   if (threshold > 256) return fail(YPDQ_ERR_INVALID, "threshold %u > 256", threshold);
-  if (algo < YPDQ_SCAN_AUTO || algo > YPDQ_SCAN_TC_FP4)
+  if (algo < YPDQ_SCAN_AUTO || algo > YPDQ_SCAN_TC_FP8)
     return fail(YPDQ_ERR_INVALID, "algo %d", algo);
   if (!aligned16(d_rows) || !aligned16(d_queries))
     return fail(YPDQ_ERR_ALIGN, "rows and queries must be 16-byte aligned");

@@ -282,6 +282,17 @@ cudaError_t launch_scan(const ScanLaunch& p, int algo, int num_sms, cudaStream_t
     if (p.threshold <= 36) q.pair_n = kPairFp4N;  // FP4, three queries per column
     return launch_scan_tc(q, num_sms, s);
   }
+  if (algo == YPDQ_SCAN_TC_FP8) {
+    // FP8 at t <= 36 too: query pairs past 256 queries, else one pass of up to 256
+    ScanLaunch q = p;
+    if (p.threshold <= 36) {
+      if (p.n_queries > 256)
+        q.pair_n = 256;
+      else
+        q.n_tile = (p.n_queries + 63u) & ~63u;
+    }
+    return launch_scan_tc(q, num_sms, s);
+  }
   // a device-side query count needs the whole query set in one launch
   if (p.nq_dev && (algo != YPDQ_SCAN_SIMT || p.n_queries > kMaxSmemQueries))
     return cudaErrorInvalidValue;

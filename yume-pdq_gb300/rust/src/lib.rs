@@ -31,6 +31,7 @@ pub const YPDQ_SCAN_SIMT: c_int = 1;
 pub const YPDQ_SCAN_B1MMA: c_int = 2;
 pub const YPDQ_SCAN_TC: c_int = 3;
 pub const YPDQ_SCAN_TC_FP4: c_int = 4;
+pub const YPDQ_SCAN_TC_FP8: c_int = 5;
 pub const YPDQ_PDQF_T: c_int = 0;
 pub const YPDQ_PDQF_NEGATE_ALT_COLS: c_int = 1;
 pub const YPDQ_PDQF_NEGATE_ALT_ROWS: c_int = 2;
