@@ -666,6 +666,13 @@ def run_ours(args):
                            "GPU, this run)" if fp8 else "%s bf16 burst x 2 (fp8 dense)" % peak_kind)
             kernel = ("scan_pair_kernel<0> (tcgen05 kind::f8f6f4, e5m2, two queries per f32 "
                       "accumulator column)" if pairs else "scan_tc_kernel (tcgen05 kind::f8f6f4)")
+        if form == "rows3":
+            # launches of <= 128 queries stream the database once each: HBM-bound
+            launch_ms = scan_avg / scan_launches
+            achieved_gbs = (n * 32 + hits_per_step * 16.0 / scan_launches) / (launch_ms / 1e3) / 1e9
+            roofline_hbm = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak,
+                            "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                            "peak_source": peak_kind}
         roofline = {"bound": "tensor",
                     "kernel": kernel,
                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -687,6 +694,9 @@ def run_ours(args):
                     "pairs_per_s": nq * n / (scan_avg / 1e3),
                     "db_stream_gbs": (n * 32 * passes) / (scan_avg / 1e3) / 1e9,
                     "query_passes": passes}
+        if form == "rows3":
+            roofline.update(roofline_hbm)
+            roofline["mma_flop_note"] += " (the launch is bound by its database stream)"
     elif scan_avg >= hash_avg:
         # SIMT scan: one launch reads the whole database once for up to 2048 queries
         dom_ms = scan_avg / scan_launches
