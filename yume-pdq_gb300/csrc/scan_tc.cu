@@ -1695,13 +1695,14 @@ __global__ void __launch_bounds__(threads_of(false), 1) scan_rows_kernel(const P
 }
 
 // ---------------------------------------------------------------------------------------
-// scan_rows3_kernel: narrow passes (<= 128 queries) at t <= 36 with three database rows per
-// f32 accumulator column and block-scaled FP4 operands.
+// scan_rows3_kernel: narrow passes (<= 128 queries a launch; the launcher runs up to 512 as
+// launches of 128) at t <= 36 with three database rows per f32 accumulator column and
+// block-scaled FP4 operands.
 //
 // The triple form of scan_pair_kernel with the operands swapped: the queries (126-bit
 // prefixes) are A, M = 128 lanes, expanded once per launch; a tile of 720 database rows is B,
-// rows 3j, 3j + 1 and 3j + 2 in column j (bytes 0-63 and 64-127 of row j of B chunk 0, bytes
-// 0-63 of row j of chunk 1, with B scales 2^-1, 2^7 and 2^15). Column j of lane q then holds
+// rows 3j, 3j + 1 and 3j + 2 in column j (fields a, b and c: see the chunk layout below, with
+// B scales 2^-1, 2^7 and 2^15). Column j of lane q then holds
 // e_a + 256 e_b + 65536 e_c over the decoding constant, e = 63 - (distance over the prefix),
 // decoded by the same bit tests. Per database row the tensor core runs 6 MMAs of N = 240 for
 // 720 rows (~1.4 clk) where scan_rows_kernel runs 4 FP8 MMAs of N = 256 for 256 rows (~2 clk),
