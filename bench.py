@@ -285,41 +285,21 @@ def setup_workload(yp, ctx, args, rank):
     return batch, d_img, rows, d_rows, d_hash, d_q
 
 
-def serve_run(yp, srv, pool, rate, seconds, rng, hit_cap=4096):
+def serve_run(yp, srv, pool, rate, seconds, rng, hit_cap=1024):
     """Open-loop Poisson arrivals at `rate` req/s (rate None: submit whenever the queue has
-    room, i.e. saturation) of log-uniform 1..64-image requests sliced from `pool`. Returns
-    the server's window statistics once every accepted request has completed."""
-    import gc
+    room, i.e. saturation) of log-uniform 1..64-image requests sliced from `pool`, for
+    `seconds`. The arrival times are drawn here and the requests submitted by the library's
+    native load generator (ypdq_server_replay), so no pause of this interpreter shifts an
+    arrival. Returns the server's window statistics once every accepted request has
+    completed."""
     n_pool = pool.shape[0]
-    # the arrivals come from this loop: a collector pause would submit the requests it owes
-    # at once, a burst the arrival process does not have
-    gc.collect()
-    gc.disable()
+    m = int((rate if rate is not None else 20000.0) * seconds * 1.25) + 16
+    n = np.minimum(64, np.maximum(1, np.exp(rng.uniform(0.0, np.log(65.0), m)).astype(np.int64)))
+    first = rng.integers(0, n_pool - n + 1)
+    arrival = (None if rate is None else
+               (np.cumsum(rng.exponential(1.0 / rate, m)) * 1e9).astype(np.uint64))
     srv.stats(reset=True)
-    t0 = time.perf_counter()
-    t_next = t0
-    offered = rejected = 0
-    while True:
-        now = time.perf_counter()
-        if now - t0 >= seconds:
-            break
-        if rate is not None and now < t_next:
-            # spin: a thread that sleeps until the next arrival can wake late and then submit
-            # the requests it owes at once (a burst the arrival process does not have)
-            srv.poll(timeout_us=0)
-            continue
-        n = int(min(64, max(1, np.exp(rng.uniform(0.0, np.log(65.0))))))
-        s0 = int(rng.integers(0, n_pool - n + 1))
-        rid = srv.try_submit(pool[s0:s0 + n], hit_capacity=hit_cap)
-        if rate is not None:
-            offered += 1
-            rejected += rid is None
-            t_next += rng.exponential(1.0 / rate)
-        elif rid is None:
-            srv.poll(timeout_us=200)
-        srv.poll(timeout_us=0)
-    srv.drain()
-    gc.enable()
+    srv.replay(pool, first, n, arrival, duration_s=seconds, hit_capacity=hit_cap)
     st = srv.stats()
     return {"offered_req_s": rate, "seconds": round(st["elapsed_s"], 3),
             "completed_req_s": st["completed"] / st["elapsed_s"],

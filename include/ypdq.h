@@ -465,6 +465,24 @@ ypdq_status ypdq_server_submit(ypdq_server *srv, const void *h_images, uint32_t 
  * is there or nothing is pending). Thread-safe. */
 ypdq_status ypdq_server_poll(ypdq_server *srv, ypdq_completion *out, uint32_t max,
                              uint32_t *n_out, int64_t timeout_us);
+/*
+ * Load generator for measurement: submits requests from the calling thread (native, so no
+ * interpreter pause of a caller delays an arrival) and takes their completions meanwhile.
+ * Request i is images first[i] .. first[i] + n_images[i] - 1 of h_pool (pool_images images
+ * of the configured input kind, pinned), submitted arrival_ns[i] ns after the call starts
+ * (open loop: an arrival that finds the queue full is lost and counted in *n_rejected), or,
+ * with arrival_ns NULL, as soon as the queue has room (closed loop: a full queue is waited
+ * for and counted). Submission stops after n_requests requests or duration_ns ns; the call
+ * returns once every submitted request has completed. Request i's hits go to h_hits +
+ * i * hit_capacity (NULL with hit_capacity 0: counts only) and its true hit count to
+ * n_hits[i] (may be NULL). No other request of the server may be in flight meanwhile. The
+ * server's statistics window (ypdq_server_get_stats) covers the replay.
+ */
+ypdq_status ypdq_server_replay(ypdq_server *srv, const void *h_pool, uint32_t pool_images,
+                               const uint32_t *first, const uint32_t *n_images,
+                               const uint64_t *arrival_ns, uint32_t n_requests,
+                               uint64_t duration_ns, ypdq_hit *h_hits, uint64_t hit_capacity,
+                               uint64_t *n_hits, uint64_t *n_submitted, uint64_t *n_rejected);
 /* Latency percentiles, counters and the bucket table; reset != 0 starts a new window. */
 ypdq_status ypdq_server_get_stats(ypdq_server *srv, ypdq_server_stats *out, int reset);
 /* Finishes every queued and in-flight request, stops the worker and frees the slots.

@@ -202,3 +202,31 @@ def test_rgba_requests(ctx, yp, workload):
         res = {r.tag: r for r in srv.drain()}
     assert np.array_equal(res[0].hits, yp.screen_host(ctx, db, rgba[:4], threshold=31))
     assert np.array_equal(res[1].hits, yp.screen_host(ctx, db, rgba[4:], threshold=31))
+
+
+def test_native_replay(ctx, yp, workload):
+    """ypdq_server_replay, the native load generator: an open-loop trace (arrivals spread over
+    20 ms) and a closed loop over the same requests. Every request completes, its hits (in
+    (index, query) order, query numbers local to the request) equal ypdq_screen_host's on its
+    images, its true hit count is reported, and the server's window counts the requests."""
+    imgs, rows, db = workload
+    rng = np.random.default_rng(1290)
+    reqs = request_slices(rng, 24)
+    first = np.array([s for s, _ in reqs])
+    n = np.array([k for _, k in reqs])
+    want = [yp.screen_host(ctx, db, imgs[s:s + k], threshold=31) for s, k in reqs]
+    cap = max(len(w) for w in want) + 8
+    with yp.Server(ctx, db, max_step_images=64, slots=2, max_queued_images=4096) as srv:
+        for arrival in (np.sort(rng.integers(0, 20_000_000, len(reqs))), None):
+            srv.stats(reset=True)
+            sub, rej, n_hits, hits = srv.replay(imgs, first, n, arrival, duration_s=10.0,
+                                                hit_capacity=cap)
+            assert (sub, rej) == (len(reqs), 0)
+            st = srv.stats()
+            assert st["completed"] == len(reqs) and st["images_completed"] == n.sum()
+            for i, w in enumerate(want):
+                assert n_hits[i] == len(w), i
+                assert np.array_equal(hits[i, :len(w)], w), i
+        # a pool range outside the pool is refused before anything is submitted
+        with pytest.raises(yp.YpdqError):
+            srv.replay(imgs, np.array([POOL - 1]), np.array([2]))

@@ -128,6 +128,8 @@ SIGNATURES = {
     "ypdq_server_config_default": (i32, [ctypes.POINTER(ServerConfig)]),
     "ypdq_server_create": (i32, [P, P, ctypes.POINTER(ServerConfig), PP]),
     "ypdq_server_submit": (i32, [P, P, u32, P, u64, P, P, u64, ctypes.POINTER(ctypes.c_uint64)]),
+    "ypdq_server_replay": (i32, [P, P, u32, P, P, P, u32, u64, P, u64, P,
+                                 ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "ypdq_server_poll": (i32, [P, ctypes.POINTER(Completion), u32, ctypes.POINTER(ctypes.c_uint32),
                                i64]),
     "ypdq_server_get_stats": (i32, [P, ctypes.POINTER(ServerStats), i32]),

@@ -645,6 +645,70 @@ ypdq_status ypdq_server_poll(ypdq_server* S, ypdq_completion* out, uint32_t max,
   return YPDQ_OK;
 }
 
+ypdq_status ypdq_server_replay(ypdq_server* S, const void* h_pool, uint32_t pool_images,
+                               const uint32_t* first, const uint32_t* n_images,
+                               const uint64_t* arrival_ns, uint32_t n_requests,
+                               uint64_t duration_ns, ypdq_hit* h_hits, uint64_t hit_capacity,
+                               uint64_t* n_hits, uint64_t* n_submitted, uint64_t* n_rejected) {
+  if (!S || !h_pool || !first || !n_images || !n_submitted || !n_rejected ||
+      (hit_capacity && !h_hits))
+    return fail(YPDQ_ERR_INVALID, "NULL argument");
+  for (uint32_t i = 0; i < n_requests; ++i)
+    if (n_images[i] == 0 || first[i] > pool_images || n_images[i] > pool_images - first[i])
+      return fail(YPDQ_ERR_INVALID, "request %u: images %u..%u outside the pool of %u", i,
+                  first[i], first[i] + n_images[i], pool_images);
+  const uint8_t* pool = static_cast<const uint8_t*>(h_pool);
+  std::vector<ypdq_completion> comp(256);
+  uint64_t submitted = 0, rejected = 0, done = 0;
+  const Clock::time_point t0 = Clock::now();
+  auto elapsed_ns = [&] {
+    return static_cast<uint64_t>(
+        std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count());
+  };
+  auto take = [&](int64_t timeout_us) -> ypdq_status {
+    uint32_t got = 0;
+    const ypdq_status st = ypdq_server_poll(S, comp.data(), static_cast<uint32_t>(comp.size()),
+                                            &got, timeout_us);
+    for (uint32_t c = 0; c < got; ++c)
+      if (n_hits && comp[c].user_tag < n_requests) n_hits[comp[c].user_tag] = comp[c].n_hits;
+    done += got;
+    return st;
+  };
+  uint32_t i = 0;
+  while (i < n_requests) {
+    const uint64_t now = elapsed_ns();
+    if (now >= duration_ns) break;
+    if (arrival_ns && now < arrival_ns[i]) {
+      // spin until the next arrival, taking completions meanwhile
+      if (ypdq_status st = take(0)) return st;
+      continue;
+    }
+    ypdq_hit* hits = hit_capacity ? h_hits + static_cast<uint64_t>(i) * hit_capacity : nullptr;
+    const ypdq_status st =
+        ypdq_server_submit(S, pool + static_cast<uint64_t>(first[i]) * S->image_bytes,
+                           n_images[i], hits, hit_capacity, nullptr, nullptr, i, nullptr);
+    if (st == YPDQ_OK) {
+      ++submitted;
+      ++i;
+    } else if (st == YPDQ_ERR_BUSY) {
+      ++rejected;
+      if (arrival_ns) {
+        ++i;  // an open-loop arrival that finds the queue full is lost
+      } else if (ypdq_status st2 = take(200)) {  // closed loop: wait for room, then retry
+        return st2;
+      }
+    } else {
+      return st;
+    }
+    if (ypdq_status st2 = take(0)) return st2;
+  }
+  while (done < submitted)
+    if (ypdq_status st = take(-1)) return st;
+  *n_submitted = submitted;
+  *n_rejected = rejected;
+  return YPDQ_OK;
+}
+
 ypdq_status ypdq_server_get_stats(ypdq_server* S, ypdq_server_stats* o, int reset) {
   if (!S || !o) return fail(YPDQ_ERR_INVALID, "NULL argument");
   std::lock_guard<std::mutex> lk(S->mu);

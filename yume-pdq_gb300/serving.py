@@ -142,6 +142,33 @@ class Server:
                               c.step))
         return out
 
+    def replay(self, pool, first, n_images, arrival_ns=None, duration_s=1e9, hit_capacity=0):
+        """ypdq_server_replay: requests of pool[first[i] : first[i] + n_images[i]] submitted
+        from native code at arrival_ns[i] ns after the call starts (None: as soon as the
+        queue has room) until duration_s; returns (submitted, rejected, n_hits) once all
+        submitted requests have completed (n_hits[i]: request i's true hit count). With
+        hit_capacity > 0 also the hit buffers, one row per request. No other request of this
+        server may be in flight meanwhile."""
+        self._check_images(pool)
+        first = np.ascontiguousarray(first, np.uint32)
+        n_images = np.ascontiguousarray(n_images, np.uint32)
+        if first.shape != n_images.shape:
+            raise ValueError("first and n_images differ in length")
+        arr = None if arrival_ns is None else np.ascontiguousarray(arrival_ns, np.uint64)
+        if arr is not None and arr.shape != first.shape:
+            raise ValueError("arrival_ns and first differ in length")
+        hits = (np.zeros((len(first), int(hit_capacity)), HIT_DTYPE) if hit_capacity
+                else None)
+        n_hits = np.zeros(len(first), np.uint64)
+        sub, rej = ctypes.c_uint64(), ctypes.c_uint64()
+        check(self.ctx.lib.ypdq_server_replay(
+            self.handle, ptr(pool), pool.shape[0], ptr(first), ptr(n_images), ptr(arr),
+            len(first), int(duration_s * 1e9), ptr(hits), int(hit_capacity), ptr(n_hits),
+            ctypes.byref(sub), ctypes.byref(rej)))
+        if hits is not None:
+            return sub.value, rej.value, n_hits, hits
+        return sub.value, rej.value, n_hits
+
     def drain(self, timeout_us=-1):
         """Poll until every submitted request has completed."""
         out = []
