@@ -469,8 +469,9 @@ ypdq_status ypdq_server_poll(ypdq_server *srv, ypdq_completion *out, uint32_t ma
  * Load generator for measurement: submits requests from the calling thread (native, so no
  * interpreter pause of a caller delays an arrival) and takes their completions meanwhile.
  * Request i is images first[i] .. first[i] + n_images[i] - 1 of h_pool (pool_images images
- * of the configured input kind, pinned), submitted arrival_ns[i] ns after the call starts
- * (open loop: an arrival that finds the queue full is lost and counted in *n_rejected), or,
+ * of the configured input kind; pinned memory copies fastest). Requests go in index order,
+ * request i arrival_ns[i] ns after the call starts (non-decreasing times; open loop: an
+ * arrival that finds the queue full is lost and counted in *n_rejected), or,
  * with arrival_ns NULL, as soon as the queue has room (closed loop: a full queue is waited
  * for and counted). Submission stops after n_requests requests or duration_ns ns; the call
  * returns once every submitted request has completed. Request i's hits go to h_hits +
