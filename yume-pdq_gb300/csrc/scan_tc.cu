@@ -1720,10 +1720,10 @@ constexpr int kRows3ChunkBytes = kRows3Cols * 128;  // one B chunk (240 rows x 1
 // Three expanded tiles in five chunks of 240 rows x 128 B, every byte used: stage s's fields
 // a and b are chunk s (bytes 0-63 and 64-127 of row j); the fields c of stages 0 and 1 are
 // chunk 3 (bytes 0-63 and 64-127), that of stage 2 bytes 0-63 of chunk 4, whose bytes
-// 64-127 of rows 0-127 hold the queries (A). Three stages let the expanders fill a tile while
-// the MMAs of the two before it run (with two, the slowest expander warp, which shares its
-// scheduler with epilogue warps, sat on the MMA chain: ~2,000 clk a tile against ~1,000 of
-// MMAs); the five chunks leave room for three packed tiles in flight.
+// 64-127 of rows 0-127 hold the queries (A). Three stages let the expanders run up to two
+// tiles ahead of the MMAs (an expander warp that shares its scheduler with busy epilogue
+// warps runs slower than the others); the five chunks leave room for three packed tiles in
+// flight.
 constexpr int kRows3BStages = 3;
 constexpr int kRows3BChunks = 5;
 static_assert(kRows3ChunkBytes % 1024 == 0, "B chunks stay 1024-byte aligned");
